@@ -1,0 +1,315 @@
+"""Benchmark: FP64 merge-path SpMV and power method on the 4096x4096-grid
+2D Poisson matrix (N = 16,777,216, nnz = 83,869,696), GB300.
+
+One step = one SpMV y = A x over the whole matrix (the benchmark spec's plain FP64
+merge-path SpMV, reported as GB/s against the HBM roofline).  Inputs are
+larger than L2 (1.34 GB of matrix and vectors per pass), so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  N > 1 runs independent replicas, one per GPU
+(the path does not shard on this single-GPU pool): value = all ranks' bytes /
+max time over ranks.
+
+--impl reference times the reference's CPU path (CRSOMP::mv restated in the C
+oracle, OpenMP over all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMV GB/s vs HBM peak; power-method solves/s, p50/p99 @1e-10, mixed vs FP64"
+GRID = 4096
+NOMINAL_HBM_GBS = 8000.0
+
+
+def algorithmic_bytes(N, nnz, vbytes=8, xbytes=8):
+    """12 B per nonzero (value + int32 column), int32 row_start, x read once,
+    y written once."""
+    return (vbytes + 4) * nnz + 4 * (N + 1) + xbytes * N + xbytes * N
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                return json.load(f)
+        except Exception:
+            return {}
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline_sample(A, x, threads, seconds=10.0):
+    """The reference's CRSOMP::mv (restated in the oracle) on the host cores."""
+    from oracle import pyoracle as O
+    O.crs_omp_mv(A, x, threads)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.crs_omp_mv(A, x, threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > seconds or reps >= 50:
+            break
+    return el / reps, reps
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU SpMV on the host cores."""
+    if rank != 0:
+        return
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    A = O.fill_poisson(GRID, GRID)
+    x = np.random.default_rng(20261203).random(A.noc)
+    for _ in range(max(args.warmup, 1)):
+        O.crs_omp_mv(A, x, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.crs_omp_mv(A, x, threads)
+    el = time.perf_counter() - t0
+    ms = el / args.steps * 1e3
+    B = algorithmic_bytes(A.nor, A.nnz)
+    gbs = B / (ms * 1e-3) / 1e9
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "poisson2d_4096x4096_fp64_spmv", "N": A.nor, "nnz": A.nnz,
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": "%d full SpMVs (CRSOMP::mv restated in oracle/oracle.c, OpenMP dynamic,512)"
+                                   % args.steps},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import thesis_spmv_gb300 as pwm
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    M = pwm.CRSCuda(1)
+    M.generatePoissonMatrix(GRID, GRID, 1)
+    N, _, nnz = M.dims()
+    B = algorithmic_bytes(N, nnz)
+    tm, ntiles, grid = M.tile_info()
+
+    stream = torch.cuda.Stream(device=dev)
+    M.set_stream(stream.cuda_stream)
+    g = torch.Generator(device="cpu").manual_seed(20261203)
+    x_host = torch.rand(N, dtype=torch.float64, generator=g)
+    dx = x_host.to(dev)
+    dy = torch.zeros(N, dtype=torch.float64, device=dev)
+
+    # ---- device-resident SpMV (value) ----
+    for _ in range(args.warmup):
+        M.mv_device(dx.data_ptr(), dy.data_ptr())
+    stream.synchronize()
+    barrier(world)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            M.mv_device(dx.data_ptr(), dy.data_ptr())
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    ms_total = ev0.elapsed_time(ev1)
+    barrier(world)
+    ms_total = max_over_ranks(ms_total, world)
+    ms = ms_total / args.steps
+    value = B * world / (ms * 1e-3) / 1e9
+
+    # ---- power method: 500 iterations (reference powerIteration semantics) ----
+    p_it = args.power_iters
+    px = dx.clone()
+    py = torch.zeros_like(dx)
+    M.power_device(px.data_ptr(), py.data_ptr(), 4)
+    stream.synchronize()
+    px.copy_(dx)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    M.power_device(px.data_ptr(), py.data_ptr(), p_it)
+    e1.record(stream)
+    e1.synchronize()
+    power_ms = e0.elapsed_time(e1)
+
+    # ---- end to end through the C ABI with host buffers (pinned) ----
+    xh = x_host.pin_memory()
+    yh = torch.zeros(N, dtype=torch.float64).pin_memory()
+    xn = xh.numpy()
+    yn_ = yh.numpy()
+    M.mv(xn, yn_)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 50))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        M.mv(xn, yn_)  # H2D x, SpMV, D2H y, synchronous
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_gbs = B * world / e2e_s / 1e9
+
+    peak, peak_kind = measured_peaks()
+    traffic = profile_traffic().get("k_merge_spmv_f64_poisson4096")
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "poisson2d_4096x4096_fp64_spmv", "N": N, "nnz": nnz,
+                   "l2": "inputs larger than L2 (1.34 GB per pass)", "items_per_tile": tm, "tiles": ntiles,
+                   "grid": grid, "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": round(B / (ms * 1e-3) / 1e9, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(B / (ms * 1e-3) / 1e9 / peak, 4), "traffic": traffic,
+                     "peak_source": peak_kind, "frac_of_nominal_8TBs": round(B / (ms * 1e-3) / 1e9 / NOMINAL_HBM_GBS, 4),
+                     "algorithmic_bytes_per_launch": B, "timed": "k_merge_spmv + k_merge_fixup (one SpMV)"},
+        "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
+                "ms_per_step": round(e2e_s * 1e3, 4), "api": "pwmgpu_mv (host arrays, pinned)"},
+        "gpu_launches": 2 * args.steps,
+        "power": {"iterations": p_it, "ms_per_iteration": round(power_ms / p_it, 5),
+                  "gb_s": round(B / (power_ms / p_it * 1e-3) / 1e9, 2), "kernels_per_iteration": 2},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import pyoracle as O
+        A = O.fill_poisson(GRID, GRID)
+        threads = os.cpu_count() or 1
+        s, reps = cpu_baseline_sample(A, x_host.numpy(), threads)
+        result["cpu_baseline"] = {"value": round(B / s / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                                  "sample": "%d full SpMVs of the same matrix (CRSOMP::mv restated in oracle/oracle.c)"
+                                            % reps}
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--power-iters", type=int, default=500)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, world, rank)
+        return
+    world, rank, local = dist_setup(args.gpus)
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+/*
+ * pwmgpu.h -- C ABI of the GB300 (sm_103a) SpMV / power-method library.
+ *
+ * This is the drop-in boundary for KobeBergmans/Thesis_SPMV's operator
+ * interface pwm::SparseMatrix<T,int_type> (Matrix/SparseMatrix.hpp:13-68).
+ * Each entry point names the reference interface it replaces.  All entry
+ * points are extern "C", take plain pointers and sizes, return an int status
+ * (PWMGPU_OK == 0) and never abort; pwmgpu_last_error() gives the message of
+ * the calling thread's last failure.
+ *
+ * Index arrays are 32-bit.  The reference instantiates int_type as int,
+ * unsigned int and uint32_t (Util/Constants.hpp:38, Tests/poisson.cpp:28,146);
+ * all three have the same bits for sizes below 2^31, which the library
+ * enforces (nor + nnz < 2^31).
+ *
+ * Host-array calls (pwmgpu_mv, pwmgpu_power, pwmgpu_solve) are synchronous:
+ * results are final on return, as in the reference.  *_device calls take
+ * device pointers and are asynchronous on the handle's stream.
+ */
+#ifndef PWMGPU_H
+#define PWMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PWMGPU_OK 0
+#define PWMGPU_ERR_INVALID 1    /* bad argument: null pointer, bad size, index out of range */
+#define PWMGPU_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define PWMGPU_ERR_NOMEM 3      /* device allocation failed */
+#define PWMGPU_ERR_TIMEOUT 4    /* a bounded device-side wait gave up */
+#define PWMGPU_ERR_STATE 5      /* no matrix loaded / call out of order */
+#define PWMGPU_ERR_NOT_SQUARE 6 /* power method on a non-square matrix (CRS.hpp:119 asserts) */
+#define PWMGPU_ERR_BUDGET 7     /* service admission refused: over the HBM budget */
+#define PWMGPU_ERR_NUMERIC 8    /* zero or non-finite norm met by the power method */
+#define PWMGPU_ERR_UNSUPPORTED 9
+
+/* ---- storage formats (the reference's method numbers 8, 9, 10 in
+ *      Util/DriverUtil.hpp:67-74 selectType) ---- */
+#define PWMGPU_FMT_MERGE 0 /* CRS, merge-path SpMV (SOA_Implementations/CRS_Merge.hpp) */
+#define PWMGPU_FMT_CSB 1   /* compressed sparse blocks (SOA_Implementations/CSB.hpp) */
+#define PWMGPU_FMT_COH 2   /* row-distributed Hilbert block CO-H (SOA_Implementations/BlockCOH.hpp) */
+
+/* ---- precision of a power solve ---- */
+#define PWMGPU_PREC_F64 0   /* FP64 values, vectors and accumulation */
+#define PWMGPU_PREC_F32 1   /* FP32 values and vectors, FP32 accumulation, FP64 reductions */
+#define PWMGPU_PREC_MIXED 2 /* FP32 (or exact BF16) bulk phase, then FP64 refinement */
+
+typedef struct pwmgpu_matrix pwmgpu_matrix;
+
+/* Message of the calling thread's last failing call ("" if none). */
+const char* pwmgpu_last_error(void);
+
+/* Device facts for the current device. */
+int pwmgpu_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes);
+
+/* Replaces the reference constructors `CRS_Merge(int threads)`,
+ * `CSB(int threads)`, `BlockCOH(int threads)` (SparseMatrix.hpp:30).
+ * `partitions` is the reference's thread count where the format's layout
+ * depends on it (CO-H row partitions, BlockCOH.hpp:325-355); the GPU kernels
+ * do not depend on it otherwise.  The handle owns a CUDA stream. */
+int pwmgpu_create(int format, int partitions, pwmgpu_matrix** out);
+/* Replaces the virtual destructor (SparseMatrix.hpp:33). */
+int pwmgpu_destroy(pwmgpu_matrix* m);
+/* Use `stream` (a cudaStream_t, may be NULL for the legacy stream) for all
+ * later work of this handle instead of its own stream. */
+int pwmgpu_set_stream(pwmgpu_matrix* m, void* stream);
+
+/* Replaces generatePoissonMatrix(m, n, partitions) (SparseMatrix.hpp:41,
+ * CRS.hpp:60-74, CSB.hpp:576-582, BlockCOH.hpp:464-470).  The merge format
+ * writes the CRS arrays on the device in Util/Poisson.hpp:32-83 order. */
+int pwmgpu_generate_poisson(pwmgpu_matrix* m, int32_t mx, int32_t ny);
+/* Upload a host CRS matrix (rows sorted, columns ascending within a row). */
+int pwmgpu_load_csr(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
+                    const int32_t* col_ind, const double* vals);
+/* Replaces loadFromTriplets(input, partitions) (SparseMatrix.hpp:48).  Like
+ * the reference (Util/TripletToCRS.hpp:139-142) it sorts the caller's
+ * triplet arrays in place (by row, then column). */
+int pwmgpu_load_triplets(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, int32_t* rows, int32_t* cols,
+                         double* vals);
+int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz);
+/* Copy the device CRS arrays back (row_start[nor+1], col_ind[nnz], vals[nnz]);
+ * the reference's protected row_start / col_ind / data_arr (CRS.hpp:30-37). */
+int pwmgpu_get_csr(pwmgpu_matrix* m, int32_t* row_start, int32_t* col_ind, double* vals);
+
+/* Replaces mv(x, y) (SparseMatrix.hpp:57, CRS.hpp:99-109): y = A x with
+ * caller-owned host arrays x[noc], y[nor]; synchronous. */
+int pwmgpu_mv(pwmgpu_matrix* m, const double* x, double* y);
+/* y = A x with device arrays (x[noc], y[nor] must not overlap);
+ * asynchronous on the handle's stream. */
+int pwmgpu_mv_device(pwmgpu_matrix* m, const double* dx, double* dy);
+/* FP32 SpMV with device arrays: values converted to FP32 once, FP32
+ * accumulation. */
+int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy);
+
+/* Replaces powerIteration(x, y, it) (SparseMatrix.hpp:66, CRS.hpp:118-130):
+ * `it` times y = A x, y /= ||y||, roles swapped; the result is in x when `it`
+ * is even and in y when it is odd, the other array holds the previous
+ * iterate (the untouched input for it == 1), as in the reference.  Host
+ * arrays of length nor; synchronous.  FP64. */
+int pwmgpu_power(pwmgpu_matrix* m, double* x, double* y, int32_t it);
+/* Same on device arrays; the kernel sequence is asynchronous. */
+int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
+
+/* Power solve with an eigenvalue estimate, the eigen-residual and a stopping
+ * test (not in the reference: the benchmark spec extension).  x (host, length nor)
+ * holds the start vector on entry and the normalised eigenvector estimate on
+ * return.  Iterates until ||A u - lambda u|| / |lambda| <= tol or max_it
+ * iterations.  precision: PWMGPU_PREC_*.  lambda is the Rayleigh quotient
+ * u^T A u of the returned u (||u|| = 1). */
+typedef struct {
+    int32_t iterations;     /* total SpMVs performed */
+    int32_t iterations_low; /* of which in the FP32/BF16 phase */
+    int32_t converged;      /* 1 if the residual test was met */
+    int32_t precision;      /* the PWMGPU_PREC_* used */
+    double lambda;          /* Rayleigh quotient of the returned vector */
+    double residual;        /* ||A u - lambda u|| / |lambda| of the returned vector */
+} pwmgpu_solve_info;
+int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info);
+
+/* The merge-path coordinates the reference's CRS_Merge::mv uses for `parts`
+ * threads (CRS_Merge.hpp:96-107 diagonals, :42-62 searchPathOnDiag),
+ * computed on the device by the kernel that partitions the merge path:
+ * coords[2*t], coords[2*t+1] = (row, nonzero) for t = 0..parts. */
+int pwmgpu_merge_partition(pwmgpu_matrix* m, int32_t parts, int32_t* coords);
+/* Tile size (merge items per tile) and tile count used by the SpMV kernel. */
+int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PWMGPU_H */

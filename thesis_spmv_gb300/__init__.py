@@ -1,0 +1,9 @@
+"""GB300-native (sm_103a) SpMV and power-method library.
+
+A from-scratch GPU implementation of the hot path of KobeBergmans/Thesis_SPMV
+(merge-path CRS SpMV, CSB and CO-H variants, the power method) behind the
+reference's pwm::SparseMatrix interface.  The compute lives in
+libpwmgpu.so (C ABI: include/pwmgpu.h); this package is its Python front end.
+"""
+from ._lib import PwmGpuError, lib, lib_path  # noqa: F401
+from .matrix import COHCuda, CRSCuda, CSBCuda, CudaSparseMatrix, Triplet, selectType  # noqa: F401

@@ -1,0 +1,141 @@
+// common.cuh -- device helpers shared by the pwmgpu kernels (sm_103a).
+//
+// * TMA 1D bulk copies (cp.async.bulk) completing on an mbarrier.
+// * Bounded mbarrier waits: every wait gives up after a clock64 budget, sets
+//   the launch's status word and lets the kernel return (no trap, no hang).
+// * Exact power-of-two rescaling done on the exponent field (integer pipe),
+//   so the power method never spends an FP64 multiply per row on scaling:
+//   on GB300 the FP64 pipe (about 1.9 DFMA/clk/SM) is a co-bottleneck with HBM.
+#pragma once
+#include <cmath>
+#include <cstring>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include "pwmgpu.h"
+
+namespace pwmgpu {
+
+// Largest clock64 interval any spin-wait may take before it reports
+// PWMGPU_ERR_TIMEOUT (about 2 s at the 2.07 GHz maximum SM clock).
+constexpr long long kWaitCycles = 4000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Arrive (count 1) and announce `bytes` of asynchronous transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.  Returns false (and records the timeout)
+// when the budget runs out; the caller then leaves the kernel.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kWaitCycles) {
+            atomicCAS(status, PWMGPU_OK, PWMGPU_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// L2 eviction policy for data read exactly once per pass (the matrix stream):
+// evict-first keeps the gathered vector resident in L2 instead.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// 1D bulk copy global -> shared (TMA engine).  dst, src 16-byte aligned, bytes
+// a non-zero multiple of 16.  Completion is signalled on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                         uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
+// ---- exact scaling by 2^e ------------------------------------------------
+// Multiplying by a power of two is exact unless the result leaves the normal
+// range; the normal case is an integer add on the exponent field.  Zeros,
+// subnormals, infinities, NaNs and out-of-range results take an FP multiply.
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+    long long bits = __double_as_longlong(v);
+    int ex = (int)((bits >> 52) & 0x7FF);
+    int ne = ex + e;
+    if (ex != 0 && ex != 0x7FF && ne > 0 && ne < 0x7FF) return __longlong_as_double(bits + ((long long)e << 52));
+    return v * ldexp(1.0, e);
+}
+
+__device__ __forceinline__ float scale_pow2(float v, int e) {
+    int bits = __float_as_int(v);
+    int ex = (bits >> 23) & 0xFF;
+    int ne = ex + e;
+    if (ex != 0 && ex != 0xFF && ne > 0 && ne < 0xFF) return __int_as_float(bits + (e << 23));
+    return v * ldexpf(1.0f, e);
+}
+
+// Exponent e that brings a vector with squared norm `nsq` to a norm in
+// [1, 2) when scaled by 2^e, computed from the exponent field only
+// (nsq = m * 2^q with m in [0.5, 1) gives e = -floor((q - 1) / 2)).  Zero,
+// subnormal and non-finite inputs give 0: no rescaling.
+__host__ __device__ __forceinline__ int pow2_exponent_from_nsq(double nsq) {
+    long long bits;
+#ifdef __CUDA_ARCH__
+    bits = __double_as_longlong(nsq);
+#else
+    std::memcpy(&bits, &nsq, sizeof bits);
+#endif
+    int ex = (int)((bits >> 52) & 0x7FF);
+    if (bits <= 0 || ex == 0 || ex == 0x7FF) return 0;
+    int q = ex - 1022;  // frexp exponent of a normal positive double
+    int h = q - 1;
+    int fl = (h >= 0) ? h / 2 : -((-h + 1) / 2);  // floor(h / 2)
+    return -fl;
+}
+
+// ---- value conversions ---------------------------------------------------
+template <typename T> __device__ __forceinline__ double to_f64(T v);
+template <> __device__ __forceinline__ double to_f64<double>(double v) { return v; }
+template <> __device__ __forceinline__ double to_f64<float>(float v) { return (double)v; }
+template <> __device__ __forceinline__ double to_f64<__nv_bfloat16>(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
+
+template <typename T> __device__ __forceinline__ float to_f32(T v);
+template <> __device__ __forceinline__ float to_f32<double>(double v) { return (float)v; }
+template <> __device__ __forceinline__ float to_f32<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f32<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+}  // namespace pwmgpu

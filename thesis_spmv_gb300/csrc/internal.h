@@ -1,0 +1,67 @@
+// internal.h -- declarations shared by the host side (pwmgpu.cpp) and the
+// kernel translation units.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pwmgpu.h"
+
+namespace pwmgpu {
+
+// Device CRS view (row_start[nor+1], col[nnz], val[nnz]; each array padded by
+// kArrayPad elements past its end).
+struct DevMatrix {
+    int32_t nor = 0, noc = 0;
+    long long nnz = 0;
+    int32_t* row_start = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+};
+
+enum { kModeSpmv = 0, kModePower = 1 };
+
+// merge.cu
+int merge_items_per_tile(int cfg);
+int merge_items_per_tile_f32();
+int merge_grid(int cfg, int num_tiles, int sm_count);
+int merge_grid_f32(int num_tiles, int sm_count, bool bf16);
+int fixup_grid(int num_tiles, int sm_count);
+int dot_grid(long long n, int sm_count);
+cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
+                                   int2* out, cudaStream_t st);
+cudaError_t launch_merge_spmv_f64(int cfg, int mode, const DevMatrix& M, const int2* tiles, int num_tiles, int grid,
+                                  const double* x, double* y, double* carries, const double* nsq_in,
+                                  double* partials, int* status, cudaStream_t st);
+cudaError_t launch_merge_spmv_f32(int mode, const DevMatrix& M, const void* val, bool bf16, const int2* tiles,
+                                  int num_tiles, int grid, const float* x, float* y, float* carries,
+                                  const double* nsq_in, double* partials, int* status, cudaStream_t st);
+cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
+                                   const double* carries, const double* nsq_in, const double* spmv_partials,
+                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
+                                   double* nsq_out, cudaStream_t st);
+cudaError_t launch_merge_fixup_f32(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, float* y,
+                                   const float* carries, const double* nsq_in, const double* spmv_partials,
+                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
+                                   double* nsq_out, cudaStream_t st);
+cudaError_t launch_power_finalize_f64(double* last, const double* nsq_last, double* prev, const double* nsq_prev,
+                                      int n, int sm_count, cudaStream_t st);
+cudaError_t launch_poisson_crs(int m, int n, int32_t* row_start, int32_t* col, double* val, int sm_count,
+                               cudaStream_t st);
+cudaError_t launch_dot2_f64(const double* a, const double* b, int n, double* partials, unsigned int* counter,
+                            double* out, int grid, cudaStream_t st);
+cudaError_t launch_dot2_f32(const float* a, const float* b, int n, double* partials, unsigned int* counter,
+                            double* out, int grid, cudaStream_t st);
+cudaError_t launch_resid_f64(const double* a, double sa, const double* b, double sb, int n, double* partials,
+                             unsigned int* counter, double* out, int grid, cudaStream_t st);
+cudaError_t launch_resid_f32(const float* a, double sa, const float* b, double sb, int n, double* partials,
+                             unsigned int* counter, double* out, int grid, cudaStream_t st);
+cudaError_t launch_convert_f64_f32(const double* s, float* d, long long n, int sm_count, cudaStream_t st);
+cudaError_t launch_convert_f32_f64(const float* s, double* d, long long n, int sm_count, cudaStream_t st);
+cudaError_t launch_convert_f64_bf16(const double* s, void* d, long long n, int sm_count, cudaStream_t st);
+
+// Poisson row start closed form (shared with the host checker of the
+// device generator).
+long long poisson_row_start_host(long long row, long long m, long long n);
+
+}  // namespace pwmgpu

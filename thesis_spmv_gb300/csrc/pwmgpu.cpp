@@ -1,0 +1,540 @@
+// pwmgpu.cpp -- host side of the C ABI (include/pwmgpu.h).
+//
+// A pwmgpu_matrix owns the device copy of one sparse matrix plus the plan
+// its kernels need (merge-path tile coordinates, scratch for carries and
+// reductions) and a CUDA stream.  It mirrors pwm::SparseMatrix
+// (Matrix/SparseMatrix.hpp:13-68): load / generate, mv, powerIteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "pwmgpu.h"
+
+using namespace pwmgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(e_ == cudaErrorMemoryAllocation ? PWMGPU_ERR_NOMEM : PWMGPU_ERR_CUDA,     \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define TRY(expr)                 \
+    do {                          \
+        int r_ = (expr);          \
+        if (r_ != PWMGPU_OK) return r_; \
+    } while (0)
+
+constexpr int kPad = 16;  // kArrayPad in merge.cuh
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(PWMGPU_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    return PWMGPU_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct pwmgpu_matrix {
+    int format = PWMGPU_FMT_MERGE;
+    int partitions = 1;
+    int device = 0;
+    int sm_count = 1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool loaded = false;
+
+    DevMatrix M;
+
+    // merge-path plan (FP64 kernel)
+    int cfg = 0;
+    int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
+    int2* tiles = nullptr;
+    // FP32 / BF16 plan (lazy)
+    int tm32 = 0, num_tiles32 = 0, grid32 = 1, fix_grid32 = 1;
+    int2* tiles32 = nullptr;
+    float* val32 = nullptr;
+    void* valbf = nullptr;
+    int bf16_exact = -1;
+
+    // scratch
+    double* carries = nullptr;  // max(num_tiles, num_tiles32) doubles (also used as floats)
+    size_t carries_cap = 0;
+    double* partials = nullptr;  // spmv partials
+    size_t partials_cap = 0;
+    double* fix_partials = nullptr;
+    size_t fix_cap = 0;
+    unsigned int* counter = nullptr;
+    double* nsq = nullptr;
+    size_t nsq_cap = 0;
+    double* small = nullptr;  // 8 doubles of reduction outputs
+    int* status = nullptr;
+
+    // host-facing vector buffers
+    double* dx = nullptr;
+    double* dy = nullptr;
+    size_t vec_cap = 0;
+    float* fx = nullptr;
+    float* fy = nullptr;
+    size_t fvec_cap = 0;
+
+    void release_matrix() {
+        dfree(M.row_start);
+        dfree(M.col);
+        dfree(M.val);
+        dfree(tiles);
+        dfree(tiles32);
+        dfree(val32);
+        if (valbf) cudaFree(valbf);
+        valbf = nullptr;
+        bf16_exact = -1;
+        M = DevMatrix();
+        num_tiles = num_tiles32 = 0;
+        loaded = false;
+    }
+    void release_all() {
+        release_matrix();
+        dfree(carries);
+        dfree(partials);
+        dfree(fix_partials);
+        dfree(counter);
+        dfree(nsq);
+        dfree(small);
+        dfree(status);
+        dfree(dx);
+        dfree(dy);
+        dfree(fx);
+        dfree(fy);
+        carries_cap = partials_cap = fix_cap = nsq_cap = vec_cap = fvec_cap = 0;
+    }
+};
+
+namespace {
+
+int ensure_cap(double** p, size_t* cap, size_t need) {
+    if (*cap >= need && *p) return PWMGPU_OK;
+    dfree(*p);
+    *cap = 0;
+    TRY(dalloc(p, need));
+    *cap = need;
+    return PWMGPU_OK;
+}
+
+int check_status(pwmgpu_matrix* m) {
+    int st = 0;
+    CU(cudaMemcpyAsync(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    CU(cudaStreamSynchronize(m->stream));
+    if (st != PWMGPU_OK) {
+        cudaMemsetAsync(m->status, 0, sizeof(int), m->stream);
+        cudaStreamSynchronize(m->stream);
+        return fail(st, "device kernel reported status %d (a bounded wait timed out)", st);
+    }
+    return PWMGPU_OK;
+}
+
+// Build the merge-path plan: tile coordinates for diagonals t*TM
+// (k_merge_partition) and the scratch the kernels need.
+int build_plan(pwmgpu_matrix* m) {
+    const long long total = (long long)m->M.nor + m->M.nnz;
+    m->tm = merge_items_per_tile(m->cfg);
+    m->num_tiles = (int)((total + m->tm - 1) / m->tm);
+    dfree(m->tiles);
+    TRY(dalloc(&m->tiles, (size_t)m->num_tiles + 1));
+    if (m->num_tiles > 0)
+        CU(launch_merge_partition(m->M.row_start, m->M.nor, m->M.nnz, m->tm, m->num_tiles, m->tiles, m->stream));
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
+    m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
+    TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
+    TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)std::max(m->grid, 2 * dot_grid(m->M.nor, m->sm_count)) + 64));
+    TRY(ensure_cap(&m->fix_partials, &m->fix_cap, (size_t)m->fix_grid + 64));
+    dfree(m->tiles32);
+    m->num_tiles32 = 0;
+    CU(cudaStreamSynchronize(m->stream));
+    m->loaded = true;
+    return PWMGPU_OK;
+}
+
+int ensure_vectors(pwmgpu_matrix* m) {
+    size_t need = (size_t)std::max(m->M.nor, m->M.noc) + kPad;
+    if (m->vec_cap >= need) return PWMGPU_OK;
+    dfree(m->dx);
+    dfree(m->dy);
+    m->vec_cap = 0;
+    TRY(dalloc(&m->dx, need));
+    TRY(dalloc(&m->dy, need));
+    m->vec_cap = need;
+    return PWMGPU_OK;
+}
+
+int ensure_nsq(pwmgpu_matrix* m, size_t need) { return ensure_cap(&m->nsq, &m->nsq_cap, need + 1); }
+
+int alloc_matrix(pwmgpu_matrix* m, int32_t nor, int32_t noc, long long nnz) {
+    m->release_matrix();
+    m->M.nor = nor;
+    m->M.noc = noc;
+    m->M.nnz = nnz;
+    TRY(dalloc(&m->M.row_start, (size_t)nor + 1 + kPad));
+    TRY(dalloc(&m->M.col, (size_t)nnz + kPad));
+    TRY(dalloc(&m->M.val, (size_t)nnz + kPad));
+    // the TMA windows may read the padding: keep it defined
+    CU(cudaMemsetAsync(m->M.row_start + nor + 1, 0, kPad * sizeof(int32_t), m->stream));
+    CU(cudaMemsetAsync(m->M.col + nnz, 0, kPad * sizeof(int32_t), m->stream));
+    CU(cudaMemsetAsync(m->M.val + nnz, 0, kPad * sizeof(double), m->stream));
+    return PWMGPU_OK;
+}
+
+int check_sizes(long long nor, long long noc, long long nnz) {
+    if (nor < 0 || noc < 0 || nnz < 0) return fail(PWMGPU_ERR_INVALID, "negative size");
+    if (nor + nnz >= (1LL << 31) - 4096)
+        return fail(PWMGPU_ERR_INVALID, "nor + nnz = %lld exceeds the 32-bit merge-path range", nor + nnz);
+    if (noc >= (1LL << 31)) return fail(PWMGPU_ERR_INVALID, "noc too large");
+    return PWMGPU_OK;
+}
+
+int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
+    if (m->num_tiles == 0) return PWMGPU_OK;
+    CU(launch_merge_spmv_f64(m->cfg, kModeSpmv, m->M, m->tiles, m->num_tiles, m->grid, dx, dy, m->carries, nullptr,
+                             nullptr, m->status, m->stream));
+    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->tiles, m->num_tiles, dy, m->carries, nullptr, nullptr, 0, nullptr,
+                              m->fix_grid, nullptr, nullptr, m->stream));
+    return PWMGPU_OK;
+}
+
+// One power-method step on device vectors: out = 2^e(nsq_in) * A in, and
+// nsq_out = ||out||^2 (deterministic).
+int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
+    CU(launch_merge_spmv_f64(m->cfg, kModePower, m->M, m->tiles, m->num_tiles, m->grid, in, out, m->carries, nsq_in,
+                             m->partials, m->status, m->stream));
+    CU(launch_merge_fixup_f64(kModePower, m->M, m->tiles, m->num_tiles, out, m->carries, nsq_in, m->partials,
+                              m->grid, m->fix_partials, m->fix_grid, m->counter, nsq_out, m->stream));
+    return PWMGPU_OK;
+}
+
+int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
+    if (it <= 0 || m->M.nor == 0) return PWMGPU_OK;
+    TRY(ensure_nsq(m, (size_t)it + 1));
+    for (int k = 0; k < it; ++k) {
+        const double* in = (k % 2 == 0) ? dx : dy;
+        double* out = (k % 2 == 0) ? dy : dx;
+        TRY(power_step_f64(m, in, out, k ? m->nsq + k : nullptr, m->nsq + k + 1));
+    }
+    double* last = (it % 2 == 1) ? dy : dx;
+    double* prev = (it % 2 == 1) ? dx : dy;
+    CU(launch_power_finalize_f64(last, m->nsq + it, it >= 2 ? prev : nullptr, m->nsq + it - 1, m->M.nor,
+                                 m->sm_count, m->stream));
+    return PWMGPU_OK;
+}
+
+}  // namespace
+
+namespace pwmgpu {
+long long poisson_row_start_host(long long row, long long m, long long n) {
+    long long mn = m * n;
+    long long below = row > m ? row - m : 0;
+    long long left = row - (row + m - 1) / m;
+    long long right = row - row / m;
+    long long above = row < mn - m ? row : (mn - m > 0 ? mn - m : 0);
+    return below + left + row + right + above;
+}
+}  // namespace pwmgpu
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* pwmgpu_last_error(void) { return g_err.c_str(); }
+
+int pwmgpu_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes) {
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    int sms = 0;
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    size_t f = 0, t = 0;
+    CU(cudaMemGetInfo(&f, &t));
+    if (sm_count) *sm_count = sms;
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_create(int format, int partitions, pwmgpu_matrix** out) {
+    if (!out) return fail(PWMGPU_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (format != PWMGPU_FMT_MERGE && format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH)
+        return fail(PWMGPU_ERR_INVALID, "unknown format %d", format);
+    pwmgpu_matrix* m = new pwmgpu_matrix();
+    m->format = format;
+    m->partitions = partitions > 0 ? partitions : 1;
+    int rc = PWMGPU_OK;
+    do {
+        cudaError_t e = cudaGetDevice(&m->device);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); break; }
+        e = cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "cudaDeviceGetAttribute: %s", cudaGetErrorString(e)); break; }
+        e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); break; }
+        m->own_stream = true;
+        if ((rc = dalloc(&m->counter, 4)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&m->status, 4)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&m->small, 16)) != PWMGPU_OK) break;
+        cudaMemsetAsync(m->counter, 0, 4 * sizeof(unsigned int), m->stream);
+        cudaMemsetAsync(m->status, 0, 4 * sizeof(int), m->stream);
+        e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "init: %s", cudaGetErrorString(e)); break; }
+    } while (0);
+    if (rc != PWMGPU_OK) {
+        m->release_all();
+        if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
+        delete m;
+        return rc;
+    }
+    *out = m;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_destroy(pwmgpu_matrix* m) {
+    if (!m) return PWMGPU_OK;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    m->release_all();
+    if (m->own_stream && m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_set_stream(pwmgpu_matrix* m, void* stream) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    CU(cudaStreamSynchronize(m->stream));
+    if (m->own_stream) cudaStreamDestroy(m->stream);
+    m->stream = (cudaStream_t)stream;
+    m->own_stream = false;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_generate_poisson(pwmgpu_matrix* m, int32_t mx, int32_t ny) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (mx < 1 || ny < 1) return fail(PWMGPU_ERR_INVALID, "Poisson grid must be at least 1x1 (got %d x %d)", mx, ny);
+    long long N = (long long)mx * ny;
+    long long nnz = (long long)ny * (mx + 2LL * (mx - 1)) + 2LL * (ny - 1) * mx;  // CRS.hpp:64
+    TRY(check_sizes(N, N, nnz));
+    TRY(alloc_matrix(m, (int32_t)N, (int32_t)N, nnz));
+    CU(launch_poisson_crs(mx, ny, m->M.row_start, m->M.col, m->M.val, m->sm_count, m->stream));
+    return build_plan(m);
+}
+
+int pwmgpu_load_csr(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
+                    const int32_t* col_ind, const double* vals) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    TRY(check_sizes(nor, noc, nnz));
+    if (!row_start || (nnz > 0 && (!col_ind || !vals))) return fail(PWMGPU_ERR_INVALID, "null CRS array");
+    if (row_start[0] != 0 || row_start[nor] != nnz)
+        return fail(PWMGPU_ERR_INVALID, "row_start must run from 0 to nnz (got %d..%d, nnz %d)", row_start[0],
+                    row_start[nor], nnz);
+    for (int32_t i = 0; i < nor; ++i)
+        if (row_start[i + 1] < row_start[i]) return fail(PWMGPU_ERR_INVALID, "row_start decreases at row %d", i);
+    for (int32_t k = 0; k < nnz; ++k)
+        if (col_ind[k] < 0 || col_ind[k] >= noc)
+            return fail(PWMGPU_ERR_INVALID, "column index %d at nonzero %d out of range [0,%d)", col_ind[k], k, noc);
+    TRY(alloc_matrix(m, nor, noc, nnz));
+    CU(cudaMemcpyAsync(m->M.row_start, row_start, sizeof(int32_t) * ((size_t)nor + 1), cudaMemcpyHostToDevice,
+                       m->stream));
+    if (nnz > 0) {
+        CU(cudaMemcpyAsync(m->M.col, col_ind, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(m->M.val, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, m->stream));
+    }
+    return build_plan(m);
+}
+
+int pwmgpu_load_triplets(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, int32_t* rows, int32_t* cols,
+                         double* vals) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    TRY(check_sizes(nor, noc, nnz));
+    if (nnz > 0 && (!rows || !cols || !vals)) return fail(PWMGPU_ERR_INVALID, "null triplet array");
+    for (int32_t k = 0; k < nnz; ++k) {
+        if (rows[k] < 0 || rows[k] >= nor) return fail(PWMGPU_ERR_INVALID, "row %d at entry %d out of range", rows[k], k);
+        if (cols[k] < 0 || cols[k] >= noc) return fail(PWMGPU_ERR_INVALID, "column %d at entry %d out of range", cols[k], k);
+    }
+    // Util/TripletToCRS.hpp:135-172: rows ascending, columns ascending within
+    // a row (for unique coordinates the reference's randomised quicksort
+    // yields exactly this order).  Counting sort by row, then each row by
+    // column; the caller's arrays are left sorted, as in the reference.
+    std::vector<int32_t> row_start((size_t)nor + 1, 0);
+    for (int32_t k = 0; k < nnz; ++k) row_start[(size_t)rows[k] + 1]++;
+    for (int32_t i = 0; i < nor; ++i) row_start[(size_t)i + 1] += row_start[i];
+    std::vector<int32_t> pos(row_start.begin(), row_start.end() - 1);
+    std::vector<int32_t> c2((size_t)nnz);
+    std::vector<double> v2((size_t)nnz);
+    for (int32_t k = 0; k < nnz; ++k) {
+        int32_t p = pos[rows[k]]++;
+        c2[p] = cols[k];
+        v2[p] = vals[k];
+    }
+    std::vector<std::pair<int32_t, int32_t>> tmp;
+    for (int32_t i = 0; i < nor; ++i) {
+        int32_t a = row_start[i], b = row_start[(size_t)i + 1];
+        if (b - a < 2) continue;
+        bool sorted = true;
+        for (int32_t k = a + 1; k < b; ++k)
+            if (c2[k] < c2[k - 1]) { sorted = false; break; }
+        if (sorted) continue;
+        tmp.resize(b - a);
+        for (int32_t k = a; k < b; ++k) tmp[k - a] = {c2[k], k};
+        std::stable_sort(tmp.begin(), tmp.end(),
+                         [](const std::pair<int32_t, int32_t>& p, const std::pair<int32_t, int32_t>& q) {
+                             return p.first < q.first;
+                         });
+        std::vector<double> vv(b - a);
+        for (int32_t k = 0; k < b - a; ++k) vv[k] = v2[tmp[k].second];
+        for (int32_t k = 0; k < b - a; ++k) {
+            c2[a + k] = tmp[k].first;
+            v2[a + k] = vv[k];
+        }
+    }
+    for (int32_t i = 0; i < nor; ++i)
+        for (int32_t k = row_start[i]; k < row_start[(size_t)i + 1]; ++k) rows[k] = i;
+    if (nnz > 0) {
+        std::memcpy(cols, c2.data(), sizeof(int32_t) * (size_t)nnz);
+        std::memcpy(vals, v2.data(), sizeof(double) * (size_t)nnz);
+    }
+    return pwmgpu_load_csr(m, nor, noc, nnz, row_start.data(), c2.data(), v2.data());
+}
+
+int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (nor) *nor = m->M.nor;
+    if (noc) *noc = m->M.noc;
+    if (nnz) *nnz = m->M.nnz;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_get_csr(pwmgpu_matrix* m, int32_t* row_start, int32_t* col_ind, double* vals) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (!row_start || (m->M.nnz > 0 && (!col_ind || !vals))) return fail(PWMGPU_ERR_INVALID, "null output array");
+    CU(cudaMemcpyAsync(row_start, m->M.row_start, sizeof(int32_t) * ((size_t)m->M.nor + 1), cudaMemcpyDeviceToHost,
+                       m->stream));
+    if (m->M.nnz > 0) {
+        CU(cudaMemcpyAsync(col_ind, m->M.col, sizeof(int32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+        CU(cudaMemcpyAsync(vals, m->M.val, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+    }
+    CU(cudaStreamSynchronize(m->stream));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_mv_device(pwmgpu_matrix* m, const double* dx, double* dy) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor > 0 && (!dx || !dy)) return fail(PWMGPU_ERR_INVALID, "null vector");
+    return spmv_f64(m, dx, dy);
+}
+
+int pwmgpu_mv(pwmgpu_matrix* m, const double* x, double* y) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor == 0) return PWMGPU_OK;
+    if (!y || (m->M.noc > 0 && !x)) return fail(PWMGPU_ERR_INVALID, "null vector");
+    TRY(ensure_vectors(m));
+    if (m->M.noc > 0)
+        CU(cudaMemcpyAsync(m->dx, x, sizeof(double) * (size_t)m->M.noc, cudaMemcpyHostToDevice, m->stream));
+    TRY(spmv_f64(m, m->dx, m->dy));
+    CU(cudaMemcpyAsync(y, m->dy, sizeof(double) * (size_t)m->M.nor, cudaMemcpyDeviceToHost, m->stream));
+    return check_status(m);
+}
+
+int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor != m->M.noc) return fail(PWMGPU_ERR_NOT_SQUARE, "power method needs a square matrix");
+    if (it < 0) return fail(PWMGPU_ERR_INVALID, "negative iteration count");
+    if (m->M.nor > 0 && (!dx || !dy)) return fail(PWMGPU_ERR_INVALID, "null vector");
+    return power_device(m, dx, dy, it);
+}
+
+int pwmgpu_power(pwmgpu_matrix* m, double* x, double* y, int32_t it) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor != m->M.noc) return fail(PWMGPU_ERR_NOT_SQUARE, "power method needs a square matrix");
+    if (it < 0) return fail(PWMGPU_ERR_INVALID, "negative iteration count");
+    if (it == 0 || m->M.nor == 0) return PWMGPU_OK;
+    if (!x || !y) return fail(PWMGPU_ERR_INVALID, "null vector");
+    TRY(ensure_vectors(m));
+    const size_t bytes = sizeof(double) * (size_t)m->M.nor;
+    CU(cudaMemcpyAsync(m->dx, x, bytes, cudaMemcpyHostToDevice, m->stream));
+    TRY(power_device(m, m->dx, m->dy, it));
+    CU(cudaMemcpyAsync(x, m->dx, bytes, cudaMemcpyDeviceToHost, m->stream));
+    CU(cudaMemcpyAsync(y, m->dy, bytes, cudaMemcpyDeviceToHost, m->stream));
+    return check_status(m);
+}
+
+int pwmgpu_merge_partition(pwmgpu_matrix* m, int32_t parts, int32_t* coords) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (parts < 1 || !coords) return fail(PWMGPU_ERR_INVALID, "parts must be >= 1 and coords non-null");
+    const long long total = (long long)m->M.nor + m->M.nnz;
+    const long long ipt = (total + parts - 1) / parts;  // CRS_Merge.hpp:98
+    int2* d = nullptr;
+    TRY(dalloc(&d, (size_t)parts + 1));
+    cudaError_t e = launch_merge_partition(m->M.row_start, m->M.nor, m->M.nnz, ipt, parts, d, m->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(coords, d, sizeof(int2) * ((size_t)parts + 1), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "merge partition: %s", cudaGetErrorString(e));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (items_per_tile) *items_per_tile = m->tm;
+    if (num_tiles) *num_tiles = m->num_tiles;
+    if (grid) *grid = m->grid;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
+    (void)dx; (void)dy;
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    return fail(PWMGPU_ERR_UNSUPPORTED, "FP32 SpMV not built yet");
+}
+
+int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info) {
+    (void)x; (void)max_it; (void)tol; (void)precision; (void)info;
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    return fail(PWMGPU_ERR_UNSUPPORTED, "solve not built yet");
+}
+
+}  // extern "C"

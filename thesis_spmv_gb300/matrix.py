@@ -1,0 +1,240 @@
+"""Python mirror of the reference's operator interface, backed by libpwmgpu.so.
+
+``Triplet`` mirrors pwm::Triplet<T,int_type> (Matrix/Triplet.hpp:26-279) and
+``CRSCuda`` / ``CSBCuda`` / ``COHCuda`` mirror a pwm::SparseMatrix<T,int_type>
+subclass (Matrix/SparseMatrix.hpp:13-68): same method names, argument meaning
+and in-place behaviour (loadFromTriplets sorts the triplet; mv fills y;
+powerIteration leaves the result in x for an even and in y for an odd
+iteration count).  Every compute call goes through the C ABI; a failing call
+raises PwmGpuError.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import FMT_COH, FMT_CSB, FMT_MERGE, PREC_F32, PREC_F64, PREC_MIXED, SolveInfo, check
+
+_I32 = np.int32
+_F64 = np.float64
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+class Triplet:
+    """COO matrix: row_coord, col_coord, data, row_size, col_size, nnz."""
+
+    def __init__(self, row_size=0, col_size=0, rows=None, cols=None, vals=None):
+        self.row_size = int(row_size)
+        self.col_size = int(col_size)
+        self.row_coord = np.ascontiguousarray(rows if rows is not None else np.zeros(0), dtype=_I32)
+        self.col_coord = np.ascontiguousarray(cols if cols is not None else np.zeros(0), dtype=_I32)
+        self.data = np.ascontiguousarray(vals if vals is not None else np.zeros(0), dtype=_F64)
+
+    @property
+    def nnz(self):
+        return int(self.row_coord.size)
+
+    def generatePoisson(self, m, n):
+        """Matrix/Triplet.hpp:226-278: diagonal, super/sub, then the two far diagonals per row."""
+        m, n = int(m), int(n)
+        size = m * n
+        i = np.arange(size, dtype=np.int64)
+        parts_r, parts_c, parts_v = [i], [i], [np.full(size, 4.0)]
+        sup = (i < size - 1) & (i % m != m - 1)
+        sub = (i < size - 1) & ((i + 1) % m != 0)
+        far = i < size - m
+        # interleave in the reference's per-row emission order
+        order_r, order_c, order_v, key = [], [], [], []
+        slots = [(i, i, 4.0, np.ones(size, bool)), (i, i + 1, -1.0, sup), (i + 1, i, -1.0, sub),
+                 (i + m, i, -1.0, far), (i, i + m, -1.0, far)]
+        for s, (r, c, v, mask) in enumerate(slots):
+            idx = np.nonzero(mask)[0]
+            order_r.append(r[idx])
+            order_c.append(c[idx])
+            order_v.append(np.full(idx.size, v))
+            key.append(idx * 5 + s)
+        k = np.concatenate(key)
+        p = np.argsort(k, kind="stable")
+        self.row_size = self.col_size = size
+        self.row_coord = np.concatenate(order_r)[p].astype(_I32)
+        self.col_coord = np.concatenate(order_c)[p].astype(_I32)
+        self.data = np.concatenate(order_v)[p].astype(_F64)
+        return self
+
+    def loadFromMM(self, filename, has_data, symmetric, random_fill=False):
+        """Matrix/Triplet.hpp:75-154 (random_fill is not supported)."""
+        if random_fill:
+            raise NotImplementedError("random_fill needs Boost's uniform_real_distribution stream")
+        rows, cols, vals = [], [], []
+        with open(filename) as f:
+            for line in f:
+                if not line.startswith("%"):
+                    hdr = line.split()
+                    self.row_size, self.col_size = int(hdr[0]), int(hdr[1])
+                    break
+            for line in f:
+                t = line.split()
+                if not t:
+                    break
+                r, c = int(t[0]) - 1, int(t[1]) - 1
+                v = float(t[2]) if has_data else 1.0
+                if has_data and v == 0.0:
+                    continue
+                rows.append(r); cols.append(c); vals.append(v)
+                if symmetric and r != c:
+                    rows.append(c); cols.append(r); vals.append(v)
+        self.row_coord = np.array(rows, _I32)
+        self.col_coord = np.array(cols, _I32)
+        self.data = np.array(vals, _F64)
+        return self
+
+    def loadFromBin(self, filename, mat_size, symmetric, random_vals=False):
+        """Matrix/Triplet.hpp:164-216: uint32 (row, col) pairs, value 1."""
+        if random_vals:
+            raise NotImplementedError("random_vals needs Boost's uniform_real_distribution stream")
+        rc = np.fromfile(filename, dtype=np.uint32).reshape(-1, 2).astype(np.int64)
+        r, c = rc[:, 0], rc[:, 1]
+        if symmetric:
+            off = r != c
+            # entry, then its transpose right after it when off-diagonal
+            idx = np.repeat(np.arange(r.size), np.where(off, 2, 1))
+            first = np.concatenate([[True], idx[1:] != idx[:-1]])
+            rr = np.where(first, r[idx], c[idx])
+            cc = np.where(first, c[idx], r[idx])
+            r, c = rr, cc
+        self.row_size = self.col_size = int(mat_size)
+        self.row_coord = r.astype(_I32)
+        self.col_coord = c.astype(_I32)
+        self.data = np.ones(r.size, _F64)
+        return self
+
+
+class CudaSparseMatrix:
+    """A pwm::SparseMatrix on the GPU; `format` selects the storage."""
+
+    FORMAT = FMT_MERGE
+
+    def __init__(self, threads=1):
+        self._h = C.c_void_p()
+        check(_lib.lib().pwmgpu_create(self.FORMAT, int(threads) if threads else 1, C.byref(self._h)),
+              "pwmgpu_create")
+        self.threads = threads
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().pwmgpu_destroy(h)
+            except Exception:
+                pass
+            self._h = C.c_void_p()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- SparseMatrix.hpp:41 ----
+    def generatePoissonMatrix(self, m, n, partitions=1):
+        check(_lib.lib().pwmgpu_generate_poisson(self._h, int(m), int(n)), "generatePoissonMatrix")
+
+    # ---- SparseMatrix.hpp:48 ----
+    def loadFromTriplets(self, triplet, partitions_am=1):
+        for name in ("row_coord", "col_coord", "data"):
+            a = getattr(triplet, name)
+            want = _F64 if name == "data" else _I32
+            if not (isinstance(a, np.ndarray) and a.dtype == want and a.flags.c_contiguous):
+                setattr(triplet, name, np.ascontiguousarray(a, dtype=want))
+        check(_lib.lib().pwmgpu_load_triplets(self._h, triplet.row_size, triplet.col_size, triplet.nnz,
+                                              _ptr(triplet.row_coord), _ptr(triplet.col_coord),
+                                              _ptr(triplet.data)), "loadFromTriplets")
+
+    def loadCSR(self, nor, noc, row_start, col_ind, data):
+        rs = np.ascontiguousarray(row_start, _I32)
+        ci = np.ascontiguousarray(col_ind, _I32)
+        d = np.ascontiguousarray(data, _F64)
+        check(_lib.lib().pwmgpu_load_csr(self._h, int(nor), int(noc), int(ci.size), _ptr(rs), _ptr(ci), _ptr(d)),
+              "pwmgpu_load_csr")
+
+    def dims(self):
+        nor, noc, nnz = C.c_int32(), C.c_int32(), C.c_int64()
+        check(_lib.lib().pwmgpu_dims(self._h, C.byref(nor), C.byref(noc), C.byref(nnz)), "pwmgpu_dims")
+        return nor.value, noc.value, nnz.value
+
+    def getCSR(self):
+        """The device CRS arrays (row_start, col_ind, data) copied to the host."""
+        nor, noc, nnz = self.dims()
+        rs = np.zeros(nor + 1, _I32)
+        ci = np.zeros(max(nnz, 1), _I32)
+        d = np.zeros(max(nnz, 1), _F64)
+        check(_lib.lib().pwmgpu_get_csr(self._h, _ptr(rs), _ptr(ci), _ptr(d)), "pwmgpu_get_csr")
+        return rs, ci[:nnz], d[:nnz]
+
+    # ---- SparseMatrix.hpp:57 ----
+    def mv(self, x, y):
+        """y = A x on host arrays (y filled in place)."""
+        nor, noc, _ = self.dims()
+        assert x.dtype == _F64 and y.dtype == _F64 and x.size >= noc and y.size >= nor
+        assert x.flags.c_contiguous and y.flags.c_contiguous
+        check(_lib.lib().pwmgpu_mv(self._h, _ptr(x), _ptr(y)), "mv")
+
+    # ---- SparseMatrix.hpp:66 ----
+    def powerIteration(self, x, y, it):
+        nor, _, _ = self.dims()
+        assert x.dtype == _F64 and y.dtype == _F64 and x.size >= nor and y.size >= nor
+        check(_lib.lib().pwmgpu_power(self._h, _ptr(x), _ptr(y), int(it)), "powerIteration")
+
+    # ---- device-resident and extended entry points ----
+    def mv_device(self, dx_ptr, dy_ptr):
+        check(_lib.lib().pwmgpu_mv_device(self._h, C.c_void_p(dx_ptr), C.c_void_p(dy_ptr)), "mv_device")
+
+    def mv_device_f32(self, dx_ptr, dy_ptr):
+        check(_lib.lib().pwmgpu_mv_device_f32(self._h, C.c_void_p(dx_ptr), C.c_void_p(dy_ptr)), "mv_device_f32")
+
+    def power_device(self, dx_ptr, dy_ptr, it):
+        check(_lib.lib().pwmgpu_power_device(self._h, C.c_void_p(dx_ptr), C.c_void_p(dy_ptr), int(it)),
+              "power_device")
+
+    def set_stream(self, stream_ptr):
+        check(_lib.lib().pwmgpu_set_stream(self._h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def solve(self, x, max_it, tol, precision=PREC_F64):
+        info = SolveInfo()
+        check(_lib.lib().pwmgpu_solve(self._h, _ptr(x), int(max_it), float(tol), int(precision), C.byref(info)),
+              "solve")
+        return info
+
+    def merge_partition(self, parts):
+        out = np.zeros(2 * (parts + 1), _I32)
+        check(_lib.lib().pwmgpu_merge_partition(self._h, int(parts), _ptr(out)), "merge_partition")
+        return out.reshape(parts + 1, 2)
+
+    def tile_info(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        check(_lib.lib().pwmgpu_tile_info(self._h, C.byref(a), C.byref(b), C.byref(c)), "tile_info")
+        return a.value, b.value, c.value
+
+
+class CRSCuda(CudaSparseMatrix):
+    """Merge-path CRS on the GPU (drop-in beside CRS_Merge, method 12)."""
+    FORMAT = FMT_MERGE
+
+
+class CSBCuda(CudaSparseMatrix):
+    """CSB on the GPU (drop-in beside CSB, method 13)."""
+    FORMAT = FMT_CSB
+
+
+class COHCuda(CudaSparseMatrix):
+    """Block CO-H on the GPU (drop-in beside BlockCOH, method 14)."""
+    FORMAT = FMT_COH
+
+
+def selectType(method, threads=1):
+    """Util/DriverUtil.hpp:38-84 selectType for the GPU method numbers
+    (12 merge-path CRS, 13 CSB, 14 CO-H); None for any other number, like the
+    reference's NULL."""
+    return {12: CRSCuda, 13: CSBCuda, 14: COHCuda}.get(int(method), lambda t: None)(threads)
