@@ -55,15 +55,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase.  Returns false (and records the timeout)
-// when the budget runs out; the caller then leaves the kernel.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait on an mbarrier phase.  Returns false when the budget runs out
+// (recording PWMGPU_ERR_TIMEOUT) or when another thread of the launch has
+// already recorded a failure; the caller then leaves the kernel.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status,
+                                                  long long budget = kWaitCycles, bool watch_status = true) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
+    unsigned spins = 0;
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) {
-            atomicCAS(status, PWMGPU_OK, PWMGPU_ERR_TIMEOUT);
-            return false;
+        if ((++spins & 255u) == 0u) {
+            if (watch_status && *(volatile int*)status != PWMGPU_OK) return false;
+            if (clock64() - t0 > budget) {
+                atomicCAS(status, PWMGPU_OK, PWMGPU_ERR_TIMEOUT);
+                return false;
+            }
         }
     }
     return true;

@@ -22,20 +22,26 @@ struct DevMatrix {
 enum { kModeSpmv = 0, kModePower = 1 };
 
 // merge.cu
-int merge_items_per_tile(int cfg);
-int merge_items_per_tile_f32();
-int merge_grid(int cfg, int num_tiles, int sm_count);
-int merge_grid_f32(int num_tiles, int sm_count, bool bf16);
+// Merge-path kernel configurations.
+enum { kCfgF64 = 0, kCfgF64Small = 1, kCfgF32 = 2, kCfgBF16 = 3 };
+struct MergeGeom {
+    int wm;    // merge items per sub-tile (one warp)
+    int w;     // sub-tiles per tile (warps per CTA)
+    int smem;  // dynamic shared memory per CTA
+    int occ;   // resident CTAs per SM
+    int nt;    // threads per CTA
+};
+MergeGeom merge_geometry(int cfg);
+int merge_grid(int cfg, int nsub, int sm_count);
 int fixup_grid(int num_tiles, int sm_count);
 int dot_grid(long long n, int sm_count);
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
                                    int2* out, cudaStream_t st);
-cudaError_t launch_merge_spmv_f64(int cfg, int mode, const DevMatrix& M, const int2* tiles, int num_tiles, int grid,
-                                  const double* x, double* y, double* carries, const double* nsq_in,
-                                  double* partials, int* status, cudaStream_t st);
-cudaError_t launch_merge_spmv_f32(int mode, const DevMatrix& M, const void* val, bool bf16, const int2* tiles,
-                                  int num_tiles, int grid, const float* x, float* y, float* carries,
-                                  const double* nsq_in, double* partials, int* status, cudaStream_t st);
+cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* val, const int2* subc,
+                              const uint8_t* subflag, int nsub, int grid, const void* x, void* y, void* carries,
+                              const double* nsq_in, double* partials, int* status, cudaStream_t st);
+cudaError_t launch_mark_empty_rows(const int32_t* row_start, int nor, int wm, uint8_t* flags, int sm_count,
+                                   cudaStream_t st);
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
                                    const double* carries, const double* nsq_in, const double* spmv_partials,
                                    int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,

@@ -30,6 +30,15 @@ __global__ void k_merge_partition(const int32_t* __restrict__ row_start, int nor
     }
 }
 
+// Sub-tiles that hold an empty row (its end item lies at diagonal
+// row_start[r+1] + r) take the general path of the tile kernel.
+__global__ void k_mark_empty_rows(const int32_t* __restrict__ row_start, int nor, int wm, uint8_t* flags) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nor; r += gridDim.x * blockDim.x) {
+        const int e = row_start[r + 1];
+        if (e == row_start[r]) flags[(e + r) / wm] = 1;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // K2: merge-path SpMV (plain or with the power-method epilogue)
 // ---------------------------------------------------------------------------
@@ -38,45 +47,70 @@ struct MergeArgs {
     const int32_t* row_start;
     const int32_t* col;
     const VT* val;
-    const int2* tiles;
-    int nor, nnz, num_tiles;
+    const int2* subc;        // sub-tile boundaries, nsub + 1 entries
+    const uint8_t* subflag;  // 1 if the sub-tile holds an empty row
+    int nor, nnz, nsub, num_tiles;
     const XT* x;
     XT* y;
-    AT* carries;
+    AT* carries;           // one per sub-tile
     const double* nsq_in;  // MODE_POWER: ||x||^2 (source of the 2^e rescale), or null for e = 0
     double* partials;      // MODE_POWER: per-CTA sum of squares
     int* status;
 };
 
 template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int STAGES>
-__global__ void __launch_bounds__(NT, 2) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
+__global__ void __launch_bounds__(NT, (MergeLayout<VT, XT, AT, NT, IPT, STAGES>::MINB)) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
+    using L = MergeLayout<VT, XT, AT, NT, IPT, STAGES>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     MergeSmem<VT, XT, AT, NT, IPT, STAGES> sm{smem_raw};
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int G = gridDim.x;
-    const int my_tiles = blockIdx.x < a.num_tiles ? (a.num_tiles - 1 - blockIdx.x) / G + 1 : 0;
+    const int my_tiles = (int)blockIdx.x < a.num_tiles ? (a.num_tiles - 1 - (int)blockIdx.x) / G + 1 : 0;
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
     const uint64_t pol = policy_evict_first();
+    const bool producer = (tid == 0);
 
-    if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(&sm.bar()[s], 1);
+    if (producer) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sm.full()[s], 1);
+            mbar_init(&sm.empty()[s], L::W);
+        }
         fence_mbar_init();
     }
     __syncthreads();
-    if (tid == 0)
-        for (int s = 0; s < STAGES && s < my_tiles; ++s)
-            issue_tile(sm, s, blockIdx.x + s * G, a.tiles, a.row_start, a.col, a.val, a.nor, pol);
+    int issued = 0;
+    if (producer)
+        for (; issued < STAGES && issued < my_tiles; ++issued)
+            issue_tile(sm, issued, blockIdx.x + issued * G, a.subc, a.subflag, a.nsub, a.row_start, a.col, a.val, a.nor,
+                       pol);
 
     double sumsq = 0.0;
-    for (int i = 0; i < my_tiles; ++i) {
+    int i = 0;
+    for (; i < my_tiles; ++i) {
         const int s = i % STAGES;
-        const uint32_t parity = (uint32_t)(i / STAGES) & 1u;
-        // the stage of tile i-1 is free (the previous iteration ended with a barrier)
-        if (tid == 0 && i >= 1 && i + STAGES - 1 < my_tiles)
-            issue_tile(sm, (i + STAGES - 1) % STAGES, blockIdx.x + (i + STAGES - 1) * G, a.tiles, a.row_start,
-                       a.col, a.val, a.nor, pol);
-        if (!process_tile<MODE>(sm, s, parity, blockIdx.x + i * G, a.x, a.y, a.carries, a.nor, e, sumsq, a.status))
-            return;
+        bool ok = true;
+        // Producer: refill the stage tile i-1 used once every warp released it.
+        if (producer && i >= 1 && i - 1 + STAGES < my_tiles) {
+            const int sp = (i - 1) % STAGES;
+            ok = mbar_wait_bounded(&sm.empty()[sp], (uint32_t)((i - 1) / STAGES) & 1u, a.status);
+            if (ok) {
+                issue_tile(sm, sp, blockIdx.x + (i - 1 + STAGES) * G, a.subc, a.subflag, a.nsub, a.row_start, a.col,
+                           a.val,
+                           a.nor, pol);
+                ++issued;
+            }
+        }
+        if (ok) ok = mbar_wait_bounded(&sm.full()[s], (uint32_t)(i / STAGES) & 1u, a.status);
+        if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
+        process_subtile<MODE>(sm, s, blockIdx.x + i * G, a.x, a.y, a.carries, a.nor, e, sumsq);
+        if (lane == 0) mbar_arrive(&sm.empty()[s]);
+    }
+    if (producer && i < my_tiles) {
+        // Leaving early after a timeout: let copies already in flight land
+        // (short bounded waits) before the CTA's shared memory goes away.
+        for (int t = i; t < issued; ++t)
+            mbar_wait_bounded(&sm.full()[t % STAGES], (uint32_t)(t / STAGES) & 1u, a.status, kWaitCycles / 8,
+                              false);
     }
     if (MODE == MODE_POWER) {
         double t = block_sum<NT>(sumsq, sm.red());
@@ -289,14 +323,13 @@ __global__ void k_convert<double, __nv_bfloat16>(const double* __restrict__ s, _
 // Host launchers
 // ===========================================================================
 
-// Tile configurations (threads per CTA, items per thread, pipeline stages).
+// Tile configurations (threads per CTA, items per lane, pipeline stages).
 template <typename VT, typename XT, typename AT, int NT, int IPT, int STAGES>
 struct MergeKernels {
     using L = MergeLayout<VT, XT, AT, NT, IPT, STAGES>;
-    static constexpr int TM = L::TM;
     static constexpr int SMEM = L::BYTES;
 
-    static int occupancy() {
+    static MergeGeom geom() {
         static int occ = -1;
         if (occ < 0) {
             auto k = k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, STAGES>;
@@ -307,15 +340,16 @@ struct MergeKernels {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM);
             occ = o > 0 ? o : 1;
         }
-        return occ;
+        return MergeGeom{L::WM, L::W, SMEM, occ, NT};
     }
 
-    static cudaError_t spmv(int mode, const DevMatrix& M, const VT* val, const int2* tiles, int num_tiles, int grid,
-                            const XT* x, XT* y, AT* carries, const double* nsq_in, double* partials, int* status,
-                            cudaStream_t st) {
-        occupancy();
-        MergeArgs<VT, XT, AT> a{M.row_start, M.col, val, tiles, M.nor, (int)M.nnz, num_tiles, x, y, carries,
-                                nsq_in, partials, status};
+    static cudaError_t spmv(int mode, const DevMatrix& M, const void* val, const int2* subc, const uint8_t* subflag,
+                            int nsub, int grid, const void* x, void* y, void* carries, const double* nsq_in,
+                            double* partials, int* status, cudaStream_t st) {
+        geom();
+        const int num_tiles = (nsub + L::W - 1) / L::W;
+        MergeArgs<VT, XT, AT> a{M.row_start, M.col, (const VT*)val, subc, subflag, M.nor, (int)M.nnz, nsub, num_tiles,
+                                (const XT*)x, (XT*)y, (AT*)carries, nsq_in, partials, status};
         if (mode == MODE_POWER)
             k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, STAGES><<<grid, NT, SMEM, st>>>(a);
         else
@@ -324,32 +358,28 @@ struct MergeKernels {
     }
 };
 
-// The configurations the library instantiates.  Config ids are stable
-// numbers used by the autotuner cache.
-using F64_256x7 = MergeKernels<double, double, double, 256, 7, 2>;
-using F64_128x11 = MergeKernels<double, double, double, 128, 11, 3>;
-using F32_256x7 = MergeKernels<float, float, float, 256, 7, 2>;
-using BF16_256x7 = MergeKernels<__nv_bfloat16, float, float, 256, 7, 2>;
+// The configurations the library instantiates (ids are stable: the
+// autotuner cache stores them).
+using CfgF64a = MergeKernels<double, double, double, 128, 12, 2>;       // kCfgF64
+using CfgF64b = MergeKernels<double, double, double, 128, 8, 2>;        // kCfgF64Small
+using CfgF32 = MergeKernels<float, float, float, 128, 12, 2>;           // kCfgF32
+using CfgBF16 = MergeKernels<__nv_bfloat16, float, float, 128, 12, 2>;  // kCfgBF16
 
-int merge_items_per_tile(int cfg) {
+MergeGeom merge_geometry(int cfg) {
     switch (cfg) {
-        case 1: return F64_128x11::TM;
-        default: return F64_256x7::TM;
+        case kCfgF64Small: return CfgF64b::geom();
+        case kCfgF32: return CfgF32::geom();
+        case kCfgBF16: return CfgBF16::geom();
+        default: return CfgF64a::geom();
     }
 }
 
-int merge_grid(int cfg, int num_tiles, int sm_count) {
-    int occ = (cfg == 1) ? F64_128x11::occupancy() : F64_256x7::occupancy();
-    long long g = (long long)occ * sm_count;
-    if (g > num_tiles) g = num_tiles;
-    return g > 0 ? (int)g : 1;
-}
-
-int merge_grid_f32(int num_tiles, int sm_count, bool bf16) {
-    int occ = bf16 ? BF16_256x7::occupancy() : F32_256x7::occupancy();
-    long long g = (long long)occ * sm_count;
-    if (g > num_tiles) g = num_tiles;
-    return g > 0 ? (int)g : 1;
+int merge_grid(int cfg, int nsub, int sm_count) {
+    MergeGeom g = merge_geometry(cfg);
+    long long tiles = (nsub + g.w - 1) / g.w;
+    long long grid = (long long)g.occ * sm_count;
+    if (grid > tiles) grid = tiles;
+    return grid > 0 ? (int)grid : 1;
 }
 
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
@@ -361,25 +391,29 @@ cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long 
     return cudaGetLastError();
 }
 
-cudaError_t launch_merge_spmv_f64(int cfg, int mode, const DevMatrix& M, const int2* tiles, int num_tiles, int grid,
-                                  const double* x, double* y, double* carries, const double* nsq_in,
-                                  double* partials, int* status, cudaStream_t st) {
-    if (cfg == 1)
-        return F64_128x11::spmv(mode, M, M.val, tiles, num_tiles, grid, x, y, carries, nsq_in, partials, status, st);
-    return F64_256x7::spmv(mode, M, M.val, tiles, num_tiles, grid, x, y, carries, nsq_in, partials, status, st);
+cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* val, const int2* subc,
+                              const uint8_t* subflag, int nsub, int grid, const void* x, void* y, void* carries,
+                              const double* nsq_in, double* partials, int* status, cudaStream_t st) {
+    switch (cfg) {
+        case kCfgF64Small:
+            return CfgF64b::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
+        case kCfgF32:
+            return CfgF32::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
+        case kCfgBF16:
+            return CfgBF16::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
+        default:
+            return CfgF64a::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
+    }
 }
 
-cudaError_t launch_merge_spmv_f32(int mode, const DevMatrix& M, const void* val, bool bf16, const int2* tiles,
-                                  int num_tiles, int grid, const float* x, float* y, float* carries,
-                                  const double* nsq_in, double* partials, int* status, cudaStream_t st) {
-    if (bf16)
-        return BF16_256x7::spmv(mode, M, (const __nv_bfloat16*)val, tiles, num_tiles, grid, x, y, carries, nsq_in,
-                                partials, status, st);
-    return F32_256x7::spmv(mode, M, (const float*)val, tiles, num_tiles, grid, x, y, carries, nsq_in, partials,
-                           status, st);
+cudaError_t launch_mark_empty_rows(const int32_t* row_start, int nor, int wm, uint8_t* flags, int sm_count,
+                                   cudaStream_t st) {
+    if (nor <= 0) return cudaSuccess;
+    long long blocks = (nor + 255) / 256;
+    if (blocks > sm_count * 16) blocks = sm_count * 16;
+    k_mark_empty_rows<<<(int)blocks, 256, 0, st>>>(row_start, nor, wm, flags);
+    return cudaGetLastError();
 }
-
-int merge_items_per_tile_f32() { return F32_256x7::TM; }
 
 template <typename XT, typename AT>
 static cudaError_t fixup_impl(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, XT* y,

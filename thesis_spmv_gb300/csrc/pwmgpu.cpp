@@ -84,6 +84,7 @@ struct pwmgpu_matrix {
     int cfg = 0;
     int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
     int2* tiles = nullptr;
+    uint8_t* subflag = nullptr;  // per sub-tile: holds an empty row
     // FP32 / BF16 plan (lazy)
     int tm32 = 0, num_tiles32 = 0, grid32 = 1, fix_grid32 = 1;
     int2* tiles32 = nullptr;
@@ -117,6 +118,7 @@ struct pwmgpu_matrix {
         dfree(M.col);
         dfree(M.val);
         dfree(tiles);
+        dfree(subflag);
         dfree(tiles32);
         dfree(val32);
         if (valbf) cudaFree(valbf);
@@ -166,16 +168,23 @@ int check_status(pwmgpu_matrix* m) {
     return PWMGPU_OK;
 }
 
-// Build the merge-path plan: tile coordinates for diagonals t*TM
-// (k_merge_partition) and the scratch the kernels need.
+// Build the merge-path plan: sub-tile boundaries at diagonals s*WM
+// (k_merge_partition) and the scratch the kernels need.  `num_tiles` counts
+// sub-tiles (the unit of carries and of the fix-up).
 int build_plan(pwmgpu_matrix* m) {
     const long long total = (long long)m->M.nor + m->M.nnz;
-    m->tm = merge_items_per_tile(m->cfg);
+    const MergeGeom g = merge_geometry(m->cfg);
+    m->tm = g.wm;
     m->num_tiles = (int)((total + m->tm - 1) / m->tm);
     dfree(m->tiles);
+    dfree(m->subflag);
     TRY(dalloc(&m->tiles, (size_t)m->num_tiles + 1));
-    if (m->num_tiles > 0)
+    TRY(dalloc(&m->subflag, (size_t)m->num_tiles + 1));
+    CU(cudaMemsetAsync(m->subflag, 0, (size_t)m->num_tiles + 1, m->stream));
+    if (m->num_tiles > 0) {
         CU(launch_merge_partition(m->M.row_start, m->M.nor, m->M.nnz, m->tm, m->num_tiles, m->tiles, m->stream));
+        CU(launch_mark_empty_rows(m->M.row_start, m->M.nor, m->tm, m->subflag, m->sm_count, m->stream));
+    }
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
     m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
     TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
@@ -227,8 +236,8 @@ int check_sizes(long long nor, long long noc, long long nnz) {
 
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->num_tiles == 0) return PWMGPU_OK;
-    CU(launch_merge_spmv_f64(m->cfg, kModeSpmv, m->M, m->tiles, m->num_tiles, m->grid, dx, dy, m->carries, nullptr,
-                             nullptr, m->status, m->stream));
+    CU(launch_merge_spmv(m->cfg, kModeSpmv, m->M, m->M.val, m->tiles, m->subflag, m->num_tiles, m->grid, dx, dy,
+                         m->carries, nullptr, nullptr, m->status, m->stream));
     CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->tiles, m->num_tiles, dy, m->carries, nullptr, nullptr, 0, nullptr,
                               m->fix_grid, nullptr, nullptr, m->stream));
     return PWMGPU_OK;
@@ -237,8 +246,8 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
 // One power-method step on device vectors: out = 2^e(nsq_in) * A in, and
 // nsq_out = ||out||^2 (deterministic).
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
-    CU(launch_merge_spmv_f64(m->cfg, kModePower, m->M, m->tiles, m->num_tiles, m->grid, in, out, m->carries, nsq_in,
-                             m->partials, m->status, m->stream));
+    CU(launch_merge_spmv(m->cfg, kModePower, m->M, m->M.val, m->tiles, m->subflag, m->num_tiles, m->grid, in, out,
+                         m->carries, nsq_in, m->partials, m->status, m->stream));
     CU(launch_merge_fixup_f64(kModePower, m->M, m->tiles, m->num_tiles, out, m->carries, nsq_in, m->partials,
                               m->grid, m->fix_partials, m->fix_grid, m->counter, nsq_out, m->stream));
     return PWMGPU_OK;
