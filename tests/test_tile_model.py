@@ -1,31 +1,38 @@
-"""CPU model of the merge kernel (thesis_spmv_gb300/csrc/merge.cuh and
-merge.cu), checked before any of it runs on a GPU:
+"""CPU model of the merge-path kernel (thesis_spmv_gb300/csrc/merge.cuh,
+merge.cu), checked before any of it runs on a GPU.
 
-* geometry: sub-tile ends are merge-path coordinates of the oracle's
-  searchPathOnDiag restatement (CRS_Merge.hpp:42-62) at diagonals s*WM; a
-  tile is W consecutive sub-tiles;
-* TMA windows: every staged window starts 16-byte aligned, has a size that is
-  a multiple of 16 bytes, fits its shared-memory capacity and stays inside
-  the array plus its kArrayPad padding; the row window covers every
-  row_start entry the lanes read;
-* algorithm: a step-by-step simulation of process_subtile (nonzero split over
-  32 lanes, row completion, the run-leader carry merge, the a < rw1 rule) and
-  of k_merge_fixup reproduces the oracle's y = A x within the row bound.
+Layout ("lane-interleaved merge-path CRS"): the merge path is cut into
+sub-tiles of WM = 32*IPT items, one per warp; sub-tile s spans the nonzeros
+[kw0, kw1) and hands lane l the contiguous range [kw0 + start_l, + cnt_l)
+(qm = nkw // 32, rem = nkw % 32, cnt_l = qm + (l < rem)).  Each array is
+stored per sub-tile at an 8-element-aligned base so that element j of lane l
+sits at mli_pos(l, j, qm, V): full V-blocks first (one 16-byte vector load per
+lane per block, coalesced across the warp), then a compact scalar tail.
+
+Checks: the permutation is a bijection into [base, base + nkw) and vector
+slots are 16-byte aligned; bases never overlap and stay inside the
+allocation; row-end masks, first rows and flags reproduce the CRS structure;
+a step-by-step simulation of the kernel (fast and general paths, carries,
+k_merge_fixup) reproduces the oracle's y = A x within the row bound and
+counts every row's square exactly once (power-method epilogue).
 """
 import numpy as np
 import pytest
 
 from oracle import pyoracle as O
 
-PAD = 16
+BIG = 2 ** 31 - 1
 
 
-def geometry(NT, IPT, vsize):
-    W = NT // 32
-    WM = 32 * IPT
-    TM = W * WM
-    VE = 16 // vsize
-    return dict(W=W, WM=WM, TM=TM, VE=VE, VAL_CAP=TM + 2 * VE, COL_CAP=TM + 8, ROW_CAP=TM + 12)
+def mli_pos(lane, j, qm, V):
+    B = qm // V
+    if j < V * B:
+        return (j // V) * 32 * V + lane * V + (j % V)
+    return 32 * V * B + (j - V * B) * 32 + lane
+
+
+def mli_base(kw0, s):
+    return 8 * ((kw0 + 7 * s + 7) // 8)
 
 
 def sub_coords(A, WM):
@@ -34,149 +41,136 @@ def sub_coords(A, WM):
     return [O.merge_search(A, min(s * WM, total)) for s in range(ns + 1)]
 
 
-def windows(r0, k0, r1, k1, nor, G):
-    nk = k1 - k0
-    rlast = min(r1, nor - 1)
-    VE = G["VE"]
-    k0a = k0 & ~(VE - 1)
-    k1a = ((k1 + VE - 1) & ~(VE - 1)) if nk else k0a
-    k0c = k0 & ~3
-    k1c = ((k1 + 3) & ~3) if nk else k0c
-    rs = r0 & ~3
-    re = (rlast + 2 + 3) & ~3
-    return (k0a, k1a), (k0c, k1c), (rs, re)
+def lane_range(kw0, kw1, lane):
+    nkw = kw1 - kw0
+    qm, rem = nkw >> 5, nkw & 31
+    start = lane * qm + min(lane, rem)
+    cnt = qm + (1 if lane < rem else 0)
+    return kw0 + start, cnt, qm, rem
 
 
-def check_windows(A, NT, IPT, vsize):
-    G = geometry(NT, IPT, vsize)
-    nor, nnz = A.nor, A.nnz
-    sc = sub_coords(A, G["WM"])
-    ns = len(sc) - 1
-    assert sc[0] == (0, 0) and sc[-1] == (nor, nnz)
-    nt = -(-ns // G["W"])
-    for t in range(nt):
-        s0, s1 = t * G["W"], min((t + 1) * G["W"], ns)
-        (r0, k0), (r1, k1) = sc[s0], sc[s1]
-        assert r0 <= nor - 1
-        assert (r1 - r0) + (k1 - k0) <= G["TM"]
-        (va, vb), (ca, cb), (ra, rb) = windows(r0, k0, r1, k1, nor, G)
-        assert (va * vsize) % 16 == 0 and ((vb - va) * vsize) % 16 == 0
-        assert (ca * 4) % 16 == 0 and ((cb - ca) * 4) % 16 == 0
-        assert (ra * 4) % 16 == 0 and ((rb - ra) * 4) % 16 == 0 and rb > ra
-        assert vb - va <= G["VAL_CAP"] and cb - ca <= G["COL_CAP"] and rb - ra <= G["ROW_CAP"]
-        assert vb <= nnz + PAD and cb <= nnz + PAD and rb <= nor + 1 + PAD
-        if k1 > k0:
-            assert va <= k0 and vb >= k1 and ca <= k0 and cb >= k1
-        rlast = min(r1, nor - 1)
-        assert ra <= r0 and rb >= rlast + 2  # row_start[r0 .. rlast+1] staged
-        for w in range(s1 - s0):
-            (rw0, kw0), (rw1, kw1) = sc[s0 + w], sc[s0 + w + 1]
-            assert r0 <= rw0 <= rw1 <= r1 and (rw1 - rw0) + (kw1 - kw0) <= G["WM"]
+def row_of(rs, b, lo, hi):
+    """largest a in [lo, hi] with row_start[a] <= b"""
+    while lo < hi:
+        mid = (lo + hi + 1) >> 1
+        if rs[mid] <= b:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
 
 
-def simulate(A, x, IPT):
-    """process_subtile for every sub-tile, then k_merge_fixup.  Returns y and
-    how many times each row's square entered the power method's ||y||^2
-    (must be exactly once)."""
+def plan(A, IPT):
+    """k_mli_plan: permuted arrays, per-lane row-end masks, per-sub-tile meta."""
     WM = 32 * IPT
+    rs = A.row_start
     sc = sub_coords(A, WM)
     ns = len(sc) - 1
-    rs = A.row_start
-    nor = A.nor
-    BIG = 2 ** 31 - 1
-    y = np.full(nor, np.nan)
-    counted = np.zeros(nor, np.int64)
-    carries = np.zeros(ns)
-    # k_mark_empty_rows: sub-tiles holding the end item of an empty row
-    slow = np.zeros(ns + 1, bool)
-    for r in range(nor):
-        if rs[r + 1] == rs[r]:
-            slow[(rs[r + 1] + r) // WM] = True
+    size = A.nnz + 7 * ns + 16
+    valp = np.full(size, np.nan)
+    colp = np.full(size, -1, np.int64)
+    masks = np.zeros((ns, 32), np.int64)
+    meta = []
     for s in range(ns):
         (rw0, kw0), (rw1, kw1) = sc[s], sc[s + 1]
         nkw = kw1 - kw0
-        q = (nkw + 31) >> 5
-        assert q <= IPT
-        lane_a, lane_acc, lane_b0 = [], [], []
+        base = mli_base(kw0, s)
+        fr = row_of(rs, kw0, rw0, rw1) if nkw > 0 else rw1
+        has_empty = any(rs[r] == rs[r + 1] for r in range(rw0, rw1))
+        open0 = nkw > 0 and rs[fr] < kw0
         for lane in range(32):
-            b0 = kw0 + lane * q
-            qe = min(max(kw1 - b0, 0), q)
-            a, rend = rw1, BIG
-            if qe > 0:
-                lo, hi = rw0, rw1
-                while lo < hi:
-                    mid = (lo + hi + 1) >> 1
-                    if rs[mid] <= b0:
-                        lo = mid
-                    else:
-                        hi = mid - 1
-                a = lo
-                assert rs[a] <= b0 < rs[a + 1] or a == rw1
-                rend = rs[a + 1] if a < rw1 else BIG
-            lane_a.append(a)
-            lane_b0.append((b0, qe, rend))
-        # rows [rw0, a_lane0) carry no nonzeros here
-        for r in range(rw0, lane_a[0]):
+            b0, cnt, qm, rem = lane_range(kw0, kw1, lane)
+            if cnt == 0:
+                continue
+            a = row_of(rs, b0, rw0, rw1)
+            m = 0
+            for j in range(cnt):
+                b = b0 + j
+                while a < rw1 and rs[a + 1] <= b:  # row a ends before b (empty rows)
+                    a += 1
+                if a < rw1 and b + 1 == rs[a + 1]:
+                    m |= 1 << j
+                pv, pc = mli_pos(lane, j, qm, 2), mli_pos(lane, j, qm, 4)
+                assert np.isnan(valp[base + pv]) and colp[base + pc] == -1
+                valp[base + pv] = A.data[b]
+                colp[base + pc] = A.col_ind[b]
+            masks[s, lane] = m
+        meta.append((fr, int(has_empty), int(open0), base))
+    return sc, valp, colp, masks, meta
+
+
+def simulate(A, x, IPT):
+    """The kernel (fast path unless the sub-tile holds an empty row) and
+    k_merge_fixup; returns y and per-row counts of squares summed."""
+    sc, valp, colp, masks, meta = plan(A, IPT)
+    rs, nor = A.row_start, A.nor
+    ns = len(sc) - 1
+    y = np.full(nor, np.nan)
+    counted = np.zeros(nor, np.int64)
+    carries = np.zeros(ns)
+    for s in range(ns):
+        (rw0, kw0), (rw1, kw1) = sc[s], sc[s + 1]
+        fr, has_empty, open0, base = meta[s]
+        nkw = kw1 - kw0
+        qm, rem = nkw >> 5, nkw & 31
+        q = qm + (1 if rem else 0)
+        # per lane: values / gathers, row-end masks
+        lanes = []
+        for lane in range(32):
+            b0, cnt, _, _ = lane_range(kw0, kw1, lane)
+            vv = [valp[base + mli_pos(lane, j, qm, 2)] if j < cnt else 0.0 for j in range(IPT)]
+            xv = [x[colp[base + mli_pos(lane, j, qm, 4)]] if j < cnt else 0.0 for j in range(IPT)]
+            lanes.append((b0, cnt, vv, xv, int(masks[s, lane])))
+        # rows [rw0, fr) carry no nonzeros in this sub-tile
+        for r in range(rw0, fr):
             y[r] = 0.0
+            if rs[r] == rs[r + 1]:
+                counted[r] += 1
+        # first rows: exclusive prefix of popcounts (fast) or search (general)
+        pc = [bin(l[4]).count("1") for l in lanes]
         crow, cval, hval = [], [], [None] * 32
         for lane in range(32):
-            b0, qe, rend = lane_b0[lane]
-            a = lane_a[lane]
-            head_open = qe > 0 and rs[a] < b0
-            acc, first = 0.0, True
-            if not slow[s]:
-                mask = 0
-                r = a
-                while r < rw1:
-                    rr = rs[r + 1]
-                    if rr > b0 + qe:
-                        break
-                    assert 0 <= rr - b0 - 1 < IPT and not (mask >> (rr - b0 - 1)) & 1
-                    mask |= 1 << (rr - b0 - 1)
-                    r += 1
-                to_head = head_open and lane > 0
-                count = not head_open
-                for j in range(IPT):
-                    if j < q:
-                        if j < qe:
-                            acc = acc + A.data[b0 + j] * x[A.col_ind[b0 + j]]
-                        if (mask >> j) & 1:
-                            if to_head:
-                                hval[lane] = acc
-                                to_head = False
-                            else:
-                                y[a] = acc
-                                if count:
-                                    counted[a] += 1
-                            count = True
-                            acc = 0.0
-                            a += 1
-                crow.append(a)
-                cval.append(acc)
-                continue
+            b0, cnt, vv, xv, m = lanes[lane]
+            if not has_empty:
+                a = fr + sum(pc[:lane])
+                if cnt:
+                    assert rs[a] <= b0 < rs[a + 1] or a == rw1
+                if lane == 0:
+                    head_open = bool(open0)
+                else:
+                    pb, pcnt = lanes[lane - 1][0], lanes[lane - 1][1]
+                    head_open = cnt > 0 and not ((lanes[lane - 1][4] >> (pcnt - 1)) & 1)
+                assert head_open == (cnt > 0 and rs[a] < b0)
+            else:
+                a = row_of(rs, b0, rw0, rw1) if cnt else rw1
+                head_open = cnt > 0 and rs[a] < b0
+            to_head = head_open and lane > 0
+            count = not head_open
+            acc = 0.0
             for j in range(IPT):
                 if j < q:
-                    if j < qe:
-                        acc = acc + A.data[b0 + j] * x[A.col_ind[b0 + j]]
-                    bn = b0 + j + 1
-                    if j < qe and bn == rend:
-                        if first and head_open and lane > 0:
+                    acc = acc + vv[j] * xv[j]
+                    if (m >> j) & 1:
+                        if to_head:
                             hval[lane] = acc
+                            to_head = False
                         else:
                             y[a] = acc
-                            if not (first and head_open):
+                            if count:
                                 counted[a] += 1
-                        acc, first = 0.0, False
+                        count = True
+                        acc = 0.0
                         a += 1
-                        rend = rs[a + 1] if a < rw1 else BIG
-                        while rend == bn:
-                            y[a] = 0.0
-                            counted[a] += 1  # an empty row's square (0) is final here
-                            a += 1
-                            rend = rs[a + 1] if a < rw1 else BIG
+                        if has_empty:  # general path: pass empty rows
+                            while a < rw1 and rs[a + 1] == rs[a]:
+                                y[a] = 0.0
+                                counted[a] += 1
+                                a += 1
+            if cnt == 0:
+                a = rw1
             crow.append(a)
             cval.append(acc)
-        assert crow[31] == rw1
+        assert crow[31] == rw1, (crow, rw1)
         for lane in range(32):
             a = crow[lane]
             if lane == 0 or crow[lane - 1] != a:
@@ -186,7 +180,8 @@ def simulate(A, x, IPT):
                     tot += cval[u]
                     u += 1
                 if a < rw1:
-                    if rs[a] < kw0 + u * q:
+                    b0u = lanes[u][0]
+                    if rs[a] < b0u:
                         assert hval[u] is not None
                         y[a] = hval[u] + tot
                         if rs[a] >= kw0:
@@ -195,9 +190,7 @@ def simulate(A, x, IPT):
                         assert tot == 0.0
                 elif a < nor:
                     carries[s] = tot
-    # empty rows zeroed before lane 0's first row are final there too
-    # (k_merge_fixup counts the open row rw0 of a sub-tile instead)
-    for t in range(ns):
+    for t in range(ns):  # k_merge_fixup
         r = sc[t + 1][0]
         if r >= nor or (t > 0 and sc[t][0] == r):
             continue
@@ -227,7 +220,6 @@ def _random_csr(n, mean_len, seed, noc=None, empty_frac=0.0, dense_rows=0, dense
     return O.CRSArrays(n, noc, rs, cols, rng.uniform(-1, 1, int(lens.sum())))
 
 
-CONFIGS = [(128, 12, 8), (128, 8, 8), (128, 12, 4), (128, 12, 2)]
 MATRICES = {
     "poisson1x1": lambda: O.fill_poisson(1, 1),
     "poisson2x3": lambda: O.fill_poisson(2, 3),
@@ -237,17 +229,38 @@ MATRICES = {
     "nnz0": lambda: _random_csr(700, 0, 3),
     "all_empty": lambda: O.CRSArrays(5, 5, np.zeros(6, np.int32), np.zeros(0, np.int32), np.zeros(0)),
     "wide": lambda: _random_csr(300, 40, 4, noc=5000),
-    "long_rows_exact": lambda: _random_csr(400, 224, 5, noc=600),
+    "long_rows": lambda: _random_csr(400, 224, 5, noc=600),
+    "short_rows": lambda: _random_csr(3000, 1, 6),
 }
 
 
-@pytest.mark.parametrize("cfg", CONFIGS)
+@pytest.mark.parametrize("IPT", [8, 10, 12])
 @pytest.mark.parametrize("name", sorted(MATRICES))
-def test_windows(cfg, name):
-    check_windows(MATRICES[name](), *cfg)
+def test_layout(IPT, name):
+    A = MATRICES[name]()
+    sc, valp, colp, masks, meta = plan(A, IPT)
+    ns = len(sc) - 1
+    size = A.nnz + 7 * ns + 16
+    for s in range(ns):
+        (rw0, kw0), (rw1, kw1) = sc[s], sc[s + 1]
+        nkw = kw1 - kw0
+        base = meta[s][3]
+        assert base % 8 == 0 and base + nkw <= size
+        if s + 1 < ns:
+            assert mli_base(sc[s + 1][1], s + 1) >= base + nkw  # no overlap
+        qm = nkw >> 5
+        assert (nkw + 31) >> 5 <= IPT
+        for V in (2, 4, 8):
+            pos = sorted(mli_pos(l, j, qm, V) for l in range(32) for j in range(lane_range(kw0, kw1, l)[1]))
+            assert pos == list(range(nkw))  # bijection onto [0, nkw)
+            for l in range(32):
+                for blk in range(qm // V):  # V-element vector slots start at multiples of V: 16 bytes
+                    assert (base + mli_pos(l, blk * V, qm, V)) % V == 0
+    # all nonzeros placed exactly once
+    assert np.count_nonzero(~np.isnan(valp)) == A.nnz and np.count_nonzero(colp >= 0) == A.nnz
 
 
-@pytest.mark.parametrize("IPT", [8, 12])
+@pytest.mark.parametrize("IPT", [8, 10, 12])
 @pytest.mark.parametrize("name", sorted(MATRICES))
 def test_algorithm_simulation(IPT, name):
     A = MATRICES[name]()
@@ -256,8 +269,6 @@ def test_algorithm_simulation(IPT, name):
     ref = O.crs_mv(A, x)
     assert not np.isnan(y).any()
     assert np.all(np.abs(y - ref) <= O.row_error_bound(A, x) + 1e-300)
-    # every nonempty-or-open row's square is summed exactly once; rows with no
-    # nonzeros at all may be counted 0 or 1 times (their square is 0)
     nz = np.diff(A.row_start) > 0
     assert np.all(counted[nz] == 1), np.nonzero(counted[nz] != 1)[0][:10]
     assert np.all(counted <= 1)

@@ -22,26 +22,45 @@ struct DevMatrix {
 enum { kModeSpmv = 0, kModePower = 1 };
 
 // merge.cu
-// Merge-path kernel configurations.
-enum { kCfgF64 = 0, kCfgF64Small = 1, kCfgF32 = 2, kCfgBF16 = 3 };
+// Items per lane of a merge-path sub-tile (a sub-tile is 32 * kMliIpt merge
+// items, one warp); the lane-interleaved storage is laid out for this size.
+constexpr int kMliIpt = 12;
+
+// Merge-path kernel configurations (value / vector / accumulation types).
+enum { kCfgF64 = 0, kCfgF32 = 2, kCfgBF16 = 3 };
 struct MergeGeom {
     int wm;    // merge items per sub-tile (one warp)
-    int w;     // sub-tiles per tile (warps per CTA)
+    int w;     // warps per CTA
     int smem;  // dynamic shared memory per CTA
     int occ;   // resident CTAs per SM
     int nt;    // threads per CTA
 };
+
+// Per-matrix plan of the merge-path kernel: sub-tile boundaries, metadata,
+// row-end masks and the lane-interleaved column / FP64 value arrays.
+struct MliPlan {
+    int nsub = 0;
+    int2* subc = nullptr;       // nsub + 1 merge coordinates (row, nonzero)
+    int4* rec = nullptr;        // 2 x nsub: {rw0, kw0, rw1, kw1}, {first row, flags, base, nkw}
+    uint16_t* masks = nullptr;  // nsub x 32 row-end masks
+    int32_t* colp = nullptr;    // lane-interleaved column indices
+    double* valp = nullptr;     // lane-interleaved FP64 values
+};
+long long mli_storage_elems(long long nnz, long long nsub);
+
 MergeGeom merge_geometry(int cfg);
 int merge_grid(int cfg, int nsub, int sm_count);
 int fixup_grid(int num_tiles, int sm_count);
 int dot_grid(long long n, int sm_count);
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
                                    int2* out, cudaStream_t st);
-cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* val, const int2* subc,
-                              const uint8_t* subflag, int nsub, int grid, const void* x, void* y, void* carries,
-                              const double* nsq_in, double* partials, int* status, cudaStream_t st);
-cudaError_t launch_mark_empty_rows(const int32_t* row_start, int nor, int wm, uint8_t* flags, int sm_count,
-                                   cudaStream_t st);
+cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
+                            int sm_count, cudaStream_t st);
+cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st);
+cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
+cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
+                              const void* x, void* y, void* carries, const double* nsq_in, double* partials,
+                              int* status, cudaStream_t st);
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
                                    const double* carries, const double* nsq_in, const double* spmv_partials,
                                    int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,

@@ -30,26 +30,104 @@ __global__ void k_merge_partition(const int32_t* __restrict__ row_start, int nor
     }
 }
 
-// Sub-tiles that hold an empty row (its end item lies at diagonal
-// row_start[r+1] + r) take the general path of the tile kernel.
-__global__ void k_mark_empty_rows(const int32_t* __restrict__ row_start, int nor, int wm, uint8_t* flags) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nor; r += gridDim.x * blockDim.x) {
-        const int e = row_start[r + 1];
-        if (e == row_start[r]) flags[(e + r) / wm] = 1;
+// ---------------------------------------------------------------------------
+// Plan: lane-interleaved storage, row-end masks and per-sub-tile metadata.
+// One warp per sub-tile (see merge.cuh for the layout).
+//   rec[2s]   = {rw0, kw0, rw1, kw1}: the sub-tile's merge coordinates
+//   rec[2s+1] = {fr: row holding the sub-tile's first nonzero (rw1 if none),
+//                flags: kFlagGeneral if an empty row completes here,
+//                       kFlagOpen0 if row fr began in an earlier sub-tile,
+//                base: storage base of the sub-tile, nkw}
+// ---------------------------------------------------------------------------
+__global__ void k_mli_plan(const int32_t* __restrict__ row_start, const int32_t* __restrict__ col,
+                           const double* __restrict__ val, const int2* __restrict__ subc, int nsub,
+                           int32_t* __restrict__ colp, double* __restrict__ valp, uint16_t* __restrict__ masks,
+                           int4* __restrict__ rec) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
+        const int2 c0 = subc[s], c1 = subc[s + 1];
+        const int rw0 = c0.x, kw0 = c0.y, rw1 = c1.x, kw1 = c1.y;
+        const int nkw = kw1 - kw0;
+        const int qm = nkw >> 5, rem = nkw & 31;
+        const int cnt = qm + (lane < rem ? 1 : 0);
+        const int b0 = kw0 + lane * qm + (lane < rem ? lane : rem);
+        const long long base = mli_base(kw0, s);
+        // an empty row whose end item lies in this sub-tile?
+        bool empty_here = false;
+        for (int r = rw0 + lane; r < rw1; r += 32) empty_here |= (row_start[r] == row_start[r + 1]);
+        const bool general = __any_sync(0xffffffffu, empty_here);
+        uint32_t m = 0;
+        if (cnt > 0) {
+            int a = row_of(row_start, b0, rw0, rw1);
+            for (int j = 0; j < cnt; ++j) {
+                const int b = b0 + j;
+                while (a < rw1 && row_start[a + 1] <= b) ++a;  // past empty rows
+                if (a < rw1 && b + 1 == row_start[a + 1]) m |= 1u << j;
+                colp[base + mli_pos(lane, j, qm, 4)] = col[b];
+                valp[base + mli_pos(lane, j, qm, 2)] = val[b];
+            }
+        }
+        masks[(long long)s * 32 + lane] = (uint16_t)m;
+        if (lane == 0) {
+            const int fr = nkw > 0 ? row_of(row_start, kw0, rw0, rw1) : rw1;
+            int flags = general ? kFlagGeneral : 0;
+            if (nkw > 0 && row_start[fr] < kw0) flags |= kFlagOpen0;
+            rec[2LL * s] = make_int4(rw0, kw0, rw1, kw1);
+            rec[2LL * s + 1] = make_int4(fr, flags, (int)base, nkw);
+        }
+    }
+}
+
+// Values in another precision / vector width: element (l, j) moves from
+// mli_pos(l, j, qm, 2) (FP64) to mli_pos(l, j, qm, 16/sizeof(T)).
+template <typename T>
+__global__ void k_mli_convert(const double* __restrict__ valp, const int2* __restrict__ subc,
+                              const int4* __restrict__ rec, int nsub, T* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    constexpr int V = 16 / (int)sizeof(T);
+    for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
+        const int nkw = subc[s + 1].y - subc[s].y;
+        const int qm = nkw >> 5, rem = nkw & 31;
+        const int cnt = qm + (lane < rem ? 1 : 0);
+        const long long base = rec[2LL * s + 1].z;
+        for (int j = 0; j < cnt; ++j) out[base + mli_pos(lane, j, qm, V)] = (T)valp[base + mli_pos(lane, j, qm, 2)];
+    }
+}
+
+// Back to CRS order (for reading the matrix out).
+__global__ void k_mli_unpermute(const int32_t* __restrict__ colp, const double* __restrict__ valp,
+                                const int2* __restrict__ subc, const int4* __restrict__ rec, int nsub,
+                                int32_t* __restrict__ col, double* __restrict__ val) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
+        const int kw0 = subc[s].y, nkw = subc[s + 1].y - kw0;
+        const int qm = nkw >> 5, rem = nkw & 31;
+        const int cnt = qm + (lane < rem ? 1 : 0);
+        const int b0 = kw0 + lane * qm + (lane < rem ? lane : rem);
+        const long long base = rec[2LL * s + 1].z;
+        for (int j = 0; j < cnt; ++j) {
+            col[b0 + j] = colp[base + mli_pos(lane, j, qm, 4)];
+            val[b0 + j] = valp[base + mli_pos(lane, j, qm, 2)];
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
-// K2: merge-path SpMV (plain or with the power-method epilogue)
+// K2: merge-path SpMV (plain or with the power-method epilogue).  Each warp
+// takes sub-tiles s = global warp, + total warps, ... and double-buffers them
+// through its own shared-memory stages (TMA bulk copies, mbarriers).
 // ---------------------------------------------------------------------------
 template <typename VT, typename XT, typename AT>
 struct MergeArgs {
     const int32_t* row_start;
-    const int32_t* col;
-    const VT* val;
-    const int2* subc;        // sub-tile boundaries, nsub + 1 entries
-    const uint8_t* subflag;  // 1 if the sub-tile holds an empty row
-    int nor, nnz, nsub, num_tiles;
+    const int32_t* colp;
+    const VT* valp;
+    const int4* rec;
+    const uint16_t* masks;
+    int nor, nsub;
     const XT* x;
     XT* y;
     AT* carries;           // one per sub-tile
@@ -58,63 +136,72 @@ struct MergeArgs {
     int* status;
 };
 
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int STAGES>
-__global__ void __launch_bounds__(NT, (MergeLayout<VT, XT, AT, NT, IPT, STAGES>::MINB)) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
-    using L = MergeLayout<VT, XT, AT, NT, IPT, STAGES>;
+constexpr int kMliStages = 2;
+
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT>
+__global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
+    using S = WarpStage<VT, IPT>;
+    constexpr int W = NT / 32;
+    constexpr int NS = kMliStages;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    MergeSmem<VT, XT, AT, NT, IPT, STAGES> sm{smem_raw};
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int G = gridDim.x;
-    const int my_tiles = (int)blockIdx.x < a.num_tiles ? (a.num_tiles - 1 - (int)blockIdx.x) / G + 1 : 0;
+    __shared__ uint64_t bars[W][NS];
+    __shared__ int crow[NT];
+    __shared__ AT cval[NT];
+    __shared__ AT hval[NT];
+    __shared__ double red[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
+    const int gw = blockIdx.x * W + w, tw = gridDim.x * W;
+    const int n = gw < a.nsub ? (a.nsub - 1 - gw) / tw + 1 : 0;  // this warp's sub-tiles
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
     const uint64_t pol = policy_evict_first();
-    const bool producer = (tid == 0);
 
-    if (producer) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&sm.full()[s], 1);
-            mbar_init(&sm.empty()[s], L::W);
-        }
+    int4 pref = make_int4(0, 0, 0, 0);
+    if (lane == 0) {
+        for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
         fence_mbar_init();
+        for (int k = 0; k < NS && k < n; ++k) {
+            const int s = gw + k * tw;
+            issue_subtile<VT, IPT>(stages + k * S::BYTES, &bars[w][k], s, __ldg(a.rec + 2LL * s + 1), a.rec,
+                                   a.masks, a.colp, a.valp, pol);
+        }
+        if (n > NS) pref = __ldg(a.rec + 2LL * (gw + NS * tw) + 1);
     }
-    __syncthreads();
-    int issued = 0;
-    if (producer)
-        for (; issued < STAGES && issued < my_tiles; ++issued)
-            issue_tile(sm, issued, blockIdx.x + issued * G, a.subc, a.subflag, a.nsub, a.row_start, a.col, a.val, a.nor,
-                       pol);
+    __syncwarp();
 
     double sumsq = 0.0;
     int i = 0;
-    for (; i < my_tiles; ++i) {
-        const int s = i % STAGES;
-        bool ok = true;
-        // Producer: refill the stage tile i-1 used once every warp released it.
-        if (producer && i >= 1 && i - 1 + STAGES < my_tiles) {
-            const int sp = (i - 1) % STAGES;
-            ok = mbar_wait_bounded(&sm.empty()[sp], (uint32_t)((i - 1) / STAGES) & 1u, a.status);
-            if (ok) {
-                issue_tile(sm, sp, blockIdx.x + (i - 1 + STAGES) * G, a.subc, a.subflag, a.nsub, a.row_start, a.col,
-                           a.val,
-                           a.nor, pol);
-                ++issued;
-            }
-        }
-        if (ok) ok = mbar_wait_bounded(&sm.full()[s], (uint32_t)(i / STAGES) & 1u, a.status);
+    for (; i < n; ++i) {
+        const int s = gw + i * tw;
+        const int k = i % NS;
+        unsigned char* st = stages + k * S::BYTES;
+        const bool ok = mbar_wait_bounded(&bars[w][k], (uint32_t)(i / NS) & 1u, a.status);
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
-        process_subtile<MODE>(sm, s, blockIdx.x + i * G, a.x, a.y, a.carries, a.nor, e, sumsq);
-        if (lane == 0) mbar_arrive(&sm.empty()[s]);
+        AT xv[IPT];
+        gather_subtile<VT, XT, AT, IPT>(st, a.x, xv);
+        if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
+            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, a.y, a.carries, a.nor, e, sumsq,
+                                                        crow + 32 * w, cval + 32 * w, hval + 32 * w);
+        else
+            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, a.y, a.carries, a.nor, e, sumsq,
+                                                         crow + 32 * w, cval + 32 * w, hval + 32 * w);
+        // every lane is done with this stage (finish_subtile ends with a warp
+        // barrier): refill it with sub-tile i + NS
+        if (lane == 0 && i + NS < n) {
+            fence_proxy_async();
+            issue_subtile<VT, IPT>(st, &bars[w][k], s + NS * tw, pref, a.rec, a.masks, a.colp, a.valp, pol);
+            pref = (i + NS + 1 < n) ? __ldg(a.rec + 2LL * (s + (NS + 1) * tw) + 1) : make_int4(0, 0, 0, 0);
+        }
     }
-    if (producer && i < my_tiles) {
-        // Leaving early after a timeout: let copies already in flight land
+    if (lane == 0 && i < n) {
+        // Leaving early after a timeout: let this warp's copies in flight land
         // (short bounded waits) before the CTA's shared memory goes away.
-        for (int t = i; t < issued; ++t)
-            mbar_wait_bounded(&sm.full()[t % STAGES], (uint32_t)(t / STAGES) & 1u, a.status, kWaitCycles / 8,
-                              false);
+        for (int t = i; t < n && t < i + NS; ++t)
+            mbar_wait_bounded(&bars[w][t % NS], (uint32_t)(t / NS) & 1u, a.status, kWaitCycles / 8, false);
     }
     if (MODE == MODE_POWER) {
-        double t = block_sum<NT>(sumsq, sm.red());
-        if (tid == 0) a.partials[blockIdx.x] = t;
+        double t = block_sum<NT>(sumsq, red);
+        if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
     }
 }
 
@@ -323,62 +410,61 @@ __global__ void k_convert<double, __nv_bfloat16>(const double* __restrict__ s, _
 // Host launchers
 // ===========================================================================
 
-// Tile configurations (threads per CTA, items per lane, pipeline stages).
-template <typename VT, typename XT, typename AT, int NT, int IPT, int STAGES>
+long long mli_storage_elems(long long nnz, long long nsub) { return mli_size(nnz, nsub); }
+
+// Kernel configurations (threads per CTA, items per lane).
+template <typename VT, typename XT, typename AT, int NT, int IPT>
 struct MergeKernels {
-    using L = MergeLayout<VT, XT, AT, NT, IPT, STAGES>;
-    static constexpr int SMEM = L::BYTES;
+    static constexpr int SMEM = (NT / 32) * kMliStages * WarpStage<VT, IPT>::BYTES;
 
     static MergeGeom geom() {
         static int occ = -1;
         if (occ < 0) {
-            auto k = k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, STAGES>;
-            auto kp = k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, STAGES>;
+            auto k = k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT>;
+            auto kp = k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT>;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
             cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
             int o = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM);
             occ = o > 0 ? o : 1;
         }
-        return MergeGeom{L::WM, L::W, SMEM, occ, NT};
+        return MergeGeom{32 * IPT, NT / 32, SMEM, occ, NT};
     }
 
-    static cudaError_t spmv(int mode, const DevMatrix& M, const void* val, const int2* subc, const uint8_t* subflag,
-                            int nsub, int grid, const void* x, void* y, void* carries, const double* nsq_in,
-                            double* partials, int* status, cudaStream_t st) {
+    static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
+                            const void* x, void* y, void* carries, const double* nsq_in, double* partials,
+                            int* status, cudaStream_t st) {
         geom();
-        const int num_tiles = (nsub + L::W - 1) / L::W;
-        MergeArgs<VT, XT, AT> a{M.row_start, M.col, (const VT*)val, subc, subflag, M.nor, (int)M.nnz, nsub, num_tiles,
+        MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub,
                                 (const XT*)x, (XT*)y, (AT*)carries, nsq_in, partials, status};
         if (mode == MODE_POWER)
-            k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, STAGES><<<grid, NT, SMEM, st>>>(a);
+            k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT><<<grid, NT, SMEM, st>>>(a);
         else
-            k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, STAGES><<<grid, NT, SMEM, st>>>(a);
+            k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT><<<grid, NT, SMEM, st>>>(a);
         return cudaGetLastError();
     }
 };
 
 // The configurations the library instantiates (ids are stable: the
-// autotuner cache stores them).
-using CfgF64a = MergeKernels<double, double, double, 128, 12, 2>;       // kCfgF64
-using CfgF64b = MergeKernels<double, double, double, 128, 8, 2>;        // kCfgF64Small
-using CfgF32 = MergeKernels<float, float, float, 128, 12, 2>;           // kCfgF32
-using CfgBF16 = MergeKernels<__nv_bfloat16, float, float, 128, 12, 2>;  // kCfgBF16
+// autotuner cache stores them).  All share IPT = 12 (the storage layout
+// depends on the sub-tile size), and differ in value type.
+using CfgF64 = MergeKernels<double, double, double, 128, kMliIpt>;
+using CfgF32 = MergeKernels<float, float, float, 128, kMliIpt>;
+using CfgBF16 = MergeKernels<__nv_bfloat16, float, float, 128, kMliIpt>;
 
 MergeGeom merge_geometry(int cfg) {
     switch (cfg) {
-        case kCfgF64Small: return CfgF64b::geom();
         case kCfgF32: return CfgF32::geom();
         case kCfgBF16: return CfgBF16::geom();
-        default: return CfgF64a::geom();
+        default: return CfgF64::geom();
     }
 }
 
 int merge_grid(int cfg, int nsub, int sm_count) {
     MergeGeom g = merge_geometry(cfg);
-    long long tiles = (nsub + g.w - 1) / g.w;
+    long long ctas = (nsub + g.w - 1) / g.w;
     long long grid = (long long)g.occ * sm_count;
-    if (grid > tiles) grid = tiles;
+    if (grid > ctas) grid = ctas;
     return grid > 0 ? (int)grid : 1;
 }
 
@@ -391,28 +477,46 @@ cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long 
     return cudaGetLastError();
 }
 
-cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* val, const int2* subc,
-                              const uint8_t* subflag, int nsub, int grid, const void* x, void* y, void* carries,
-                              const double* nsq_in, double* partials, int* status, cudaStream_t st) {
-    switch (cfg) {
-        case kCfgF64Small:
-            return CfgF64b::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
-        case kCfgF32:
-            return CfgF32::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
-        case kCfgBF16:
-            return CfgBF16::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
-        default:
-            return CfgF64a::spmv(mode, M, val, subc, subflag, nsub, grid, x, y, carries, nsq_in, partials, status, st);
-    }
+static int warp_grid(int nsub, int sm_count) {
+    long long g = (nsub + 7) / 8;
+    if (g > (long long)sm_count * 32) g = (long long)sm_count * 32;
+    return g > 0 ? (int)g : 1;
 }
 
-cudaError_t launch_mark_empty_rows(const int32_t* row_start, int nor, int wm, uint8_t* flags, int sm_count,
-                                   cudaStream_t st) {
-    if (nor <= 0) return cudaSuccess;
-    long long blocks = (nor + 255) / 256;
-    if (blocks > sm_count * 16) blocks = sm_count * 16;
-    k_mark_empty_rows<<<(int)blocks, 256, 0, st>>>(row_start, nor, wm, flags);
+cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
+                            int sm_count, cudaStream_t st) {
+    if (P.nsub == 0) return cudaSuccess;
+    k_mli_plan<<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(row_start, col, val, P.subc, P.nsub, P.colp, P.valp,
+                                                             P.masks, P.rec);
     return cudaGetLastError();
+}
+
+cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st) {
+    if (P.nsub == 0) return cudaSuccess;
+    if (cfg == kCfgBF16)
+        k_mli_convert<__nv_bfloat16><<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(P.valp, P.subc, P.rec, P.nsub,
+                                                                                   (__nv_bfloat16*)out);
+    else
+        k_mli_convert<float><<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(P.valp, P.subc, P.rec, P.nsub,
+                                                                           (float*)out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st) {
+    if (P.nsub == 0) return cudaSuccess;
+    k_mli_unpermute<<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(P.colp, P.valp, P.subc, P.rec, P.nsub, col, val);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
+                              const void* x, void* y, void* carries, const double* nsq_in, double* partials,
+                              int* status, cudaStream_t st) {
+    if (P.nsub == 0) return cudaSuccess;
+    switch (cfg) {
+        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
+        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
+        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
+    }
 }
 
 template <typename XT, typename AT>

@@ -80,14 +80,12 @@ struct pwmgpu_matrix {
 
     DevMatrix M;
 
-    // merge-path plan (FP64 kernel)
-    int cfg = 0;
+    // merge-path plan: sub-tiles of tm merge items (num_tiles of them), the
+    // lane-interleaved arrays, and launch geometry
+    int cfg = kCfgF64;
     int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
-    int2* tiles = nullptr;
-    uint8_t* subflag = nullptr;  // per sub-tile: holds an empty row
-    // FP32 / BF16 plan (lazy)
-    int tm32 = 0, num_tiles32 = 0, grid32 = 1, fix_grid32 = 1;
-    int2* tiles32 = nullptr;
+    MliPlan P;
+    // lane-interleaved FP32 / BF16 copies of the values (lazy)
     float* val32 = nullptr;
     void* valbf = nullptr;
     int bf16_exact = -1;
@@ -117,15 +115,18 @@ struct pwmgpu_matrix {
         dfree(M.row_start);
         dfree(M.col);
         dfree(M.val);
-        dfree(tiles);
-        dfree(subflag);
-        dfree(tiles32);
+        dfree(P.subc);
+        dfree(P.rec);
+        dfree(P.masks);
+        dfree(P.colp);
+        dfree(P.valp);
+        P = MliPlan();
         dfree(val32);
         if (valbf) cudaFree(valbf);
         valbf = nullptr;
         bf16_exact = -1;
         M = DevMatrix();
-        num_tiles = num_tiles32 = 0;
+        num_tiles = 0;
         loaded = false;
     }
     void release_all() {
@@ -168,30 +169,38 @@ int check_status(pwmgpu_matrix* m) {
     return PWMGPU_OK;
 }
 
-// Build the merge-path plan: sub-tile boundaries at diagonals s*WM
-// (k_merge_partition) and the scratch the kernels need.  `num_tiles` counts
-// sub-tiles (the unit of carries and of the fix-up).
+// Build the merge-path plan from the CRS arrays in M: sub-tile boundaries at
+// diagonals s*WM (k_merge_partition), then the lane-interleaved columns and
+// values, row-end masks and metadata (k_mli_plan).  The CRS column / value
+// arrays are released afterwards; row_start stays (fix-up, general path).
 int build_plan(pwmgpu_matrix* m) {
     const long long total = (long long)m->M.nor + m->M.nnz;
     const MergeGeom g = merge_geometry(m->cfg);
     m->tm = g.wm;
     m->num_tiles = (int)((total + m->tm - 1) / m->tm);
-    dfree(m->tiles);
-    dfree(m->subflag);
-    TRY(dalloc(&m->tiles, (size_t)m->num_tiles + 1));
-    TRY(dalloc(&m->subflag, (size_t)m->num_tiles + 1));
-    CU(cudaMemsetAsync(m->subflag, 0, (size_t)m->num_tiles + 1, m->stream));
-    if (m->num_tiles > 0) {
-        CU(launch_merge_partition(m->M.row_start, m->M.nor, m->M.nnz, m->tm, m->num_tiles, m->tiles, m->stream));
-        CU(launch_mark_empty_rows(m->M.row_start, m->M.nor, m->tm, m->subflag, m->sm_count, m->stream));
+    MliPlan& P = m->P;
+    P.nsub = m->num_tiles;
+    const long long elems = mli_storage_elems(m->M.nnz, P.nsub);
+    TRY(dalloc(&P.subc, (size_t)P.nsub + 1));
+    TRY(dalloc(&P.rec, 2 * (size_t)P.nsub + 2));
+    TRY(dalloc(&P.masks, (size_t)P.nsub * 32 + 32));
+    TRY(dalloc(&P.colp, (size_t)elems));
+    TRY(dalloc(&P.valp, (size_t)elems));
+    // gaps between sub-tiles are never read by the kernels; keep them defined
+    CU(cudaMemsetAsync(P.colp, 0, sizeof(int32_t) * (size_t)elems, m->stream));
+    CU(cudaMemsetAsync(P.valp, 0, sizeof(double) * (size_t)elems, m->stream));
+    if (P.nsub > 0) {
+        CU(launch_merge_partition(m->M.row_start, m->M.nor, m->M.nnz, m->tm, P.nsub, P.subc, m->stream));
+        CU(launch_mli_plan(m->M.row_start, m->M.col, m->M.val, P, m->sm_count, m->stream));
     }
+    CU(cudaStreamSynchronize(m->stream));
+    dfree(m->M.col);
+    dfree(m->M.val);
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
     m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
     TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
     TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)std::max(m->grid, 2 * dot_grid(m->M.nor, m->sm_count)) + 64));
     TRY(ensure_cap(&m->fix_partials, &m->fix_cap, (size_t)m->fix_grid + 64));
-    dfree(m->tiles32);
-    m->num_tiles32 = 0;
     CU(cudaStreamSynchronize(m->stream));
     m->loaded = true;
     return PWMGPU_OK;
@@ -236,9 +245,9 @@ int check_sizes(long long nor, long long noc, long long nnz) {
 
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->num_tiles == 0) return PWMGPU_OK;
-    CU(launch_merge_spmv(m->cfg, kModeSpmv, m->M, m->M.val, m->tiles, m->subflag, m->num_tiles, m->grid, dx, dy,
-                         m->carries, nullptr, nullptr, m->status, m->stream));
-    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->tiles, m->num_tiles, dy, m->carries, nullptr, nullptr, 0, nullptr,
+    CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, nullptr,
+                         m->status, m->stream));
+    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, nullptr, 0, nullptr,
                               m->fix_grid, nullptr, nullptr, m->stream));
     return PWMGPU_OK;
 }
@@ -246,9 +255,9 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
 // One power-method step on device vectors: out = 2^e(nsq_in) * A in, and
 // nsq_out = ||out||^2 (deterministic).
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
-    CU(launch_merge_spmv(m->cfg, kModePower, m->M, m->M.val, m->tiles, m->subflag, m->num_tiles, m->grid, in, out,
-                         m->carries, nsq_in, m->partials, m->status, m->stream));
-    CU(launch_merge_fixup_f64(kModePower, m->M, m->tiles, m->num_tiles, out, m->carries, nsq_in, m->partials,
+    CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
+                         m->partials, m->status, m->stream));
+    CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in, m->partials,
                               m->grid, m->fix_partials, m->fix_grid, m->counter, nsq_out, m->stream));
     return PWMGPU_OK;
 }
@@ -457,8 +466,22 @@ int pwmgpu_get_csr(pwmgpu_matrix* m, int32_t* row_start, int32_t* col_ind, doubl
     CU(cudaMemcpyAsync(row_start, m->M.row_start, sizeof(int32_t) * ((size_t)m->M.nor + 1), cudaMemcpyDeviceToHost,
                        m->stream));
     if (m->M.nnz > 0) {
-        CU(cudaMemcpyAsync(col_ind, m->M.col, sizeof(int32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
-        CU(cudaMemcpyAsync(vals, m->M.val, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+        // back from the lane-interleaved storage to CRS order
+        int32_t* dc = nullptr;
+        double* dv = nullptr;
+        TRY(dalloc(&dc, (size_t)m->M.nnz));
+        int rc = dalloc(&dv, (size_t)m->M.nnz);
+        cudaError_t e = cudaSuccess;
+        if (rc == PWMGPU_OK) e = launch_mli_unpermute(m->P, dc, dv, m->sm_count, m->stream);
+        if (rc == PWMGPU_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(col_ind, dc, sizeof(int32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream);
+        if (rc == PWMGPU_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(vals, dv, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        dfree(dc);
+        dfree(dv);
+        if (rc != PWMGPU_OK) return rc;
+        if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "get_csr: %s", cudaGetErrorString(e));
     }
     CU(cudaStreamSynchronize(m->stream));
     return PWMGPU_OK;
