@@ -127,6 +127,25 @@ int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int pr
  * computed on the device by the kernel that partitions the merge path:
  * coords[2*t], coords[2*t+1] = (row, nonzero) for t = 0..parts. */
 int pwmgpu_merge_partition(pwmgpu_matrix* m, int32_t parts, int32_t* coords);
+/* y = A x for a CRS matrix whose arrays are already on the device and owned
+ * by the caller (row_start[nor+1], col_ind[nnz], vals[nnz], x[noc], y[nor]),
+ * without allocating anything.  No counterpart in the reference: it is for
+ * callers that cannot allocate device memory at call time -- a host runtime
+ * whose allocator owns all device memory, a serving loop that must not hit
+ * cudaMalloc / cudaFree (both may synchronise the device), a plug-in that is
+ * handed device pointers only.  Its scratch (merge-path sub-tile coordinates
+ * and carries) lives in one fixed 8 MiB array in device memory that every GPU
+ * loading the library keeps until the process exits; this limits a call to
+ * nor + nnz <= 134,217,472 (larger sizes return PWMGPU_ERR_INVALID).
+ * Asynchronous on `stream` (a cudaStream_t, NULL for the legacy stream).
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  Every call shares the one
+ * array, so calls that overlap on the GPU (other streams, other host threads)
+ * race: order them on one stream. */
+int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
+                                 const int32_t* col_ind, const double* vals, const double* x, double* y,
+                                 void* stream);
+
 /* Tile size (merge items per tile) and tile count used by the SpMV kernel. */
 int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid);
 

@@ -56,6 +56,7 @@ SIGNATURES = {
     "pwmgpu_solve": (C.c_int, [vp, vp, i32, C.c_double, C.c_int, C.POINTER(SolveInfo)]),
     "pwmgpu_merge_partition": (C.c_int, [vp, i32, vp]),
     "pwmgpu_tile_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "pwmgpu_mv_csr_device_noalloc": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp]),
 }
 
 

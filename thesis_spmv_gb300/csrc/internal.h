@@ -85,6 +85,9 @@ cudaError_t launch_convert_f64_f32(const double* s, float* d, long long n, int s
 cudaError_t launch_convert_f32_f64(const float* s, double* d, long long n, int sm_count, cudaStream_t st);
 cudaError_t launch_convert_f64_bf16(const double* s, void* d, long long n, int sm_count, cudaStream_t st);
 
+// Record the calling thread's last error message (pwmgpu_last_error).
+void record_error(const char* msg);
+
 // Poisson row start closed form (shared with the host checker of the
 // device generator).
 long long poisson_row_start_host(long long row, long long m, long long n);

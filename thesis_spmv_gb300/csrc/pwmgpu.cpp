@@ -280,6 +280,8 @@ int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
 }  // namespace
 
 namespace pwmgpu {
+void record_error(const char* msg) { g_err = msg ? msg : ""; }
+
 long long poisson_row_start_host(long long row, long long m, long long n) {
     long long mn = m * n;
     long long below = row > m ? row - m : 0;
