@@ -106,12 +106,28 @@ int pwmgpu_power(pwmgpu_matrix* m, double* x, double* y, int32_t it);
 /* Same on device arrays; the kernel sequence is asynchronous. */
 int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
 
+/* How pwmgpu_power / pwmgpu_power_device run the iterations:
+ * AUTO (default) and FUSED use one persistent cooperative kernel for all
+ * iterations (SpMV, norm and rescale fused; two grid barriers per iteration;
+ * FUSED fails with PWMGPU_ERR_UNSUPPORTED where it cannot be co-resident);
+ * MULTI launches an SpMV kernel and a fix-up / reduction kernel per
+ * iteration.  Results are equal within the power method's tolerance. */
+#define PWMGPU_POWER_AUTO 0
+#define PWMGPU_POWER_FUSED 1
+#define PWMGPU_POWER_MULTI 2
+int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
+
 /* Power solve with an eigenvalue estimate, the eigen-residual and a stopping
  * test (not in the reference: the benchmark spec extension).  x (host, length nor)
  * holds the start vector on entry and the normalised eigenvector estimate on
  * return.  Iterates until ||A u - lambda u|| / |lambda| <= tol or max_it
- * iterations.  precision: PWMGPU_PREC_*.  lambda is the Rayleigh quotient
- * u^T A u of the returned u (||u|| = 1). */
+ * iterations (max_it >= 2; tol = 0 runs exactly max_it SpMVs).  precision:
+ * PWMGPU_PREC_*.  lambda is the Rayleigh quotient u^T A u of the returned u
+ * (||u|| = 1), the normalised iterate after iterations - 1 SpMVs (the last
+ * SpMV computes A u for lambda and the residual).  The residual test runs
+ * every chunk of iterations inside the persistent kernel (FP64 reductions);
+ * MIXED runs FP32 (BF16 values where exact) until the residual reaches 2e-6
+ * or stops falling, then FP64 to tol. */
 typedef struct {
     int32_t iterations;     /* total SpMVs performed */
     int32_t iterations_low; /* of which in the FP32/BF16 phase */

@@ -247,6 +247,29 @@ void orc_power(int kind, int32_t nor, int32_t nnz, const int32_t* row_start, con
     }
 }
 
+void orc_rayleigh(int32_t nor, const int32_t* row_start, const int32_t* col_ind, const double* data,
+                  const double* u, double* lambda, double* residual) {
+    /* Not in the reference (its powerIteration has no eigenvalue output):
+     * the harness's eigenvalue estimate lambda = u.(Au) / u.u with Au from
+     * CRS::mv (CRS.hpp:99-109) and sequential FP64 dot products, and the
+     * relative eigen-residual ||Au - lambda u|| / (|lambda| ||u||). */
+    double* au = (double*)malloc(sizeof(double) * (size_t)(nor > 0 ? nor : 1));
+    orc_crs_mv(nor, row_start, col_ind, data, u, au);
+    double num = 0., den = 0.;
+    for (int32_t i = 0; i < nor; ++i) {
+        num = num + u[i] * au[i];
+        den = den + u[i] * u[i];
+    }
+    double lam = num / den, rr = 0.;
+    for (int32_t i = 0; i < nor; ++i) {
+        double d = au[i] - lam * u[i];
+        rr = rr + d * d;
+    }
+    free(au);
+    *lambda = lam;
+    *residual = sqrt(rr) / (fabs(lam) * sqrt(den));
+}
+
 /* ------------------------------------------------------------------ */
 /* CSB                                                                  */
 /* ------------------------------------------------------------------ */

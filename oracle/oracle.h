@@ -67,6 +67,11 @@ void orc_power(int kind, int32_t nor, int32_t nnz, const int32_t* row_start, con
 
 /* ---- CSB (SOA_Implementations/CSB.hpp) ---- */
 /* :96-113 setBlockSizeParam for T=double. */
+/* Eigenvalue estimate (Rayleigh quotient) and relative eigen-residual of u
+ * (harness arithmetic; the reference has none). */
+void orc_rayleigh(int32_t nor, const int32_t* row_start, const int32_t* col_ind, const double* data,
+                  const double* u, double* lambda, double* residual);
+
 void orc_csb_params(int32_t nor, int32_t noc, int32_t* beta, int32_t* block_bits);
 /* :464-567 loadFromTriplets.  ind[nnz], data[nnz], blk_ptr[H*V+1].
  * The triplet is sorted in place (row, then column).  Returns the balanced

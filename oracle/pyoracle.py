@@ -39,6 +39,7 @@ def lib():
         L.orc_norm2.argtypes = [F64P, C.c_int64]
         L.orc_normalize.argtypes = [F64P, C.c_int64]
         L.orc_power.argtypes = [C.c_int, C.c_int32, C.c_int32, I32P, I32P, F64P, F64P, F64P, C.c_int32, C.c_int]
+        L.orc_rayleigh.argtypes = [C.c_int32, I32P, I32P, F64P, F64P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_csb_params.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.orc_csb_build.restype = C.c_int
         L.orc_csb_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, I32P, I32P, F64P, U32P, F64P, I32P]
@@ -156,6 +157,15 @@ def power(A, x, it, kind=0, threads=1):
 def power_result(A, x, it, kind=0, threads=1):
     xo, yo = power(A, x, it, kind, threads)
     return xo if it % 2 == 0 else yo
+
+
+def rayleigh(A, u):
+    """(lambda, relative eigen-residual) of u: lambda = u.(Au)/u.u with Au
+    from CRS::mv, residual = ||Au - lambda u|| / (|lambda| ||u||)."""
+    u = np.ascontiguousarray(u, np.float64)
+    lam, res = C.c_double(), C.c_double()
+    lib().orc_rayleigh(A.nor, A.row_start, _nz(A.col_ind, np.int32), _nz(A.data), u, C.byref(lam), C.byref(res))
+    return lam.value, res.value
 
 
 def csb_params(nor, noc):

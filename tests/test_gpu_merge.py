@@ -171,12 +171,15 @@ def test_spmv_device_pointers_and_stream(pwm):
     assert np.all(np.abs(dy.cpu().numpy() - ref) <= O.row_error_bound(A, x))
 
 
+@pytest.mark.parametrize("mode", ["fused", "multi"])
 @pytest.mark.parametrize("it", [1, 2, 3, 10, 55])
-def test_power_iteration_equal_counts(pwm, it):
-    """x / y placement and values of powerIteration (CRS.hpp:118-130)."""
+def test_power_iteration_equal_counts(pwm, it, mode):
+    """x / y placement and values of powerIteration (CRS.hpp:118-130), with
+    the persistent kernel (fused) and with two kernels per iteration."""
     A = _random_csr(5000, 6, 21)
     A.data = np.abs(A.data) + 0.01  # positive: a dominant Perron eigenvalue
     M = _gpu_matrix(pwm, A)
+    M.set_power_mode(pwm.POWER_FUSED if mode == "fused" else pwm.POWER_MULTI)
     x0 = np.random.default_rng(4).random(A.nor)
     xg, yg = x0.copy(), np.zeros(A.nor)
     M.powerIteration(xg, yg, it)

@@ -52,6 +52,16 @@ MergeGeom merge_geometry(int cfg);
 int merge_grid(int cfg, int nsub, int sm_count);
 int fixup_grid(int num_tiles, int sm_count);
 int dot_grid(long long n, int sm_count);
+// Persistent power-method kernel (cooperative launch): grid size for a
+// matrix with nsub sub-tiles, 0 if the kernel cannot be made co-resident.
+int power_persistent_grid(int cfg, int nsub, int sm_count);
+// Iterations k0 .. k0+nk-1 on X/Y (ping-pong; v_k in X for even k), nsq[k]
+// = ||v_k||^2 (nsq[k0] read when k0 > 0), result (5 doubles, or null):
+// {lambda, residual^2, ||v_k||^2, v_k.v_{k+1}, e_k} of the last iteration.
+// partials: 2 doubles per CTA; barrier: 2 words (zeroed here).
+cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
+                                    void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
+                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st);
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
                                    int2* out, cudaStream_t st);
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
@@ -84,6 +94,7 @@ cudaError_t launch_resid_f32(const float* a, double sa, const float* b, double s
 cudaError_t launch_convert_f64_f32(const double* s, float* d, long long n, int sm_count, cudaStream_t st);
 cudaError_t launch_convert_f32_f64(const float* s, double* d, long long n, int sm_count, cudaStream_t st);
 cudaError_t launch_convert_f64_bf16(const double* s, void* d, long long n, int sm_count, cudaStream_t st);
+cudaError_t launch_bf16_exact(const double* v, long long n, int* flag, int sm_count, cudaStream_t st);
 
 // Record the calling thread's last error message (pwmgpu_last_error).
 void record_error(const char* msg);

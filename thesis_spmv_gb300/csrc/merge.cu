@@ -138,6 +138,72 @@ struct MergeArgs {
 
 constexpr int kMliStages = 2;
 
+// One SpMV pass of this warp: its sub-tiles s = global warp, + total warps,
+// double-buffered through its shared-memory stages.  `ticket` counts this
+// warp's stage uses so far, so mbarrier phases carry across passes of a
+// persistent kernel.  Returns false (warp-uniformly) after a timeout, once
+// this warp's copies in flight have landed or a short bound ran out.
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH>
+__device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
+                                          XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
+                                          AT* cval, AT* hval, uint32_t& ticket, int e, double& sumsq,
+                                          const XT* __restrict__ xdot, double* dot, uint64_t pol) {
+    using S = WarpStage<VT, IPT>;
+    constexpr int NS = kMliStages;
+    constexpr int W = NT / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * W + w, tw = gridDim.x * W;
+    const int n = gw < a.nsub ? (a.nsub - 1 - gw) / tw + 1 : 0;  // this warp's sub-tiles
+    int4 pref = make_int4(0, 0, 0, 0);
+    if (lane == 0) {
+        for (int k = 0; k < NS && k < n; ++k) {
+            const uint32_t u = ticket + k;
+            const int s = gw + k * tw;
+            issue_subtile<VT, IPT>(stages + (u % NS) * S::BYTES, &bars[u % NS], s, __ldg(a.rec + 2LL * s + 1),
+                                   a.rec, a.masks, a.colp, a.valp, pol);
+        }
+        if (n > NS) pref = __ldg(a.rec + 2LL * (gw + NS * tw) + 1);
+    }
+    __syncwarp();
+    int i = 0;
+    for (; i < n; ++i) {
+        const uint32_t u = ticket + i;
+        const int k = u % NS;
+        const int s = gw + i * tw;
+        unsigned char* st = stages + k * S::BYTES;
+        const bool ok = mbar_wait_bounded(&bars[k], (u / NS) & 1u, a.status);
+        if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
+        AT xv[IPT];
+        gather_subtile<VT, XT, AT, IPT, XCOH>(st, x, xv);
+        if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
+            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, sumsq, crow,
+                                                        cval, hval, xdot, dot);
+        else
+            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, sumsq,
+                                                         crow, cval, hval, xdot, dot);
+        // every lane is done with this stage (finish_subtile ends with a warp
+        // barrier): refill it with the warp's sub-tile i + NS
+        if (lane == 0 && i + NS < n) {
+            fence_proxy_async();
+            issue_subtile<VT, IPT>(st, &bars[k], s + NS * tw, pref, a.rec, a.masks, a.colp, a.valp, pol);
+            pref = (i + NS + 1 < n) ? __ldg(a.rec + 2LL * (s + (NS + 1) * tw) + 1) : make_int4(0, 0, 0, 0);
+        }
+    }
+    if (i < n) {
+        // Leaving early after a timeout: let this warp's copies in flight land
+        // (short bounded waits) before the CTA's shared memory goes away.
+        if (lane == 0)
+            for (int t = i; t < n && t < i + NS; ++t) {
+                const uint32_t u = ticket + t;
+                mbar_wait_bounded(&bars[u % NS], (u / NS) & 1u, a.status, kWaitCycles / 8, false);
+            }
+        __syncwarp();
+        return false;
+    }
+    ticket += (uint32_t)n;
+    return true;
+}
+
 template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT>
 __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     using S = WarpStage<VT, IPT>;
@@ -150,55 +216,17 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     __shared__ AT hval[NT];
     __shared__ double red[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
-    const int gw = blockIdx.x * W + w, tw = gridDim.x * W;
-    const int n = gw < a.nsub ? (a.nsub - 1 - gw) / tw + 1 : 0;  // this warp's sub-tiles
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
-    const uint64_t pol = policy_evict_first();
-
-    int4 pref = make_int4(0, 0, 0, 0);
     if (lane == 0) {
         for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
         fence_mbar_init();
-        for (int k = 0; k < NS && k < n; ++k) {
-            const int s = gw + k * tw;
-            issue_subtile<VT, IPT>(stages + k * S::BYTES, &bars[w][k], s, __ldg(a.rec + 2LL * s + 1), a.rec,
-                                   a.masks, a.colp, a.valp, pol);
-        }
-        if (n > NS) pref = __ldg(a.rec + 2LL * (gw + NS * tw) + 1);
     }
     __syncwarp();
-
-    double sumsq = 0.0;
-    int i = 0;
-    for (; i < n; ++i) {
-        const int s = gw + i * tw;
-        const int k = i % NS;
-        unsigned char* st = stages + k * S::BYTES;
-        const bool ok = mbar_wait_bounded(&bars[w][k], (uint32_t)(i / NS) & 1u, a.status);
-        if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
-        AT xv[IPT];
-        gather_subtile<VT, XT, AT, IPT>(st, a.x, xv);
-        if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
-            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, a.y, a.carries, a.nor, e, sumsq,
-                                                        crow + 32 * w, cval + 32 * w, hval + 32 * w);
-        else
-            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, a.y, a.carries, a.nor, e, sumsq,
-                                                         crow + 32 * w, cval + 32 * w, hval + 32 * w);
-        // every lane is done with this stage (finish_subtile ends with a warp
-        // barrier): refill it with sub-tile i + NS
-        if (lane == 0 && i + NS < n) {
-            fence_proxy_async();
-            issue_subtile<VT, IPT>(st, &bars[w][k], s + NS * tw, pref, a.rec, a.masks, a.colp, a.valp, pol);
-            pref = (i + NS + 1 < n) ? __ldg(a.rec + 2LL * (s + (NS + 1) * tw) + 1) : make_int4(0, 0, 0, 0);
-        }
-    }
-    if (lane == 0 && i < n) {
-        // Leaving early after a timeout: let this warp's copies in flight land
-        // (short bounded waits) before the CTA's shared memory goes away.
-        for (int t = i; t < n && t < i + NS; ++t)
-            mbar_wait_bounded(&bars[w][t % NS], (uint32_t)(t / NS) & 1u, a.status, kWaitCycles / 8, false);
-    }
+    uint32_t ticket = 0;
+    double sumsq = 0.0, dot = 0.0;
+    warp_pass<MODE, VT, XT, AT, NT, IPT, false>(a, a.x, a.y, smem_raw + (size_t)w * NS * S::BYTES, bars[w], crow + 32 * w,
+                                         cval + 32 * w, hval + 32 * w, ticket, e, sumsq, nullptr, &dot,
+                                         policy_evict_first());
     if (MODE == MODE_POWER) {
         double t = block_sum<NT>(sumsq, red);
         if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
@@ -206,14 +234,40 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
 }
 
 // ---------------------------------------------------------------------------
-// Fix-up: add each tile's carry to the row that the tile left unfinished.
-// One thread per tile; the first tile of a run of tiles ending in the same
-// row adds the run in tile order (deterministic).  The run's row r is
-// completed (and its partial written) by the first tile after the run; the
-// carry is real only if that tile started inside row r.
-// MODE_POWER also finishes ||y||^2: the sum of squares of the rows fixed
-// here, then one deterministic reduction over all partials by the last CTA.
+// Fix-up: add each sub-tile's carry to the row the sub-tile left unfinished.
+// One thread per sub-tile; the first sub-tile of a run of sub-tiles ending in
+// the same row adds the run in order (deterministic).  The run's row r is
+// completed (and its partial written) by the first sub-tile after the run; the
+// carry is real only if that sub-tile started inside row r.  MODE_POWER also
+// sums the squares (and, with xdot, x[r]*y[r]) of the rows fixed here.
 // ---------------------------------------------------------------------------
+template <int MODE, typename XT, typename AT>
+__device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start, const int2* __restrict__ tiles,
+                                           int nor, int num_tiles, XT* __restrict__ y, const AT* __restrict__ carries,
+                                           int e, double& sumsq, const XT* __restrict__ xdot, double* dot, int t0,
+                                           int stride) {
+    for (int t = t0; t < num_tiles; t += stride) {
+        const int r = tiles[t + 1].x;
+        if (r >= nor) continue;
+        if (t > 0 && tiles[t].x == r) continue;  // not the first sub-tile of the run
+        // carries and y[r] were written by other CTAs: read them through L2
+        AT sum = __ldcg(carries + t);
+        int n = t + 1;
+        while (n < num_tiles && tiles[n + 1].x == r) sum += __ldcg(carries + n++);
+        // sub-tile n starts at (r, tiles[n].y) and completes row r
+        if (tiles[n].y > row_start[r]) {
+            AT v;
+            if (MODE == MODE_POWER) v = (AT)__ldcg(y + r) + scale_pow2(sum, e);
+            else v = (AT)__ldcg(y + r) + sum;
+            y[r] = (XT)v;
+            if (MODE == MODE_POWER) {
+                sumsq = fma((double)v, (double)v, sumsq);
+                if (xdot) *dot = fma((double)xdot[r], (double)v, *dot);
+            }
+        }
+    }
+}
+
 template <typename XT, typename AT>
 struct FixArgs {
     const int32_t* row_start;
@@ -229,28 +283,16 @@ struct FixArgs {
     double* nsq_out;
 };
 
+// Stand-alone fix-up kernel; MODE_POWER finishes ||y||^2 with one
+// deterministic reduction over all partials by the last CTA.
 template <int MODE, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
     __shared__ double red[32];
     __shared__ bool am_last;
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
-    double sumsq = 0.0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < a.num_tiles; t += gridDim.x * blockDim.x) {
-        const int r = a.tiles[t + 1].x;
-        if (r >= a.nor) continue;
-        if (t > 0 && a.tiles[t].x == r) continue;  // not the first tile of the run
-        AT sum = a.carries[t];
-        int n = t + 1;
-        while (n < a.num_tiles && a.tiles[n + 1].x == r) sum += a.carries[n++];
-        // tile n starts at (r, tiles[n].y) and completes row r
-        if (a.tiles[n].y > a.row_start[r]) {
-            AT v;
-            if (MODE == MODE_POWER) v = (AT)a.y[r] + scale_pow2(sum, e);
-            else v = (AT)a.y[r] + sum;
-            a.y[r] = (XT)v;
-            if (MODE == MODE_POWER) sumsq = fma((double)v, (double)v, sumsq);
-        }
-    }
+    double sumsq = 0.0, dot = 0.0;
+    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, sumsq, nullptr, &dot,
+                             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
     if (MODE != MODE_POWER) return;
     double t = block_sum<256>(sumsq, red);
     if (threadIdx.x == 0) {
@@ -271,6 +313,172 @@ __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
         if (l == 0) {
             *a.nsq_out = s;
             *a.counter = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grid-wide barrier for a cooperative launch, with a bounded wait: after
+// kWaitCycles (or once another CTA has recorded a failure) it records
+// PWMGPU_ERR_TIMEOUT and returns false in every thread of the CTA.
+// bar[0] counts arrivals, bar[1] is the generation; both start at zero.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = bar + 1;
+        const unsigned int g = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
+        int ok = 1;
+        if (arrived == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            unsigned int spins = 0;
+            while (*vgen == g) {
+                if ((++spins & 1023u) == 0u) {
+                    if (*(volatile int*)status != PWMGPU_OK) { ok = 0; break; }
+                    if (clock64() - t0 > kWaitCycles) {
+                        atomicCAS(status, PWMGPU_OK, PWMGPU_ERR_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        __threadfence();
+        ok_s = ok && (*(volatile int*)status == PWMGPU_OK);
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// ---------------------------------------------------------------------------
+// K5: the power-method step fused into one persistent kernel (cooperative
+// launch).  Iteration k (k0 <= k < k0 + nk):
+//   v_{k+1} = 2^{e_k} A v_k         (SpMV; e_k from ||v_k||^2, exact rescale)
+//   ||v_{k+1}||^2                    (epilogue + fix-up, deterministic)
+//   v_k . v_{k+1} on the last iteration when `result` is set, then the
+//   Rayleigh quotient lambda_k = 2^{-e_k} v_k.v_{k+1} / ||v_k||^2 and the
+//   eigen-residual ||2^{-e_k} v_{k+1} - lambda_k v_k||^2 (one more pass)
+// Vectors ping-pong: iteration k reads X when k is even, Y when odd.  Two grid
+// barriers per iteration (SpMV | fix-up | reduction).  The normalisation of
+// the reference (y /= ||y||, Util/VectorUtill.hpp:34-41) is carried by the
+// exponent and applied once at the end (k_power_finalize).  All reductions
+// are FP64 and in a fixed order, whatever the vector type.
+// ---------------------------------------------------------------------------
+template <typename VT, typename XT, typename AT>
+struct PowerArgs {
+    MergeArgs<VT, XT, AT> m;
+    const int2* subc;
+    XT* X;
+    XT* Y;
+    int k0, nk;
+    double* nsq;       // nsq[k] = ||v_k||^2; nsq[k0] read when k0 > 0; nsq[k0+1 .. k0+nk] written
+    double* result;    // null, or (k = k0+nk-1 >= 1): {lambda_k, residual^2, ||v_k||^2, v_k.v_{k+1}, e_k}
+    double* partials;  // 2 per CTA
+    unsigned int* barrier;
+};
+
+// Sum two per-CTA partials over the grid in a fixed order (every CTA gets the
+// same totals); call after a grid barrier.
+template <int NT>
+__device__ __forceinline__ void grid_total2(const double* partials, double* total) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int i = lane; i < (int)gridDim.x; i += 32) {
+            s0 += __ldcg(partials + 2 * i);
+            s1 += __ldcg(partials + 2 * i + 1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_down_sync(0xffffffffu, s0, o);
+            s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        }
+        if (lane == 0) {
+            total[0] = s0;
+            total[1] = s1;
+        }
+    }
+    __syncthreads();
+}
+
+template <typename VT, typename XT, typename AT, int NT, int IPT>
+__global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p) {
+    using S = WarpStage<VT, IPT>;
+    constexpr int W = NT / 32;
+    constexpr int NS = kMliStages;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t bars[W][NS];
+    __shared__ int crow[NT];
+    __shared__ AT cval[NT];
+    __shared__ AT hval[NT];
+    __shared__ double red[32];
+    __shared__ double total[2];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const MergeArgs<VT, XT, AT>& a = p.m;
+    if (lane == 0) {
+        for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const uint64_t pol = policy_evict_first();
+    uint32_t ticket = 0;
+    double nsq_cur = p.k0 > 0 ? p.nsq[p.k0] : 0.0;
+    double nsq_last = 0.0;
+    int e = 0;
+    for (int k = p.k0; k < p.k0 + p.nk; ++k) {
+        const XT* in = (k & 1) ? p.Y : p.X;
+        XT* out = (k & 1) ? p.X : p.Y;
+        e = k > 0 ? pow2_exponent_from_nsq(nsq_cur) : 0;
+        nsq_last = nsq_cur;
+        const bool want_dot = p.result && k == p.k0 + p.nk - 1;
+        double ss = 0.0, dd = 0.0;
+        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true>(a, in, out, smem_raw + (size_t)w * NS * S::BYTES, bars[w],
+                                                   crow + 32 * w, cval + 32 * w, hval + 32 * w, ticket, e, ss,
+                                                   want_dot ? in : nullptr, &dd, pol);
+        if (!grid_sync(p.barrier, a.status)) return;
+        fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, ss,
+                                       want_dot ? in : nullptr, &dd, blockIdx.x * NT + threadIdx.x, gridDim.x * NT);
+        const double t_ss = block_sum<NT>(ss, red);
+        const double t_dd = block_sum<NT>(dd, red);
+        if (threadIdx.x == 0) {
+            p.partials[2 * blockIdx.x] = t_ss;
+            p.partials[2 * blockIdx.x + 1] = t_dd;
+        }
+        if (!grid_sync(p.barrier, a.status)) return;
+        grid_total2<NT>(p.partials, total);  // every CTA, same order
+        nsq_cur = total[0];
+        const double dot = total[1];
+        if (blockIdx.x == 0 && threadIdx.x == 0) p.nsq[k + 1] = nsq_cur;
+        __syncthreads();  // total[] is rewritten below
+        if (want_dot) {
+            // lambda_k and the eigen-residual of u = v_k / ||v_k||
+            const double lam = scale_pow2(dot, -e) / nsq_last;
+            double rr = 0.0;
+            for (int i = blockIdx.x * NT + threadIdx.x; i < a.nor; i += gridDim.x * NT) {
+                const double d = scale_pow2((double)__ldcg(out + i), -e) - lam * (double)__ldcg(in + i);
+                rr = fma(d, d, rr);
+            }
+            const double t_rr = block_sum<NT>(rr, red);
+            if (!grid_sync(p.barrier, a.status)) return;  // everyone has read partials
+            if (threadIdx.x == 0) {
+                p.partials[2 * blockIdx.x] = t_rr;
+                p.partials[2 * blockIdx.x + 1] = 0.0;
+            }
+            if (!grid_sync(p.barrier, a.status)) return;
+            grid_total2<NT>(p.partials, total);
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                p.result[0] = lam;
+                p.result[1] = total[0];
+                p.result[2] = nsq_last;
+                p.result[3] = dot;
+                p.result[4] = (double)e;
+            }
         }
     }
 }
@@ -406,6 +614,17 @@ __global__ void k_convert<double, __nv_bfloat16>(const double* __restrict__ s, _
         d[i] = __double2bfloat16(s[i]);
 }
 
+// flag[0] |= 1 if some value is not exactly representable in BF16 (the mixed
+// solve then streams FP32 values instead)
+__global__ void k_bf16_exact(const double* __restrict__ v, long long n, int* flag) {
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double d = v[i];
+        bad |= (double)__bfloat162float(__double2bfloat16(d)) != d;
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 // ===========================================================================
 // Host launchers
 // ===========================================================================
@@ -429,6 +648,35 @@ struct MergeKernels {
             occ = o > 0 ? o : 1;
         }
         return MergeGeom{32 * IPT, NT / 32, SMEM, occ, NT};
+    }
+
+    // resident CTAs per SM of the persistent power kernel (0: cannot launch)
+    static int power_occ() {
+        static int occ = -1;
+        if (occ < 0) {
+            auto k = k_power_persistent<VT, XT, AT, NT, IPT>;
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+            int o = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM) != cudaSuccess) o = 0;
+            occ = o;
+        }
+        return occ;
+    }
+
+    static cudaError_t power(const DevMatrix& M, const void* valp, const MliPlan& P, int grid, void* X, void* Y,
+                             void* carries, int k0, int nk, double* nsq, double* result, double* partials,
+                             unsigned int* barrier, int* status, cudaStream_t st) {
+        power_occ();
+        PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
+                                 nullptr, (AT*)carries, nullptr, nullptr, status},
+                                P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier};
+        cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned int), st);
+        if (e != cudaSuccess) return e;
+        void* args[] = {&p};
+        // cooperative launch: fails instead of running if the grid cannot be
+        // co-resident, so the grid barriers cannot wait on unscheduled CTAs
+        return cudaLaunchCooperativeKernel((const void*)k_power_persistent<VT, XT, AT, NT, IPT>, dim3(grid),
+                                           dim3(NT), args, SMEM, st);
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
@@ -466,6 +714,36 @@ int merge_grid(int cfg, int nsub, int sm_count) {
     long long grid = (long long)g.occ * sm_count;
     if (grid > ctas) grid = ctas;
     return grid > 0 ? (int)grid : 1;
+}
+
+int power_persistent_grid(int cfg, int nsub, int sm_count) {
+    int occ;
+    switch (cfg) {
+        case kCfgF32: occ = CfgF32::power_occ(); break;
+        case kCfgBF16: occ = CfgBF16::power_occ(); break;
+        default: occ = CfgF64::power_occ(); break;
+    }
+    if (occ <= 0) return 0;
+    const MergeGeom g = merge_geometry(cfg);
+    long long ctas = (nsub + g.w - 1) / g.w;
+    long long grid = (long long)occ * sm_count;
+    if (grid > ctas) grid = ctas;
+    return grid > 0 ? (int)grid : 1;
+}
+
+cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
+                                    void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
+                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st) {
+    if (nk <= 0) return cudaSuccess;
+    switch (cfg) {
+        case kCfgF32:
+            return CfgF32::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st);
+        case kCfgBF16:
+            return CfgBF16::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status,
+                                  st);
+        default:
+            return CfgF64::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st);
+    }
 }
 
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
@@ -612,6 +890,14 @@ cudaError_t launch_convert_f32_f64(const float* s, double* d, long long n, int s
 }
 cudaError_t launch_convert_f64_bf16(const double* s, void* d, long long n, int sm_count, cudaStream_t st) {
     k_convert<double, __nv_bfloat16><<<sm_count * 8, 256, 0, st>>>(s, (__nv_bfloat16*)d, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bf16_exact(const double* v, long long n, int* flag, int sm_count, cudaStream_t st) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > sm_count * 8) blocks = sm_count * 8;
+    if (blocks < 1) blocks = 1;
+    k_bf16_exact<<<(int)blocks, 256, 0, st>>>(v, n, flag);
     return cudaGetLastError();
 }
 

@@ -156,7 +156,9 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 
 // First half of a sub-tile: the lane's gathers x[col], all issued together
 // (read from the staged columns).
-template <typename VT, typename XT, typename AT, int IPT>
+// XCOH: x was written earlier in the same launch (persistent power kernel), so
+// it is read through L2 (ld.global.cg) instead of the read-only path.
+template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false>
 __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT]) {
     using S = WarpStage<VT, IPT>;
     const int lane = threadIdx.x & 31;
@@ -166,7 +168,10 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
     int32_t cv[IPT];
     load_lane<int32_t, IPT>(reinterpret_cast<const int32_t*>(st + S::REC_B + S::MASK_B), qm, cnt, lane, cv);
 #pragma unroll
-    for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldg(x + cv[j]) : AT(0);
+    for (int j = 0; j < IPT; ++j) {
+        if (XCOH) xv[j] = (j < cnt) ? (AT)__ldcg(x + cv[j]) : AT(0);
+        else xv[j] = (j < cnt) ? (AT)__ldg(x + cv[j]) : AT(0);
+    }
 }
 
 // Second half: FMAs over the staged values, row completion, carries.
@@ -180,11 +185,14 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 //                 earlier lane of this sub-tile;
 //               * k_merge_fixup, if the row began in an earlier sub-tile.
 //   crow, cval, hval   this warp's 32-entry shared scratch
+//   xdot, dot when xdot is set (MODE_POWER), dot also sums x[r]*y[r] over the
+//             same rows: the Rayleigh quotient's numerator for a square A
 template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT>
 __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, const AT (&xv)[IPT],
                                                const int32_t* __restrict__ row_start, XT* __restrict__ y,
                                                AT* __restrict__ carries, int nor, int e, double& sumsq, int* crow,
-                                               AT* cval, AT* hval) {
+                                               AT* cval, AT* hval, const XT* __restrict__ xdot = nullptr,
+                                               double* dot = nullptr) {
     using S = WarpStage<VT, IPT>;
     const int lane = threadIdx.x & 31;
     const int4 r0 = reinterpret_cast<const int4*>(st)[0];
@@ -237,7 +245,10 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
                     hval[lane] = v;
                 } else {
                     y[a] = (XT)v;
-                    if (MODE == MODE_POWER && count) sumsq = fma((double)v, (double)v, sumsq);
+                    if (MODE == MODE_POWER && count) {
+                        sumsq = fma((double)v, (double)v, sumsq);
+                        if (xdot) *dot = fma((double)__ldcg(xdot + a), (double)v, *dot);
+                    }
                 }
                 to_head = false;
                 count = true;
@@ -273,7 +284,10 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
                 y[a] = (XT)v;
                 // final now if the row began in this sub-tile; otherwise
                 // k_merge_fixup adds the earlier sub-tiles' carries and counts it
-                if (MODE == MODE_POWER && rs_a >= kw0) sumsq = fma((double)v, (double)v, sumsq);
+                if (MODE == MODE_POWER && rs_a >= kw0) {
+                    sumsq = fma((double)v, (double)v, sumsq);
+                    if (xdot) *dot = fma((double)__ldcg(xdot + a), (double)v, *dot);
+                }
             }
         } else if (a < nor) {
             carries[s] = sum;  // a == rw1: the sub-tile's unfinished row

@@ -84,6 +84,9 @@ struct pwmgpu_matrix {
     // lane-interleaved arrays, and launch geometry
     int cfg = kCfgF64;
     int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
+    // persistent power kernel grids per configuration (0: not launchable)
+    int pgrid = 0, pgrid32 = 0, pgridbf = 0;
+    int power_mode = PWMGPU_POWER_AUTO;
     MliPlan P;
     // lane-interleaved FP32 / BF16 copies of the values (lazy)
     float* val32 = nullptr;
@@ -100,8 +103,10 @@ struct pwmgpu_matrix {
     unsigned int* counter = nullptr;
     double* nsq = nullptr;
     size_t nsq_cap = 0;
-    double* small = nullptr;  // 8 doubles of reduction outputs
+    double* small = nullptr;  // 16 doubles of reduction outputs
     int* status = nullptr;
+    unsigned int* barrier = nullptr;  // grid barrier words of the persistent kernel
+    double* hres = nullptr;           // pinned host copy of a solve chunk's results
 
     // host-facing vector buffers
     double* dx = nullptr;
@@ -138,6 +143,9 @@ struct pwmgpu_matrix {
         dfree(nsq);
         dfree(small);
         dfree(status);
+        dfree(barrier);
+        if (hres) cudaFreeHost(hres);
+        hres = nullptr;
         dfree(dx);
         dfree(dy);
         dfree(fx);
@@ -198,8 +206,13 @@ int build_plan(pwmgpu_matrix* m) {
     dfree(m->M.val);
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
     m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count);
+    const int pmax = std::max(m->pgrid, std::max(m->pgrid32, m->pgridbf));
     TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
-    TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)std::max(m->grid, 2 * dot_grid(m->M.nor, m->sm_count)) + 64));
+    TRY(ensure_cap(&m->partials, &m->partials_cap,
+                   (size_t)std::max(std::max(m->grid, 2 * pmax), 2 * dot_grid(m->M.nor, m->sm_count)) + 64));
     TRY(ensure_cap(&m->fix_partials, &m->fix_cap, (size_t)m->fix_grid + 64));
     CU(cudaStreamSynchronize(m->stream));
     m->loaded = true;
@@ -262,18 +275,200 @@ int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double
     return PWMGPU_OK;
 }
 
+bool use_fused(const pwmgpu_matrix* m, int pgrid) {
+    if (m->power_mode == PWMGPU_POWER_MULTI) return false;
+    return pgrid > 0;
+}
+
 int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
     if (it <= 0 || m->M.nor == 0) return PWMGPU_OK;
     TRY(ensure_nsq(m, (size_t)it + 1));
-    for (int k = 0; k < it; ++k) {
-        const double* in = (k % 2 == 0) ? dx : dy;
-        double* out = (k % 2 == 0) ? dy : dx;
-        TRY(power_step_f64(m, in, out, k ? m->nsq + k : nullptr, m->nsq + k + 1));
+    if (m->power_mode == PWMGPU_POWER_FUSED && m->pgrid == 0)
+        return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident on this device");
+    if (use_fused(m, m->pgrid)) {
+        // K5: all `it` iterations in one persistent launch
+        CU(launch_power_persistent(kCfgF64, m->M, m->P.valp, m->P, m->pgrid, dx, dy, m->carries, 0, it, m->nsq,
+                                   nullptr, m->partials, m->barrier, m->status, m->stream));
+    } else {
+        for (int k = 0; k < it; ++k) {
+            const double* in = (k % 2 == 0) ? dx : dy;
+            double* out = (k % 2 == 0) ? dy : dx;
+            TRY(power_step_f64(m, in, out, k ? m->nsq + k : nullptr, m->nsq + k + 1));
+        }
     }
     double* last = (it % 2 == 1) ? dy : dx;
     double* prev = (it % 2 == 1) ? dx : dy;
     CU(launch_power_finalize_f64(last, m->nsq + it, it >= 2 ? prev : nullptr, m->nsq + it - 1, m->M.nor,
                                  m->sm_count, m->stream));
+    return PWMGPU_OK;
+}
+
+// Lane-interleaved FP32 or (when every value is exactly a BF16 number, as the
+// Poisson 4 / -1 stencil is) BF16 copy of the values, made on first use.
+int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** valp, int* pgrid) {
+    const long long elems = mli_storage_elems(m->M.nnz, m->P.nsub);
+    if (allow_bf16) {
+        if (m->bf16_exact < 0) {
+            int* flag = reinterpret_cast<int*>(m->barrier + 2);
+            int h = 0;
+            CU(cudaMemsetAsync(flag, 0, sizeof(int), m->stream));
+            CU(launch_bf16_exact(m->P.valp, elems, flag, m->sm_count, m->stream));
+            CU(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+            CU(cudaStreamSynchronize(m->stream));
+            m->bf16_exact = h == 0 ? 1 : 0;
+        }
+        if (m->bf16_exact == 1) {
+            if (!m->valbf) {
+                CU(cudaMalloc(&m->valbf, 2 * (size_t)elems + 16));
+                CU(cudaMemsetAsync(m->valbf, 0, 2 * (size_t)elems + 16, m->stream));
+                CU(launch_mli_convert(m->P, kCfgBF16, m->valbf, m->sm_count, m->stream));
+            }
+            *cfg = kCfgBF16;
+            *valp = m->valbf;
+            *pgrid = m->pgridbf;
+            return PWMGPU_OK;
+        }
+    }
+    if (!m->val32) {
+        TRY(dalloc(&m->val32, (size_t)elems + 4));
+        CU(cudaMemsetAsync(m->val32, 0, sizeof(float) * ((size_t)elems + 4), m->stream));
+        CU(launch_mli_convert(m->P, kCfgF32, m->val32, m->sm_count, m->stream));
+    }
+    *cfg = kCfgF32;
+    *valp = m->val32;
+    *pgrid = m->pgrid32;
+    return PWMGPU_OK;
+}
+
+int ensure_fvectors(pwmgpu_matrix* m) {
+    size_t need = (size_t)std::max(m->M.nor, m->M.noc) + kPad;
+    if (m->fvec_cap >= need) return PWMGPU_OK;
+    dfree(m->fx);
+    dfree(m->fy);
+    m->fvec_cap = 0;
+    TRY(dalloc(&m->fx, need));
+    TRY(dalloc(&m->fy, need));
+    m->fvec_cap = need;
+    return PWMGPU_OK;
+}
+
+// One chunk of the persistent power kernel (iterations k0 .. k0+nk-1 of the
+// current phase, k0 + nk >= 2) with the Rayleigh quotient and eigen-residual
+// of its last iterate v_k, k = k0 + nk - 1.
+struct ChunkOut {
+    double lambda, rel;
+};
+int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X, void* Y, int k0, int nk,
+                ChunkOut* o) {
+    CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
+                               m->partials, m->barrier, m->status, m->stream));
+    CU(cudaMemcpyAsync(m->hres, m->small, 5 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+    TRY(check_status(m));
+    const double lam = m->hres[0], r2 = m->hres[1], nsq = m->hres[2];
+    if (!(nsq > 0.0) || !std::isfinite(nsq) || !std::isfinite(lam) || !std::isfinite(r2))
+        return fail(PWMGPU_ERR_NUMERIC, "power solve met a zero or non-finite iterate (||v||^2 = %g)", nsq);
+    o->lambda = lam;
+    o->rel = lam != 0.0 ? std::sqrt(r2 / nsq) / std::fabs(lam) : INFINITY;
+    return PWMGPU_OK;
+}
+
+// Length of the next chunk: the iterations the residual's observed rate
+// needs to reach `target`, within [8, 512].
+int next_chunk(double rel, double prev_rel, int nk, double target) {
+    if (std::isfinite(prev_rel) && rel < prev_rel && rel > 0.0 && target > 0.0) {
+        const double rate = std::log(rel / prev_rel) / nk;  // < 0
+        const double need = std::log(target / rel) / rate;
+        if (need <= 0.0) return 8;
+        return (int)std::min(512.0, std::max(8.0, std::ceil(need * 1.05) + 1.0));
+    }
+    return std::min(2 * nk, 512);
+}
+
+// Residual at which the mixed solve leaves the FP32 / BF16 phase: above the
+// FP32 rounding floor of the residual (about nnz_row * 2^-24).
+constexpr double kSwitchRel = 2e-6;
+
+int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info) {
+    const int N = m->M.nor;
+    TRY(ensure_vectors(m));
+    TRY(ensure_nsq(m, (size_t)max_it + 2));
+    CU(cudaMemcpyAsync(m->dx, x, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, m->stream));
+    int k = 0, low = 0;
+    bool conv = false;
+    ChunkOut o{0.0, INFINITY};
+    double* result = nullptr;  // device vector holding the final (unnormalised) iterate
+
+    // the mixed solve leaves at least 2 (at most 64) iterations for the FP64 phase
+    const int budget = precision == PWMGPU_PREC_F32 ? max_it : max_it - std::max(2, std::min(64, max_it / 4));
+    if (precision == PWMGPU_PREC_F32 || (precision == PWMGPU_PREC_MIXED && budget >= 2)) {
+        int cfg = kCfgF32, pg = 0;
+        const void* valp = nullptr;
+        TRY(ensure_low_values(m, precision == PWMGPU_PREC_MIXED, &cfg, &valp, &pg));
+        if (pg == 0) return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
+        TRY(ensure_fvectors(m));
+        CU(launch_convert_f64_f32(m->dx, m->fx, N, m->sm_count, m->stream));
+        int kl = 0, chunk = 16, nchunks = 0;
+        double prev = INFINITY;
+        const double target = precision == PWMGPU_PREC_F32 ? tol : std::max(tol, kSwitchRel);
+        while (true) {
+            int nk = std::min(chunk, budget - k);
+            if (kl + nk < 2) nk = 2 - kl;
+            TRY(solve_chunk(m, cfg, valp, pg, m->fx, m->fy, kl, nk, &o));
+            kl += nk;
+            k += nk;
+            low += nk;
+            ++nchunks;
+            if (o.rel <= target) {
+                conv = precision == PWMGPU_PREC_F32;
+                break;
+            }
+            if (k >= budget) break;
+            // FP32 has stopped converging: refine in FP64 from here
+            if (precision == PWMGPU_PREC_MIXED && nchunks >= 3 && o.rel >= 0.7 * prev) break;
+            chunk = next_chunk(o.rel, prev, nk, target);
+            prev = o.rel;
+        }
+        if (precision == PWMGPU_PREC_F32) {
+            // v_{kl-1} is the iterate whose Rayleigh quotient was measured
+            float* last = ((kl - 1) & 1) ? m->fy : m->fx;
+            CU(launch_convert_f32_f64(last, m->dx, N, m->sm_count, m->stream));
+            result = m->dx;
+        } else {
+            // the newest iterate v_kl starts the FP64 phase
+            float* newest = (kl & 1) ? m->fy : m->fx;
+            CU(launch_convert_f32_f64(newest, m->dx, N, m->sm_count, m->stream));
+        }
+    }
+    if (precision != PWMGPU_PREC_F32) {
+        if (m->pgrid == 0) return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
+        int kl = 0, chunk = precision == PWMGPU_PREC_MIXED ? 8 : 16;
+        double prev = INFINITY;
+        while (true) {
+            int nk = std::min(chunk, max_it - k);
+            if (kl + nk < 2) nk = 2 - kl;
+            TRY(solve_chunk(m, kCfgF64, m->P.valp, m->pgrid, m->dx, m->dy, kl, nk, &o));
+            kl += nk;
+            k += nk;
+            if (o.rel <= tol) {
+                conv = true;
+                break;
+            }
+            if (k >= max_it) break;
+            chunk = next_chunk(o.rel, prev, nk, tol);
+            prev = o.rel;
+        }
+        result = ((kl - 1) & 1) ? m->dy : m->dx;
+    }
+    // u = v / ||v|| (||v||^2 = result[2] of the last chunk, still on the device)
+    CU(launch_power_finalize_f64(result, m->small + 2, nullptr, nullptr, N, m->sm_count, m->stream));
+    CU(cudaMemcpyAsync(x, result, sizeof(double) * (size_t)N, cudaMemcpyDeviceToHost, m->stream));
+    TRY(check_status(m));
+    info->iterations = k;
+    info->iterations_low = low;
+    info->converged = conv ? 1 : 0;
+    info->precision = precision;
+    info->lambda = o.lambda;
+    info->residual = o.rel;
     return PWMGPU_OK;
 }
 
@@ -332,6 +527,9 @@ int pwmgpu_create(int format, int partitions, pwmgpu_matrix** out) {
         if ((rc = dalloc(&m->counter, 4)) != PWMGPU_OK) break;
         if ((rc = dalloc(&m->status, 4)) != PWMGPU_OK) break;
         if ((rc = dalloc(&m->small, 16)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&m->barrier, 4)) != PWMGPU_OK) break;
+        e = cudaMallocHost((void**)&m->hres, 16 * sizeof(double));
+        if (e != cudaSuccess) { m->hres = nullptr; rc = fail(PWMGPU_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)); break; }
         cudaMemsetAsync(m->counter, 0, 4 * sizeof(unsigned int), m->stream);
         cudaMemsetAsync(m->status, 0, 4 * sizeof(int), m->stream);
         e = cudaStreamSynchronize(m->stream);
@@ -560,15 +758,42 @@ int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* n
 }
 
 int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
-    (void)dx; (void)dy;
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
-    return fail(PWMGPU_ERR_UNSUPPORTED, "FP32 SpMV not built yet");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor > 0 && (!dx || !dy)) return fail(PWMGPU_ERR_INVALID, "null vector");
+    if (m->num_tiles == 0) return PWMGPU_OK;
+    int cfg = kCfgF32, pg = 0;
+    const void* valp = nullptr;
+    TRY(ensure_low_values(m, false, &cfg, &valp, &pg));
+    CU(launch_merge_spmv(kCfgF32, kModeSpmv, m->M, valp, m->P, merge_grid(kCfgF32, m->num_tiles, m->sm_count), dx,
+                         dy, m->carries, nullptr, nullptr, m->status, m->stream));
+    CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
+                              nullptr, nullptr, 0, nullptr, m->fix_grid, nullptr, nullptr, m->stream));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (mode != PWMGPU_POWER_AUTO && mode != PWMGPU_POWER_FUSED && mode != PWMGPU_POWER_MULTI)
+        return fail(PWMGPU_ERR_INVALID, "unknown power mode %d", mode);
+    m->power_mode = mode;
+    return PWMGPU_OK;
 }
 
 int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info) {
-    (void)x; (void)max_it; (void)tol; (void)precision; (void)info;
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
-    return fail(PWMGPU_ERR_UNSUPPORTED, "solve not built yet");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor != m->M.noc) return fail(PWMGPU_ERR_NOT_SQUARE, "power method needs a square matrix");
+    if (m->M.nor == 0) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    if (!x || !info) return fail(PWMGPU_ERR_INVALID, "null vector or info");
+    if (max_it < 2) return fail(PWMGPU_ERR_INVALID, "max_it must be at least 2 (got %d)", max_it);
+    if (!(tol >= 0.0)) return fail(PWMGPU_ERR_INVALID, "tol must be >= 0");
+    if (precision != PWMGPU_PREC_F64 && precision != PWMGPU_PREC_F32 && precision != PWMGPU_PREC_MIXED)
+        return fail(PWMGPU_ERR_INVALID, "unknown precision %d", precision);
+    if (m->power_mode == PWMGPU_POWER_MULTI)
+        return fail(PWMGPU_ERR_UNSUPPORTED, "the solve runs on the fused power kernel only");
+    std::memset(info, 0, sizeof *info);
+    return solve(m, x, max_it, tol, precision, info);
 }
 
 }  // extern "C"

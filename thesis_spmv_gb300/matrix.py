@@ -14,7 +14,8 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import FMT_COH, FMT_CSB, FMT_MERGE, PREC_F32, PREC_F64, PREC_MIXED, SolveInfo, check
+from ._lib import (FMT_COH, FMT_CSB, FMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32,  # noqa: F401
+                   PREC_F64, PREC_MIXED, SolveInfo, check)
 
 _I32 = np.int32
 _F64 = np.float64
@@ -201,7 +202,17 @@ class CudaSparseMatrix:
     def set_stream(self, stream_ptr):
         check(_lib.lib().pwmgpu_set_stream(self._h, C.c_void_p(stream_ptr)), "set_stream")
 
+    def set_power_mode(self, mode):
+        """POWER_AUTO / POWER_FUSED (one persistent kernel) / POWER_MULTI
+        (two kernels per iteration)."""
+        check(_lib.lib().pwmgpu_set_power_mode(self._h, int(mode)), "set_power_mode")
+
     def solve(self, x, max_it, tol, precision=PREC_F64):
+        """Power solve to ||A u - lambda u|| / |lambda| <= tol (or max_it
+        SpMVs); x: start vector in, normalised eigenvector estimate out.
+        Returns the SolveInfo (iterations, iterations_low, converged,
+        precision, lambda_, residual)."""
+        assert x.dtype == _F64 and x.flags.c_contiguous
         info = SolveInfo()
         check(_lib.lib().pwmgpu_solve(self._h, _ptr(x), int(max_it), float(tol), int(precision), C.byref(info)),
               "solve")
