@@ -194,8 +194,9 @@ def run_ours(args, world, rank, local):
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    grid_side = args.grid
     M = pwm.CRSCuda(1)
-    M.generatePoissonMatrix(GRID, GRID, 1)
+    M.generatePoissonMatrix(grid_side, grid_side, 1)
     N, _, nnz = M.dims()
     B = algorithmic_bytes(N, nnz)
     tm, ntiles, grid = M.tile_info()
@@ -228,34 +229,41 @@ def run_ours(args, world, rank, local):
     ms = ms_total / args.steps
     value = B * world / (ms * 1e-3) / 1e9
 
-    # ---- power method: 500 iterations (reference powerIteration semantics) ----
+    # ---- power method: 500 iterations (reference powerIteration semantics),
+    #      fused persistent kernel and two kernels per iteration ----
     p_it = args.power_iters
     px = dx.clone()
     py = torch.zeros_like(dx)
-    M.power_device(px.data_ptr(), py.data_ptr(), 4)
-    stream.synchronize()
-    px.copy_(dx)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    M.power_device(px.data_ptr(), py.data_ptr(), p_it)
-    e1.record(stream)
-    e1.synchronize()
-    power_ms = e0.elapsed_time(e1)
+    power_ms = {}
+    for mode, name in ((pwm.POWER_FUSED, "fused"), (pwm.POWER_MULTI, "multi")):
+        M.set_power_mode(mode)
+        M.power_device(px.data_ptr(), py.data_ptr(), 4)
+        stream.synchronize()
+        px.copy_(dx)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        M.power_device(px.data_ptr(), py.data_ptr(), p_it)
+        e1.record(stream)
+        e1.synchronize()
+        power_ms[name] = e0.elapsed_time(e1)
+    M.set_power_mode(pwm.POWER_AUTO)
 
     # ---- end to end through the C ABI with host buffers (pinned) ----
-    xh = x_host.pin_memory()
-    yh = torch.zeros(N, dtype=torch.float64).pin_memory()
-    xn = xh.numpy()
-    yn_ = yh.numpy()
-    M.mv(xn, yn_)
-    torch.cuda.synchronize()
-    e2e_steps = max(3, min(args.steps, 50))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        M.mv(xn, yn_)  # H2D x, SpMV, D2H y, synchronous
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_gbs = B * world / e2e_s / 1e9
+    e2e_s = float("nan")
+    e2e_steps = 0 if args.no_e2e else max(3, min(args.steps, 50))
+    if e2e_steps:
+        xh = x_host.pin_memory()
+        yh = torch.zeros(N, dtype=torch.float64).pin_memory()
+        xn = xh.numpy()
+        yn_ = yh.numpy()
+        M.mv(xn, yn_)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            M.mv(xn, yn_)  # H2D x, SpMV, D2H y, synchronous
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_gbs = B * world / e2e_s / 1e9 if e2e_steps else None
 
     peak, peak_kind = measured_peaks()
     traffic = profile_traffic().get("k_merge_spmv_f64_poisson4096")
@@ -263,23 +271,29 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "poisson2d_4096x4096_fp64_spmv", "N": N, "nnz": nnz,
+        "config": {"workload": "poisson2d_%dx%d_fp64_spmv" % (grid_side, grid_side), "N": N, "nnz": nnz,
                    "l2": "inputs larger than L2 (1.34 GB per pass)", "items_per_tile": tm, "tiles": ntiles,
                    "grid": grid, "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(B / (ms * 1e-3) / 1e9, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(B / (ms * 1e-3) / 1e9 / peak, 4), "traffic": traffic,
                      "peak_source": peak_kind, "frac_of_nominal_8TBs": round(B / (ms * 1e-3) / 1e9 / NOMINAL_HBM_GBS, 4),
                      "algorithmic_bytes_per_launch": B, "timed": "k_merge_spmv + k_merge_fixup (one SpMV)"},
-        "e2e": {"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
-                "ms_per_step": round(e2e_s * 1e3, 4), "api": "pwmgpu_mv (host arrays, pinned)"},
+        "e2e": ({"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 8 * N,
+                 "d2h_bytes_per_step": 8 * N, "ms_per_step": round(e2e_s * 1e3, 4),
+                 "api": "pwmgpu_mv (host arrays, pinned)"} if e2e_steps else None),
         "gpu_launches": 2 * args.steps,
-        "power": {"iterations": p_it, "ms_per_iteration": round(power_ms / p_it, 5),
-                  "gb_s": round(B / (power_ms / p_it * 1e-3) / 1e9, 2), "kernels_per_iteration": 2},
+        "power": {"iterations": p_it,
+                  "fused": {"ms_per_iteration": round(power_ms["fused"] / p_it, 5),
+                            "gb_s": round(B / (power_ms["fused"] / p_it * 1e-3) / 1e9, 2),
+                            "kernels": "k_power_persistent (1 launch for all iterations)"},
+                  "multi": {"ms_per_iteration": round(power_ms["multi"] / p_it, 5),
+                            "gb_s": round(B / (power_ms["multi"] / p_it * 1e-3) / 1e9, 2),
+                            "kernels": "k_merge_spmv + k_merge_fixup per iteration"}},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import pyoracle as O
-        A = O.fill_poisson(GRID, GRID)
+        A = O.fill_poisson(grid_side, grid_side)
         threads = os.cpu_count() or 1
         s, reps = cpu_baseline_sample(A, x_host.numpy(), threads)
         result["cpu_baseline"] = {"value": round(B / s / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
@@ -296,7 +310,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--power-iters", type=int, default=500)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--grid", type=int, default=GRID, help="Poisson grid side (default 4096)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -323,23 +323,43 @@ __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
 // PWMGPU_ERR_TIMEOUT and returns false in every thread of the CTA.
 // bar[0] counts arrivals, bar[1] is the generation; both start at zero.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel_gpu(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_add_release_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 of each CTA releases the CTA's writes (fence after the CTA
+// barrier) and arrives with an acq_rel atomic; the last arrival resets the
+// count and bumps the generation with a release; the others spin on the
+// generation with acquire loads.  After the final CTA barrier every thread's
+// ordinary loads see every CTA's writes from before the barrier.
 __device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = bar + 1;
-        const unsigned int g = *vgen;
+        const unsigned int g = ld_acquire_gpu(bar + 1);
         __threadfence();
-        const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
+        const unsigned int arrived = atom_add_acq_rel_gpu(bar, 1u) + 1u;
         int ok = 1;
         if (arrived == gridDim.x) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+            st_relaxed_gpu(bar, 0u);
+            red_add_release_gpu(bar + 1, 1u);
         } else {
             const long long t0 = clock64();
             unsigned int spins = 0;
-            while (*vgen == g) {
+            while (ld_acquire_gpu(bar + 1) == g) {
                 if ((++spins & 1023u) == 0u) {
                     if (*(volatile int*)status != PWMGPU_OK) { ok = 0; break; }
                     if (clock64() - t0 > kWaitCycles) {
@@ -486,15 +506,18 @@ __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p
 // ---------------------------------------------------------------------------
 // Normalise the last two iterates of the power method (VectorUtill.hpp:34-41):
 // v_last /= sqrt(nsq_last); v_prev /= sqrt(nsq_prev) when prev is an iterate.
+// The reference divides each element; here each element is multiplied by
+// the FP64 reciprocal (within 1 ulp of the quotient; an FP64 divide per
+// element would make this pass FP64-pipe bound on GB300).
 // ---------------------------------------------------------------------------
 template <typename XT>
 __global__ void k_power_finalize(XT* __restrict__ last, const double* nsq_last, XT* __restrict__ prev,
                                  const double* nsq_prev, int n) {
-    const double nl = sqrt(*nsq_last);
-    const double np = prev ? sqrt(*nsq_prev) : 1.0;
+    const double rl = 1.0 / sqrt(*nsq_last);
+    const double rp = prev ? 1.0 / sqrt(*nsq_prev) : 1.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        last[i] = (XT)((double)last[i] / nl);
-        if (prev) prev[i] = (XT)((double)prev[i] / np);
+        last[i] = (XT)((double)last[i] * rl);
+        if (prev) prev[i] = (XT)((double)prev[i] * rp);
     }
 }
 

@@ -157,7 +157,9 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 // First half of a sub-tile: the lane's gathers x[col], all issued together
 // (read from the staged columns).
 // XCOH: x was written earlier in the same launch (persistent power kernel), so
-// it is read through L2 (ld.global.cg) instead of the read-only path.
+// it is read with ordinary coherent loads (ld.global.ca: L1-cached, and
+// ordered after the grid barrier's acquire) instead of the read-only
+// non-coherent path.
 template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false>
 __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT]) {
     using S = WarpStage<VT, IPT>;
@@ -169,7 +171,7 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
     load_lane<int32_t, IPT>(reinterpret_cast<const int32_t*>(st + S::REC_B + S::MASK_B), qm, cnt, lane, cv);
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
-        if (XCOH) xv[j] = (j < cnt) ? (AT)__ldcg(x + cv[j]) : AT(0);
+        if (XCOH) xv[j] = (j < cnt) ? (AT)__ldca(x + cv[j]) : AT(0);
         else xv[j] = (j < cnt) ? (AT)__ldg(x + cv[j]) : AT(0);
     }
 }
