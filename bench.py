@@ -188,6 +188,62 @@ def run_reference(args, world, rank):
     }))
 
 
+IRREGULAR = dict(n=4194304, seed=20261203, length_dist=0, mean_len=16.0, sigma=1.2, max_len=20000,
+                 band_permille=300, band_half=4096)
+
+
+def irregular_and_solves(pwm, torch, dev, stream, args):
+    """The irregular lognormal-row matrix (N = 4,194,304, generated on the
+    device): FP64 SpMV GB/s, then power solves to 1e-10 relative
+    eigen-residual in FP64 and in mixed precision (FP32 bulk + FP64
+    refinement), each solve end to end through pwmgpu_solve (host vector in,
+    eigenvector out): solves/s, p50/p99 latency."""
+    M = pwm.CRSCuda(1)
+    M.set_stream(stream.cuda_stream)
+    M.generateRandom(**IRREGULAR)
+    N, _, nnz = M.dims()
+    B = algorithmic_bytes(N, nnz)
+    x = torch.rand(N, dtype=torch.float64, generator=torch.Generator().manual_seed(5), device="cpu").to(dev)
+    y = torch.zeros_like(x)
+    for _ in range(5):
+        M.mv_device(x.data_ptr(), y.data_ptr())
+    steps = 200
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        M.mv_device(x.data_ptr(), y.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out = {"irregular": {"workload": "lognormal_rows_n4194304_mean16_sigma1.2_band30pct", "N": N, "nnz": nnz,
+                         "spmv_ms": round(ms, 5), "spmv_gb_s": round(B / (ms * 1e-3) / 1e9, 2),
+                         "frac_of_measured_hbm": round(B / (ms * 1e-3) / 1e9 / measured_peaks()[0], 4)}}
+    x0 = np.random.default_rng(20261203).random(N)
+    solves = {}
+    lam = {}
+    for name, prec in (("fp64", pwm.PREC_F64), ("mixed", pwm.PREC_MIXED)):
+        u = x0.copy()
+        M.solve(u, 2000, 1e-10, prec)  # warm (value copies, buffers)
+        lat = []
+        info = None
+        for _ in range(args.solves):
+            u = x0.copy()
+            t0 = time.perf_counter()
+            info = M.solve(u, 2000, 1e-10, prec)
+            lat.append(time.perf_counter() - t0)
+        lat = np.array(lat) * 1e3
+        lam[name] = info.lambda_
+        solves[name] = {"solves_per_s": round(1e3 / lat.mean(), 3), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                        "p99_ms": round(float(np.percentile(lat, 99)), 3), "iterations": info.iterations,
+                        "iterations_low_precision": info.iterations_low, "converged": bool(info.converged),
+                        "residual": info.residual, "lambda": info.lambda_}
+    solves["mixed"]["lambda_rel_diff_vs_fp64"] = abs(lam["mixed"] - lam["fp64"]) / abs(lam["fp64"])
+    solves["speedup_mixed_vs_fp64"] = round(solves["mixed"]["solves_per_s"] / solves["fp64"]["solves_per_s"], 3)
+    out["solve_irregular_1e-10"] = solves
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import thesis_spmv_gb300 as pwm
@@ -265,6 +321,8 @@ def run_ours(args, world, rank, local):
         e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_gbs = B * world / e2e_s / 1e9 if e2e_steps else None
 
+    extra = None if args.no_extra else irregular_and_solves(pwm, torch, dev, stream, args)
+
     peak, peak_kind = measured_peaks()
     traffic = profile_traffic().get("k_merge_spmv_f64_poisson4096")
     result = {
@@ -291,6 +349,8 @@ def run_ours(args, world, rank, local):
                             "kernels": "k_merge_spmv + k_merge_fixup per iteration"}},
         "clocks": clk.summary(),
     }
+    if extra:
+        result.update(extra)
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import pyoracle as O
         A = O.fill_poisson(grid_side, grid_side)
@@ -313,6 +373,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--grid", type=int, default=GRID, help="Poisson grid side (default 4096)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the irregular matrix and the solves")
+    ap.add_argument("--solves", type=int, default=20, help="timed solves per precision")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

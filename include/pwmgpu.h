@@ -70,6 +70,21 @@ int pwmgpu_destroy(pwmgpu_matrix* m);
  * later work of this handle instead of its own stream. */
 int pwmgpu_set_stream(pwmgpu_matrix* m, void* stream);
 
+/* Seeded random square matrix generated on the device (no counterpart in
+ * the reference: the benchmarks' irregular and batch workloads).  Row
+ * lengths: PWMGPU_RAND_LOGNORMAL -- clip(round(exp(mu + sigma Z)), 1,
+ * max_len) with mu = ln(mean_len) - sigma^2/2; PWMGPU_RAND_POISSON --
+ * Poisson(mean_len) clipped to max_len.  band_permille / 1000 of a row's
+ * columns fall within +-band_half of the diagonal, the rest anywhere in
+ * [0, n); each part is stratified (sorted, no duplicates) and a column drawn
+ * by both is kept once.  Values in (0, 1].  Every array is a deterministic
+ * function of the arguments (integer hashing), reproduced bit for bit by the
+ * host restatement in the test oracle. */
+#define PWMGPU_RAND_LOGNORMAL 0
+#define PWMGPU_RAND_POISSON 1
+int pwmgpu_generate_random(pwmgpu_matrix* m, int32_t n, uint64_t seed, int length_dist, double mean_len,
+                           double sigma, int32_t max_len, int32_t band_permille, int32_t band_half);
+
 /* Replaces generatePoissonMatrix(m, n, partitions) (SparseMatrix.hpp:41,
  * CRS.hpp:60-74, CSB.hpp:576-582, BlockCOH.hpp:464-470).  The merge format
  * writes the CRS arrays on the device in Util/Poisson.hpp:32-83 order. */

@@ -664,3 +664,112 @@ int64_t orc_load_bin(const char* filename, int32_t mat_size, int symmetric, int3
     fclose(f);
     return k;
 }
+
+/* ------------------------------------------------------------------ */
+/* Seeded random matrices (benchmark inputs; no reference counterpart)  */
+/* ------------------------------------------------------------------ */
+/* Host restatement of the library's device generator (row lengths from a
+ * CDF table scaled by 2^53, stratified uniform and band columns merged
+ * without duplicates, values from a hash of (row, column)); the hash is the
+ * splitmix64 finaliser (Steele, Lea, Flood 2014) applied twice. */
+
+static uint64_t rg_mix(uint64_t z) {
+    z ^= z >> 30;
+    z *= 0xbf58476d1ce4e5b9ull;
+    z ^= z >> 27;
+    z *= 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    return z;
+}
+
+static uint64_t rg_hash(uint64_t seed, uint64_t i, uint64_t k) {
+    const uint64_t g = 0x9e3779b97f4a7c15ull;
+    return rg_mix(rg_mix(seed + g * (i + 1)) + g * (k + 1));
+}
+
+void orc_random_table(int kind, double mean, double sigma, int32_t max_len, uint64_t* thr) {
+    const double two53 = 9007199254740992.0;
+    double cdf = 0., pmf = 0.;
+    double mu = log(mean) - 0.5 * sigma * sigma;
+    for (int32_t l = 0; l <= max_len; ++l) thr[l] = (uint64_t)1 << 53;
+    for (int32_t l = 0; l < max_len; ++l) {
+        if (kind == 0) {
+            /* P(round(exp(mu + sigma Z)) <= l) = Phi((ln(l + 1/2) - mu) / sigma) */
+            cdf = l == 0 ? 0. : 0.5 * erfc(-((log(l + 0.5) - mu) / sigma) * 0.70710678118654752440);
+        } else {
+            pmf = l == 0 ? exp(-mean) : pmf * mean / l;
+            cdf = cdf + pmf;
+        }
+        double t = floor(cdf * two53);
+        thr[l] = t >= two53 ? ((uint64_t)1 << 53) : (uint64_t)t;
+    }
+}
+
+typedef struct {
+    const uint64_t* thr;
+    int32_t max_len, n;
+    uint64_t seed;
+    int32_t band_permille, band_half;
+} orc_rowgen;
+
+static int32_t rg_row(const orc_rowgen* g, int32_t i, int32_t* col, double* val) {
+    uint64_t u = rg_hash(g->seed, (uint64_t)i, 0) >> 11;
+    int32_t lo = 0, hi = g->max_len;
+    while (lo < hi) { /* smallest l with u < thr[l] */
+        int32_t mid = (lo + hi) / 2;
+        if (u < g->thr[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    long long L = lo;
+    int32_t b0 = i - g->band_half > 0 ? i - g->band_half : 0;
+    int32_t b1 = i + (long long)g->band_half < g->n - 1 ? i + g->band_half : g->n - 1;
+    long long wb = (long long)b1 - b0 + 1;
+    long long lb = 0, lu;
+    if (g->band_permille > 0) lb = (L * g->band_permille + (long long)(rg_hash(g->seed, (uint64_t)i, 1) % 1000)) / 1000;
+    if (lb > wb) lb = wb;
+    lu = L - lb;
+    if (lu > g->n) lu = g->n;
+    /* the two stratified parts, each sorted, merged */
+    long long ju = 0, jb = 0;
+    int32_t cnt = 0;
+    while (ju < lu || jb < lb) {
+        long long cu = 0, cb = 0;
+        if (ju < lu) {
+            long long l0 = ju * g->n / lu, h0 = (ju + 1) * g->n / lu;
+            cu = l0 + (long long)(rg_hash(g->seed, (uint64_t)i, (uint64_t)(2 + 2 * ju)) % (uint64_t)(h0 - l0));
+        }
+        if (jb < lb) {
+            long long l0 = b0 + jb * wb / lb, h0 = b0 + (jb + 1) * wb / lb;
+            cb = l0 + (long long)(rg_hash(g->seed, (uint64_t)i, (uint64_t)(3 + 2 * jb)) % (uint64_t)(h0 - l0));
+        }
+        long long c;
+        if (jb >= lb || (ju < lu && cu < cb)) { c = cu; ++ju; }
+        else if (ju >= lu || cb < cu) { c = cb; ++jb; }
+        else { c = cu; ++ju; ++jb; }
+        if (col) {
+            col[cnt] = (int32_t)c;
+            val[cnt] = (double)((rg_hash(g->seed ^ 0xd6e8feb86659fd93ull, (uint64_t)i, (uint64_t)c) >> 11) + 1) *
+                       (1.0 / 9007199254740992.0);
+        }
+        ++cnt;
+    }
+    return cnt;
+}
+
+int64_t orc_random_crs(int32_t n, uint64_t seed, int kind, double mean, double sigma, int32_t max_len,
+                       int32_t band_permille, int32_t band_half, int32_t* row_start, int32_t* col_ind,
+                       double* data) {
+    uint64_t* thr = (uint64_t*)malloc(sizeof(uint64_t) * ((size_t)max_len + 1));
+    orc_random_table(kind, mean, sigma, max_len, thr);
+    orc_rowgen g = {thr, max_len, n, seed, band_permille, band_half};
+    int64_t nnz = 0;
+    if (row_start) row_start[0] = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t c = rg_row(&g, i, col_ind ? col_ind + nnz : NULL, data ? data + nnz : NULL);
+        nnz += c;
+        if (row_start) row_start[i + 1] = (int32_t)nnz;
+    }
+    free(thr);
+    return nnz;
+}
+

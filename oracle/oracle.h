@@ -108,6 +108,14 @@ int64_t orc_load_mm(const char* filename, int has_data, int symmetric, int32_t* 
 int64_t orc_load_bin(const char* filename, int32_t mat_size, int symmetric, int32_t* rows, int32_t* cols,
                      double* vals, int64_t capacity);
 
+/* Seeded random matrices: restatement of the library's device generator
+ * (benchmark inputs, no reference counterpart).  Call with NULL arrays to
+ * get nnz, then with row_start[n+1], col_ind[nnz], data[nnz]. */
+void orc_random_table(int kind, double mean, double sigma, int32_t max_len, uint64_t* thr);
+int64_t orc_random_crs(int32_t n, uint64_t seed, int kind, double mean, double sigma, int32_t max_len,
+                       int32_t band_permille, int32_t band_half, int32_t* row_start, int32_t* col_ind,
+                       double* data);
+
 #ifdef __cplusplus
 }
 #endif

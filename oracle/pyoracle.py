@@ -40,6 +40,10 @@ def lib():
         L.orc_normalize.argtypes = [F64P, C.c_int64]
         L.orc_power.argtypes = [C.c_int, C.c_int32, C.c_int32, I32P, I32P, F64P, F64P, F64P, C.c_int32, C.c_int]
         L.orc_rayleigh.argtypes = [C.c_int32, I32P, I32P, F64P, F64P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_random_table.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int32, C.c_void_p]
+        L.orc_random_crs.argtypes = [C.c_int32, C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_random_crs.restype = C.c_int64
         L.orc_csb_params.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.orc_csb_build.restype = C.c_int
         L.orc_csb_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, I32P, I32P, F64P, U32P, F64P, I32P]
@@ -166,6 +170,25 @@ def rayleigh(A, u):
     lam, res = C.c_double(), C.c_double()
     lib().orc_rayleigh(A.nor, A.row_start, _nz(A.col_ind, np.int32), _nz(A.data), u, C.byref(lam), C.byref(res))
     return lam.value, res.value
+
+
+def random_table(kind, mean, sigma, max_len):
+    thr = np.zeros(max_len + 1, np.uint64)
+    lib().orc_random_table(kind, mean, sigma, max_len, thr.ctypes.data)
+    return thr
+
+
+def random_crs(n, seed, kind=0, mean=16.0, sigma=1.2, max_len=20000, band_permille=300, band_half=4096):
+    """The seeded random matrix of the library's device generator
+    (pwmgpu_generate_random), restated on the host: CRSArrays."""
+    L = lib()
+    nnz = L.orc_random_crs(n, seed, kind, mean, sigma, max_len, band_permille, band_half, None, None, None)
+    rs = np.zeros(n + 1, np.int32)
+    ci = np.zeros(max(nnz, 1), np.int32)
+    d = np.zeros(max(nnz, 1), np.float64)
+    L.orc_random_crs(n, seed, kind, mean, sigma, max_len, band_permille, band_half, rs.ctypes.data, ci.ctypes.data,
+                     d.ctypes.data)
+    return CRSArrays(n, n, rs, ci[:nnz], d[:nnz])
 
 
 def csb_params(nor, noc):

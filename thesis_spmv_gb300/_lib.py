@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ER
 FMT_MERGE, FMT_CSB, FMT_COH = 0, 1, 2
 PREC_F64, PREC_F32, PREC_MIXED = 0, 1, 2
 POWER_AUTO, POWER_FUSED, POWER_MULTI = 0, 1, 2
+RAND_LOGNORMAL, RAND_POISSON = 0, 1
 
 
 class PwmGpuError(RuntimeError):
@@ -45,6 +46,7 @@ SIGNATURES = {
     "pwmgpu_destroy": (C.c_int, [vp]),
     "pwmgpu_set_stream": (C.c_int, [vp, vp]),
     "pwmgpu_generate_poisson": (C.c_int, [vp, i32, i32]),
+    "pwmgpu_generate_random": (C.c_int, [vp, i32, C.c_uint64, C.c_int, C.c_double, C.c_double, i32, i32, i32]),
     "pwmgpu_load_csr": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_load_triplets": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_dims": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64)]),

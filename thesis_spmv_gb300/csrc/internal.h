@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "pwmgpu.h"
 
@@ -95,6 +96,17 @@ cudaError_t launch_convert_f64_f32(const double* s, float* d, long long n, int s
 cudaError_t launch_convert_f32_f64(const float* s, double* d, long long n, int sm_count, cudaStream_t st);
 cudaError_t launch_convert_f64_bf16(const double* s, void* d, long long n, int sm_count, cudaStream_t st);
 cudaError_t launch_bf16_exact(const double* v, long long n, int* flag, int sm_count, cudaStream_t st);
+
+// gen.cu: seeded random sparse matrices and an in-place int32 inclusive scan
+void random_length_table(int kind, double mean, double sigma, int max_len, std::vector<uint64_t>& thr);
+cudaError_t launch_random_count(const uint64_t* thr, int max_len, int n, uint64_t seed, int band_permille,
+                                int band_half, int32_t* row_start, unsigned long long* total, int sm_count,
+                                cudaStream_t st);
+cudaError_t launch_random_fill(const uint64_t* thr, int max_len, int n, uint64_t seed, int band_permille,
+                               int band_half, const int32_t* row_start, int32_t* col, double* val, int sm_count,
+                               cudaStream_t st);
+long long scan_scratch_elems(long long n);
+cudaError_t launch_inclusive_scan(int32_t* a, long long n, int32_t* scratch, cudaStream_t st);
 
 // Record the calling thread's last error message (pwmgpu_last_error).
 void record_error(const char* msg);

@@ -574,6 +574,66 @@ int pwmgpu_generate_poisson(pwmgpu_matrix* m, int32_t mx, int32_t ny) {
     return build_plan(m);
 }
 
+int pwmgpu_generate_random(pwmgpu_matrix* m, int32_t n, uint64_t seed, int length_dist, double mean_len,
+                           double sigma, int32_t max_len, int32_t band_permille, int32_t band_half) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (n < 1) return fail(PWMGPU_ERR_INVALID, "n must be >= 1");
+    if (length_dist != PWMGPU_RAND_LOGNORMAL && length_dist != PWMGPU_RAND_POISSON)
+        return fail(PWMGPU_ERR_INVALID, "unknown length distribution %d", length_dist);
+    if (!(mean_len > 0.0) || !std::isfinite(mean_len)) return fail(PWMGPU_ERR_INVALID, "mean_len must be > 0");
+    if (length_dist == PWMGPU_RAND_LOGNORMAL && !(sigma > 0.0 && std::isfinite(sigma)))
+        return fail(PWMGPU_ERR_INVALID, "sigma must be > 0");
+    if (max_len < 1 || max_len > (1 << 20)) return fail(PWMGPU_ERR_INVALID, "max_len must be in [1, 2^20]");
+    if (band_permille < 0 || band_permille > 1000) return fail(PWMGPU_ERR_INVALID, "band_permille in [0, 1000]");
+    if (band_half < 0 || band_half > (1 << 30)) return fail(PWMGPU_ERR_INVALID, "band_half in [0, 2^30]");
+    std::vector<uint64_t> thr;
+    random_length_table(length_dist == PWMGPU_RAND_LOGNORMAL ? 0 : 1, mean_len, sigma, max_len, thr);
+    m->release_matrix();
+    uint64_t* dthr = nullptr;
+    unsigned long long* dtotal = nullptr;
+    int32_t* scratch = nullptr;
+    int rc = PWMGPU_OK;
+    do {
+        if ((rc = dalloc(&dthr, thr.size())) != PWMGPU_OK) break;
+        if ((rc = dalloc(&dtotal, 1)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&scratch, (size_t)scan_scratch_elems(n))) != PWMGPU_OK) break;
+        if ((rc = dalloc(&m->M.row_start, (size_t)n + 1 + kPad)) != PWMGPU_OK) break;
+        m->M.nor = m->M.noc = n;
+        cudaError_t e = cudaMemcpyAsync(dthr, thr.data(), thr.size() * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                        m->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dtotal, 0, sizeof(unsigned long long), m->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->M.row_start + n + 1, 0, kPad * sizeof(int32_t), m->stream);
+        if (e == cudaSuccess)
+            e = launch_random_count(dthr, max_len, n, seed, band_permille, band_half, m->M.row_start, dtotal,
+                                    m->sm_count, m->stream);
+        unsigned long long total = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&total, dtotal, sizeof total, cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "random generator: %s", cudaGetErrorString(e)); break; }
+        if ((rc = check_sizes(n, n, (long long)total)) != PWMGPU_OK) break;
+        m->M.nnz = (long long)total;
+        e = launch_inclusive_scan(m->M.row_start + 1, n, scratch, m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "scan: %s", cudaGetErrorString(e)); break; }
+        if ((rc = dalloc(&m->M.col, (size_t)total + kPad)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&m->M.val, (size_t)total + kPad)) != PWMGPU_OK) break;
+        e = cudaMemsetAsync(m->M.col + total, 0, kPad * sizeof(int32_t), m->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(m->M.val + total, 0, kPad * sizeof(double), m->stream);
+        if (e == cudaSuccess)
+            e = launch_random_fill(dthr, max_len, n, seed, band_permille, band_half, m->M.row_start, m->M.col,
+                                   m->M.val, m->sm_count, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "random generator: %s", cudaGetErrorString(e)); break; }
+    } while (0);
+    dfree(dthr);
+    dfree(dtotal);
+    dfree(scratch);
+    if (rc != PWMGPU_OK) {
+        m->release_matrix();
+        return rc;
+    }
+    return build_plan(m);
+}
+
 int pwmgpu_load_csr(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
                     const int32_t* col_ind, const double* vals) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");

@@ -142,6 +142,15 @@ class CudaSparseMatrix:
     def generatePoissonMatrix(self, m, n, partitions=1):
         check(_lib.lib().pwmgpu_generate_poisson(self._h, int(m), int(n)), "generatePoissonMatrix")
 
+    def generateRandom(self, n, seed, length_dist=0, mean_len=16.0, sigma=1.2, max_len=20000, band_permille=300,
+                       band_half=4096):
+        """Seeded random n x n matrix generated on the device (lognormal
+        (length_dist 0) or Poisson (1) row lengths, band_permille / 1000 of
+        the columns within +-band_half of the diagonal, values in (0, 1])."""
+        check(_lib.lib().pwmgpu_generate_random(self._h, int(n), int(seed) & (2 ** 64 - 1), int(length_dist),
+                                                float(mean_len), float(sigma), int(max_len), int(band_permille),
+                                                int(band_half)), "generateRandom")
+
     # ---- SparseMatrix.hpp:48 ----
     def loadFromTriplets(self, triplet, partitions_am=1):
         for name in ("row_coord", "col_coord", "data"):
