@@ -773,3 +773,8 @@ int64_t orc_random_crs(int32_t n, uint64_t seed, int kind, double mean, double s
     return nnz;
 }
 
+void orc_uniform_vector(int32_t n, uint64_t seed, double* x) {
+    /* the service's seeded start vector: x[i] = (mix(seed + g (i + 1)) >> 11) 2^-53 */
+    for (int32_t i = 0; i < n; ++i)
+        x[i] = (double)(rg_mix(seed + 0x9e3779b97f4a7c15ull * (uint64_t)(i + 1)) >> 11) * (1.0 / 9007199254740992.0);
+}

@@ -116,6 +116,9 @@ int64_t orc_random_crs(int32_t n, uint64_t seed, int kind, double mean, double s
                        int32_t band_permille, int32_t band_half, int32_t* row_start, int32_t* col_ind,
                        double* data);
 
+/* The batched service's seeded start vector (uniform in [0, 1)). */
+void orc_uniform_vector(int32_t n, uint64_t seed, double* x);
+
 #ifdef __cplusplus
 }
 #endif

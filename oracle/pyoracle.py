@@ -44,6 +44,7 @@ def lib():
         L.orc_random_crs.argtypes = [C.c_int32, C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                      C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_random_crs.restype = C.c_int64
+        L.orc_uniform_vector.argtypes = [C.c_int32, C.c_uint64, C.c_void_p]
         L.orc_csb_params.argtypes = [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.orc_csb_build.restype = C.c_int
         L.orc_csb_build.argtypes = [C.c_int32, C.c_int32, C.c_int32, I32P, I32P, F64P, U32P, F64P, I32P]
@@ -189,6 +190,13 @@ def random_crs(n, seed, kind=0, mean=16.0, sigma=1.2, max_len=20000, band_permil
     L.orc_random_crs(n, seed, kind, mean, sigma, max_len, band_permille, band_half, rs.ctypes.data, ci.ctypes.data,
                      d.ctypes.data)
     return CRSArrays(n, n, rs, ci[:nnz], d[:nnz])
+
+
+def uniform_vector(n, seed):
+    """The service's seeded start vector (x0_seed): uniform in [0, 1)."""
+    x = np.zeros(n, np.float64)
+    lib().orc_uniform_vector(n, seed & (2 ** 64 - 1), x.ctypes.data)
+    return x
 
 
 def csb_params(nor, noc):

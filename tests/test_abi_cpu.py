@@ -40,8 +40,12 @@ def test_python_binding_covers_header():
     from thesis_spmv_gb300 import _lib
     declared = set(declared_symbols())
     bound = set(_lib.SIGNATURES)
-    # every pwmgpu_ symbol has a ctypes signature (service symbols are bound in service.py)
+    # every pwmgpu_ symbol has a ctypes signature; the service's pwmsvc_ ones
+    # are bound in service.py
     assert {n for n in declared if n.startswith("pwmgpu_")} <= bound
+    from thesis_spmv_gb300 import service
+    assert {n for n in declared if n.startswith("pwmsvc_")} <= set(service.SIGNATURES)
+    service.lib()  # binds every pwmsvc_ signature
 
 
 def _cuda_present():

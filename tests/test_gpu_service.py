@@ -1,0 +1,176 @@
+"""The batched power-method service (include/pwmsvc.h) against the oracle.
+
+Each round advances every live solve in one launch per power step (their
+merge-path sub-tiles form the block-diagonal merge path of the live
+matrices).  Tolerances as for pwmgpu_solve: at equal step counts lambda and u
+within 1e-10 relative of the oracle; converged results confirmed by the
+oracle's residual (within 2 tol) and, for Poisson grids, the analytic
+lambda_max = 4 + 4 cos(pi/(m+1)) within 1e-10.  A solve gives the same bits
+alone and in a mix (sums run over each solve's own sub-tiles in a fixed
+order); the test asserts bit equality, which implies the stated tolerance.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def svc_mod():
+    import thesis_spmv_gb300 as t
+    from thesis_spmv_gb300 import service
+    t.lib()
+    service.lib()
+    return t, service
+
+
+def _positive_random(n, mean_len, seed):
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(n):
+        c = set(rng.integers(0, n, size=int(rng.poisson(mean_len))).tolist()) | {i, (i + 1) % n}
+        rows.append(np.array(sorted(c), np.int32))
+    rs = np.zeros(n + 1, np.int32)
+    rs[1:] = np.cumsum([r.size for r in rows])
+    cols = np.concatenate(rows)
+    return O.CRSArrays(n, n, rs, cols, rng.uniform(0.0, 1.0, cols.size) + 1e-3)
+
+
+def test_service_poisson_analytic(svc_mod):
+    t, S = svc_mod
+    svc = S.Service(round_iterations=8)
+    m = 8
+    rid = svc.submit_poisson(m, m, max_it=20000, tol=1e-10, precision=t.PREC_F64, x0_seed=3, keep_vector=True)
+    svc.run_until_idle()
+    r, u = svc.result(rid, want_vector=True)
+    assert r.state == S.DONE and r.converged == 1 and r.residual <= 1e-10
+    exact = 4.0 + 4.0 * math.cos(math.pi / (m + 1))
+    assert abs(r.lambda_ - exact) <= 1e-10 * exact
+    lam_r, res_r = O.rayleigh(O.fill_poisson(m, m), u)
+    assert res_r <= 2e-10 and abs(lam_r - exact) <= 1e-10 * exact
+    assert r.iterations % 8 == 0
+
+
+@pytest.mark.parametrize("seeded", [True, False])
+def test_service_equal_counts_match_oracle(svc_mod, seeded):
+    """tol = 0: exactly max_it steps (3 rounds of 8); lambda and u are those
+    of the oracle's iterate after 23 powerIteration steps."""
+    t, S = svc_mod
+    A = O.fill_poisson(29, 31)
+    svc = S.Service(round_iterations=8)
+    if seeded:
+        x0 = O.uniform_vector(A.nor, 77)
+        rid = svc.submit_poisson(29, 31, max_it=24, tol=0.0, x0_seed=77, keep_vector=True)
+    else:
+        x0 = np.random.default_rng(5).random(A.nor)
+        rid = svc.submit_csr(A, max_it=24, tol=0.0, x0=x0, keep_vector=True)
+    svc.run_until_idle()
+    r, u = svc.result(rid, want_vector=True)
+    assert r.state == S.DONE and r.iterations == 24 and r.converged == 0
+    ur = O.power_result(A, x0, 23)
+    lam_r, res_r = O.rayleigh(A, ur)
+    assert abs(r.lambda_ - lam_r) <= 1e-10 * abs(lam_r)
+    assert abs(r.residual - res_r) <= 1e-8 * res_r
+    assert np.max(np.abs(u - ur)) <= 1e-10 * np.max(np.abs(ur))
+
+
+def _run_target(S, t, others, use_graph=True):
+    """The target solve, submitted between other requests over several
+    rounds; returns its result and vector."""
+    svc = S.Service(round_iterations=8, use_graph=use_graph)
+    for o in others[: len(others) // 2]:
+        o(svc)
+    if others:
+        svc.step()
+        svc.step()
+    rid = svc.submit_random(6000, 42, mean_len=12.0, max_it=4000, tol=1e-10, precision=t.PREC_MIXED,
+                            x0_seed=9, keep_vector=True)
+    for o in others[len(others) // 2:]:
+        svc.step()
+        o(svc)
+    svc.run_until_idle()
+    return svc.result(rid, want_vector=True)
+
+
+def test_service_alone_equals_mix(svc_mod):
+    """The same request alone and among others (sizes, sources and
+    precisions mixed, arriving before and after it) gives identical bits."""
+    t, S = svc_mod
+    A = _positive_random(2000, 6, 1)
+    others = [
+        lambda s: s.submit_poisson(40, 25, max_it=300, tol=1e-10, precision=t.PREC_F64),
+        lambda s: s.submit_random(50000, 7, length_dist=1, mean_len=8.0, max_len=64, band_permille=0, band_half=0,
+                                  max_it=400, tol=1e-10, precision=t.PREC_MIXED),
+        lambda s: s.submit_csr(A, max_it=200, tol=1e-12, precision=t.PREC_F32),
+        lambda s: s.submit_poisson(128, 128, max_it=160, tol=1e-10, precision=t.PREC_MIXED),
+        lambda s: s.submit_random(20000, 3, max_it=400, tol=1e-10, precision=t.PREC_F64),
+        lambda s: s.submit_random(1000, 5, mean_len=4.0, max_it=64, tol=0.0, precision=t.PREC_F64),
+    ]
+    r1, u1 = _run_target(S, t, [])
+    r2, u2 = _run_target(S, t, others)
+    assert r1.state == S.DONE and r1.converged == 1 and r1.iterations_low > 0
+    for f in ("iterations", "iterations_low", "converged"):
+        assert getattr(r1, f) == getattr(r2, f), f
+    assert r1.lambda_ == r2.lambda_ and r1.residual == r2.residual
+    assert np.array_equal(u1.view(np.uint64), u2.view(np.uint64))
+    # and the oracle confirms the result
+    B = O.random_crs(6000, 42, 0, 12.0, 1.2, 20000, 300, 4096)
+    lam_r, res_r = O.rayleigh(B, u1)
+    assert res_r <= 2e-10 and abs(lam_r - r1.lambda_) <= 1e-10 * abs(lam_r)
+
+
+def test_service_graph_equals_direct_launches(svc_mod):
+    t, S = svc_mod
+    r1, u1 = _run_target(S, t, [], use_graph=True)
+    r2, u2 = _run_target(S, t, [], use_graph=False)
+    assert r1.iterations == r2.iterations and r1.lambda_ == r2.lambda_
+    assert np.array_equal(u1, u2)
+
+
+def test_service_budget_admission(svc_mod):
+    t, S = svc_mod
+    n = 200_000
+    # each request is charged about 31 MB (plan, CRS during the build,
+    # vectors, for 1.1 nnz estimated per unit of mean row length): two fit
+    svc = S.Service(hbm_budget_bytes=80 << 20, round_iterations=4)
+    with pytest.raises(t.PwmGpuError) as e:
+        svc.submit_random(50 * n, 1, mean_len=16.0, max_it=10, tol=0.0)
+    assert e.value.code == 7  # PWMGPU_ERR_BUDGET
+    ids = [svc.submit_random(n, s, length_dist=1, mean_len=5.0, max_len=64, band_permille=0, band_half=0,
+                             max_it=8, tol=0.0) for s in range(6)]
+    saw_queue = False
+    for _ in range(1000):
+        live, queued, _ = svc.step()
+        st = svc.stats()
+        assert st.hbm_in_use <= st.hbm_budget
+        saw_queue |= live > 0 and queued > 0
+        if live == 0 and queued == 0:
+            break
+    assert saw_queue
+    for rid in ids:
+        r = svc.result(rid)
+        assert r.state == S.DONE and r.iterations == 8
+        assert r.t_submit <= r.t_admit <= r.t_done
+
+
+def test_service_mixed_and_f32_against_oracle(svc_mod):
+    t, S = svc_mod
+    A = _positive_random(20000, 8, 9)
+    svc = S.Service(round_iterations=8)
+    x0 = np.random.default_rng(2).random(A.nor)
+    ids = {p: svc.submit_csr(A, max_it=2000, tol=tol, precision=p, x0=x0, keep_vector=True)
+           for p, tol in ((t.PREC_F64, 1e-10), (t.PREC_MIXED, 1e-10), (t.PREC_F32, 1e-5))}
+    svc.run_until_idle()
+    res = {p: svc.result(rid, want_vector=True) for p, rid in ids.items()}
+    (r64, u64), (rmx, umx), (r32, u32) = res[t.PREC_F64], res[t.PREC_MIXED], res[t.PREC_F32]
+    assert r64.converged == rmx.converged == r32.converged == 1
+    assert 0 < rmx.iterations_low < rmx.iterations and r32.iterations_low == r32.iterations
+    for u, tol in ((u64, 1e-10), (umx, 1e-10)):
+        lam_r, res_r = O.rayleigh(A, u)
+        assert res_r <= 2 * tol and abs(lam_r - r64.lambda_) <= 1e-10 * abs(lam_r)
+    lam_r, res_r = O.rayleigh(A, u32)
+    assert res_r <= 1e-4 and abs(lam_r - r64.lambda_) <= 1e-5 * abs(lam_r)

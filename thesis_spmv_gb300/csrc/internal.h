@@ -108,6 +108,13 @@ cudaError_t launch_random_fill(const uint64_t* thr, int max_len, int n, uint64_t
 long long scan_scratch_elems(long long n);
 cudaError_t launch_inclusive_scan(int32_t* a, long long n, int32_t* scratch, cudaStream_t st);
 
+// batch.cu: one round (`steps` power steps + the residual pass) of every slot
+// of a class table; seeded uniform start vectors
+struct BatchTable;
+void batch_prepare(int sm_count);
+cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st);
+cudaError_t launch_fill_uniform(double* x, int n, uint64_t seed, int sm_count, cudaStream_t st);
+
 // Record the calling thread's last error message (pwmgpu_last_error).
 void record_error(const char* msg);
 

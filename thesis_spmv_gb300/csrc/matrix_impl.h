@@ -1,0 +1,152 @@
+// matrix_impl.h -- the pwmgpu_matrix handle and the host helpers shared by
+// the C ABI (pwmgpu.cpp) and the batched service (service.cpp).  Not part of
+// the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "internal.h"
+#include "pwmgpu.h"
+
+namespace pwmgpu {
+
+// Record a failure for pwmgpu_last_error() and return `code`.
+int fail(int code, const char* fmt, ...);
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(e_ == cudaErrorMemoryAllocation ? PWMGPU_ERR_NOMEM : PWMGPU_ERR_CUDA,     \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define TRY(expr)                 \
+    do {                          \
+        int r_ = (expr);          \
+        if (r_ != PWMGPU_OK) return r_; \
+    } while (0)
+
+constexpr int kPad = 16;  // kArrayPad in merge.cuh
+
+template <typename T>
+inline int dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(PWMGPU_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    return PWMGPU_OK;
+}
+
+template <typename T>
+inline void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace pwmgpu
+
+struct pwmgpu_matrix {
+    using DevMatrix = pwmgpu::DevMatrix;
+    using MliPlan = pwmgpu::MliPlan;
+    int format = PWMGPU_FMT_MERGE;
+    int partitions = 1;
+    int device = 0;
+    int sm_count = 1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bool loaded = false;
+
+    DevMatrix M;
+
+    // merge-path plan: sub-tiles of tm merge items (num_tiles of them), the
+    // lane-interleaved arrays, and launch geometry
+    int cfg = pwmgpu::kCfgF64;
+    int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
+    // persistent power kernel grids per configuration (0: not launchable)
+    int pgrid = 0, pgrid32 = 0, pgridbf = 0;
+    int power_mode = PWMGPU_POWER_AUTO;
+    MliPlan P;
+    // lane-interleaved FP32 / BF16 copies of the values (lazy)
+    float* val32 = nullptr;
+    void* valbf = nullptr;
+    int bf16_exact = -1;
+
+    // scratch
+    double* carries = nullptr;  // max(num_tiles, num_tiles32) doubles (also used as floats)
+    size_t carries_cap = 0;
+    double* partials = nullptr;  // spmv partials
+    size_t partials_cap = 0;
+    double* fix_partials = nullptr;
+    size_t fix_cap = 0;
+    unsigned int* counter = nullptr;
+    double* nsq = nullptr;
+    size_t nsq_cap = 0;
+    double* small = nullptr;  // 16 doubles of reduction outputs
+    int* status = nullptr;
+    unsigned int* barrier = nullptr;  // grid barrier words of the persistent kernel
+    double* hres = nullptr;           // pinned host copy of a solve chunk's results
+
+    // host-facing vector buffers
+    double* dx = nullptr;
+    double* dy = nullptr;
+    size_t vec_cap = 0;
+    float* fx = nullptr;
+    float* fy = nullptr;
+    size_t fvec_cap = 0;
+
+    void release_matrix() {
+        pwmgpu::dfree(M.row_start);
+        pwmgpu::dfree(M.col);
+        pwmgpu::dfree(M.val);
+        pwmgpu::dfree(P.subc);
+        pwmgpu::dfree(P.rec);
+        pwmgpu::dfree(P.masks);
+        pwmgpu::dfree(P.colp);
+        pwmgpu::dfree(P.valp);
+        P = MliPlan();
+        pwmgpu::dfree(val32);
+        if (valbf) cudaFree(valbf);
+        valbf = nullptr;
+        bf16_exact = -1;
+        M = DevMatrix();
+        num_tiles = 0;
+        loaded = false;
+    }
+    void release_all() {
+        release_matrix();
+        pwmgpu::dfree(carries);
+        pwmgpu::dfree(partials);
+        pwmgpu::dfree(fix_partials);
+        pwmgpu::dfree(counter);
+        pwmgpu::dfree(nsq);
+        pwmgpu::dfree(small);
+        pwmgpu::dfree(status);
+        pwmgpu::dfree(barrier);
+        if (hres) cudaFreeHost(hres);
+        hres = nullptr;
+        pwmgpu::dfree(dx);
+        pwmgpu::dfree(dy);
+        pwmgpu::dfree(fx);
+        pwmgpu::dfree(fy);
+        carries_cap = partials_cap = fix_cap = nsq_cap = vec_cap = fvec_cap = 0;
+    }
+};
+
+
+namespace pwmgpu {
+
+// Host helpers of a handle (pwmgpu.cpp).
+int check_status(pwmgpu_matrix* m);
+int check_sizes(long long nor, long long noc, long long nnz);
+int build_plan(pwmgpu_matrix* m);
+int ensure_vectors(pwmgpu_matrix* m);
+int ensure_fvectors(pwmgpu_matrix* m);
+int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** valp, int* pgrid);
+
+}  // namespace pwmgpu

@@ -233,41 +233,6 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// Fix-up: add each sub-tile's carry to the row the sub-tile left unfinished.
-// One thread per sub-tile; the first sub-tile of a run of sub-tiles ending in
-// the same row adds the run in order (deterministic).  The run's row r is
-// completed (and its partial written) by the first sub-tile after the run; the
-// carry is real only if that sub-tile started inside row r.  MODE_POWER also
-// sums the squares (and, with xdot, x[r]*y[r]) of the rows fixed here.
-// ---------------------------------------------------------------------------
-template <int MODE, typename XT, typename AT>
-__device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start, const int2* __restrict__ tiles,
-                                           int nor, int num_tiles, XT* __restrict__ y, const AT* __restrict__ carries,
-                                           int e, double& sumsq, const XT* __restrict__ xdot, double* dot, int t0,
-                                           int stride) {
-    for (int t = t0; t < num_tiles; t += stride) {
-        const int r = tiles[t + 1].x;
-        if (r >= nor) continue;
-        if (t > 0 && tiles[t].x == r) continue;  // not the first sub-tile of the run
-        // carries and y[r] were written by other CTAs: read them through L2
-        AT sum = __ldcg(carries + t);
-        int n = t + 1;
-        while (n < num_tiles && tiles[n + 1].x == r) sum += __ldcg(carries + n++);
-        // sub-tile n starts at (r, tiles[n].y) and completes row r
-        if (tiles[n].y > row_start[r]) {
-            AT v;
-            if (MODE == MODE_POWER) v = (AT)__ldcg(y + r) + scale_pow2(sum, e);
-            else v = (AT)__ldcg(y + r) + sum;
-            y[r] = (XT)v;
-            if (MODE == MODE_POWER) {
-                sumsq = fma((double)v, (double)v, sumsq);
-                if (xdot) *dot = fma((double)xdot[r], (double)v, *dot);
-            }
-        }
-    }
-}
-
 template <typename XT, typename AT>
 struct FixArgs {
     const int32_t* row_start;
@@ -292,7 +257,7 @@ __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
     double sumsq = 0.0, dot = 0.0;
     fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, sumsq, nullptr, &dot,
-                             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+                             blockIdx.x * blockDim.x + threadIdx.x, a.num_tiles, gridDim.x * blockDim.x);
     if (MODE != MODE_POWER) return;
     double t = block_sum<256>(sumsq, red);
     if (threadIdx.x == 0) {
@@ -463,7 +428,8 @@ __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p
                                                    want_dot ? in : nullptr, &dd, pol);
         if (!grid_sync(p.barrier, a.status)) return;
         fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, ss,
-                                       want_dot ? in : nullptr, &dd, blockIdx.x * NT + threadIdx.x, gridDim.x * NT);
+                                       want_dot ? in : nullptr, &dd, blockIdx.x * NT + threadIdx.x, a.nsub,
+                                       gridDim.x * NT);
         const double t_ss = block_sum<NT>(ss, red);
         const double t_dd = block_sum<NT>(dd, red);
         if (threadIdx.x == 0) {

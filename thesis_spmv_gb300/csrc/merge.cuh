@@ -299,6 +299,43 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
 }
 
 // Deterministic block reduction of one double per thread (fixed tree).
+// ---------------------------------------------------------------------------
+// Fix-up: add each sub-tile's carry to the row the sub-tile left unfinished.
+// One thread per sub-tile; the first sub-tile of a run of sub-tiles ending in
+// the same row adds the run in order (deterministic).  The run's row r is
+// completed (and its partial written) by the first sub-tile after the run; the
+// carry is real only if that sub-tile started inside row r.  MODE_POWER also
+// sums the squares (and, with xdot, x[r]*y[r]) of the rows fixed here.
+// Threads take the first sub-tiles t = t0, t0 + stride, ... < t_end (a run
+// starting before t_end may extend past it).
+// ---------------------------------------------------------------------------
+template <int MODE, typename XT, typename AT>
+__device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start, const int2* __restrict__ tiles,
+                                           int nor, int num_tiles, XT* __restrict__ y, const AT* __restrict__ carries,
+                                           int e, double& sumsq, const XT* __restrict__ xdot, double* dot, int t0,
+                                           int t_end, int stride) {
+    for (int t = t0; t < t_end; t += stride) {
+        const int r = tiles[t + 1].x;
+        if (r >= nor) continue;
+        if (t > 0 && tiles[t].x == r) continue;  // not the first sub-tile of the run
+        // carries and y[r] were written by other CTAs: read them through L2
+        AT sum = __ldcg(carries + t);
+        int n = t + 1;
+        while (n < num_tiles && tiles[n + 1].x == r) sum += __ldcg(carries + n++);
+        // sub-tile n starts at (r, tiles[n].y) and completes row r
+        if (tiles[n].y > row_start[r]) {
+            AT v;
+            if (MODE == MODE_POWER) v = (AT)__ldcg(y + r) + scale_pow2(sum, e);
+            else v = (AT)__ldcg(y + r) + sum;
+            y[r] = (XT)v;
+            if (MODE == MODE_POWER) {
+                sumsq = fma((double)v, (double)v, sumsq);
+                if (xdot) *dot = fma((double)xdot[r], (double)v, *dot);
+            }
+        }
+    }
+}
+
 template <int NT>
 __device__ __forceinline__ double block_sum(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

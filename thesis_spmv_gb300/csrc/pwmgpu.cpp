@@ -15,14 +15,16 @@
 #include <vector>
 
 #include "internal.h"
+#include "matrix_impl.h"
 #include "pwmgpu.h"
 
 using namespace pwmgpu;
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
+namespace pwmgpu {
 int fail(int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -32,127 +34,7 @@ int fail(int code, const char* fmt, ...) {
     g_err = buf;
     return code;
 }
-
-#define CU(call)                                                                                  \
-    do {                                                                                          \
-        cudaError_t e_ = (call);                                                                  \
-        if (e_ != cudaSuccess)                                                                    \
-            return fail(e_ == cudaErrorMemoryAllocation ? PWMGPU_ERR_NOMEM : PWMGPU_ERR_CUDA,     \
-                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
-
-#define TRY(expr)                 \
-    do {                          \
-        int r_ = (expr);          \
-        if (r_ != PWMGPU_OK) return r_; \
-    } while (0)
-
-constexpr int kPad = 16;  // kArrayPad in merge.cuh
-
-template <typename T>
-int dalloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
-    if (e != cudaSuccess) {
-        *p = nullptr;
-        return fail(PWMGPU_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
-    }
-    return PWMGPU_OK;
-}
-
-template <typename T>
-void dfree(T*& p) {
-    if (p) cudaFree((void*)p);
-    p = nullptr;
-}
-
-}  // namespace
-
-struct pwmgpu_matrix {
-    int format = PWMGPU_FMT_MERGE;
-    int partitions = 1;
-    int device = 0;
-    int sm_count = 1;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    bool loaded = false;
-
-    DevMatrix M;
-
-    // merge-path plan: sub-tiles of tm merge items (num_tiles of them), the
-    // lane-interleaved arrays, and launch geometry
-    int cfg = kCfgF64;
-    int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
-    // persistent power kernel grids per configuration (0: not launchable)
-    int pgrid = 0, pgrid32 = 0, pgridbf = 0;
-    int power_mode = PWMGPU_POWER_AUTO;
-    MliPlan P;
-    // lane-interleaved FP32 / BF16 copies of the values (lazy)
-    float* val32 = nullptr;
-    void* valbf = nullptr;
-    int bf16_exact = -1;
-
-    // scratch
-    double* carries = nullptr;  // max(num_tiles, num_tiles32) doubles (also used as floats)
-    size_t carries_cap = 0;
-    double* partials = nullptr;  // spmv partials
-    size_t partials_cap = 0;
-    double* fix_partials = nullptr;
-    size_t fix_cap = 0;
-    unsigned int* counter = nullptr;
-    double* nsq = nullptr;
-    size_t nsq_cap = 0;
-    double* small = nullptr;  // 16 doubles of reduction outputs
-    int* status = nullptr;
-    unsigned int* barrier = nullptr;  // grid barrier words of the persistent kernel
-    double* hres = nullptr;           // pinned host copy of a solve chunk's results
-
-    // host-facing vector buffers
-    double* dx = nullptr;
-    double* dy = nullptr;
-    size_t vec_cap = 0;
-    float* fx = nullptr;
-    float* fy = nullptr;
-    size_t fvec_cap = 0;
-
-    void release_matrix() {
-        dfree(M.row_start);
-        dfree(M.col);
-        dfree(M.val);
-        dfree(P.subc);
-        dfree(P.rec);
-        dfree(P.masks);
-        dfree(P.colp);
-        dfree(P.valp);
-        P = MliPlan();
-        dfree(val32);
-        if (valbf) cudaFree(valbf);
-        valbf = nullptr;
-        bf16_exact = -1;
-        M = DevMatrix();
-        num_tiles = 0;
-        loaded = false;
-    }
-    void release_all() {
-        release_matrix();
-        dfree(carries);
-        dfree(partials);
-        dfree(fix_partials);
-        dfree(counter);
-        dfree(nsq);
-        dfree(small);
-        dfree(status);
-        dfree(barrier);
-        if (hres) cudaFreeHost(hres);
-        hres = nullptr;
-        dfree(dx);
-        dfree(dy);
-        dfree(fx);
-        dfree(fy);
-        carries_cap = partials_cap = fix_cap = nsq_cap = vec_cap = fvec_cap = 0;
-    }
-};
+}  // namespace pwmgpu
 
 namespace {
 
@@ -165,6 +47,8 @@ int ensure_cap(double** p, size_t* cap, size_t need) {
     return PWMGPU_OK;
 }
 
+}  // namespace
+namespace pwmgpu {
 int check_status(pwmgpu_matrix* m) {
     int st = 0;
     CU(cudaMemcpyAsync(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
@@ -176,11 +60,15 @@ int check_status(pwmgpu_matrix* m) {
     }
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
 // Build the merge-path plan from the CRS arrays in M: sub-tile boundaries at
 // diagonals s*WM (k_merge_partition), then the lane-interleaved columns and
 // values, row-end masks and metadata (k_mli_plan).  The CRS column / value
 // arrays are released afterwards; row_start stays (fix-up, general path).
+}  // namespace
+namespace pwmgpu {
 int build_plan(pwmgpu_matrix* m) {
     const long long total = (long long)m->M.nor + m->M.nnz;
     const MergeGeom g = merge_geometry(m->cfg);
@@ -218,7 +106,11 @@ int build_plan(pwmgpu_matrix* m) {
     m->loaded = true;
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
+}  // namespace
+namespace pwmgpu {
 int ensure_vectors(pwmgpu_matrix* m) {
     size_t need = (size_t)std::max(m->M.nor, m->M.noc) + kPad;
     if (m->vec_cap >= need) return PWMGPU_OK;
@@ -230,6 +122,8 @@ int ensure_vectors(pwmgpu_matrix* m) {
     m->vec_cap = need;
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
 int ensure_nsq(pwmgpu_matrix* m, size_t need) { return ensure_cap(&m->nsq, &m->nsq_cap, need + 1); }
 
@@ -248,6 +142,8 @@ int alloc_matrix(pwmgpu_matrix* m, int32_t nor, int32_t noc, long long nnz) {
     return PWMGPU_OK;
 }
 
+}  // namespace
+namespace pwmgpu {
 int check_sizes(long long nor, long long noc, long long nnz) {
     if (nor < 0 || noc < 0 || nnz < 0) return fail(PWMGPU_ERR_INVALID, "negative size");
     if (nor + nnz >= (1LL << 31) - 4096)
@@ -255,6 +151,8 @@ int check_sizes(long long nor, long long noc, long long nnz) {
     if (noc >= (1LL << 31)) return fail(PWMGPU_ERR_INVALID, "noc too large");
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->num_tiles == 0) return PWMGPU_OK;
@@ -305,6 +203,8 @@ int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
 
 // Lane-interleaved FP32 or (when every value is exactly a BF16 number, as the
 // Poisson 4 / -1 stencil is) BF16 copy of the values, made on first use.
+}  // namespace
+namespace pwmgpu {
 int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** valp, int* pgrid) {
     const long long elems = mli_storage_elems(m->M.nnz, m->P.nsub);
     if (allow_bf16) {
@@ -339,7 +239,11 @@ int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** 
     *pgrid = m->pgrid32;
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
+}  // namespace
+namespace pwmgpu {
 int ensure_fvectors(pwmgpu_matrix* m) {
     size_t need = (size_t)std::max(m->M.nor, m->M.noc) + kPad;
     if (m->fvec_cap >= need) return PWMGPU_OK;
@@ -351,6 +255,8 @@ int ensure_fvectors(pwmgpu_matrix* m) {
     m->fvec_cap = need;
     return PWMGPU_OK;
 }
+}  // namespace pwmgpu
+namespace {
 
 // One chunk of the persistent power kernel (iterations k0 .. k0+nk-1 of the
 // current phase, k0 + nk >= 2) with the Rayleigh quotient and eigen-residual
@@ -373,7 +279,8 @@ int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X,
 }
 
 // Length of the next chunk: the iterations the residual's observed rate
-// needs to reach `target`, within [8, 512].
+// needs to reach `target`, within [8, 512].  Before the first chunk the
+// residual is taken as 1 (a generic start vector).
 int next_chunk(double rel, double prev_rel, int nk, double target) {
     if (std::isfinite(prev_rel) && rel < prev_rel && rel > 0.0 && target > 0.0) {
         const double rate = std::log(rel / prev_rel) / nk;  // < 0
@@ -408,7 +315,7 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
         TRY(ensure_fvectors(m));
         CU(launch_convert_f64_f32(m->dx, m->fx, N, m->sm_count, m->stream));
         int kl = 0, chunk = 16, nchunks = 0;
-        double prev = INFINITY;
+        double prev = 1.0;
         const double target = precision == PWMGPU_PREC_F32 ? tol : std::max(tol, kSwitchRel);
         while (true) {
             int nk = std::min(chunk, budget - k);
@@ -424,7 +331,7 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
             }
             if (k >= budget) break;
             // FP32 has stopped converging: refine in FP64 from here
-            if (precision == PWMGPU_PREC_MIXED && nchunks >= 3 && o.rel >= 0.7 * prev) break;
+            if (precision == PWMGPU_PREC_MIXED && nchunks >= 2 && o.rel >= 0.7 * prev) break;
             chunk = next_chunk(o.rel, prev, nk, target);
             prev = o.rel;
         }
@@ -442,7 +349,7 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
     if (precision != PWMGPU_PREC_F32) {
         if (m->pgrid == 0) return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
         int kl = 0, chunk = precision == PWMGPU_PREC_MIXED ? 8 : 16;
-        double prev = INFINITY;
+        double prev = precision == PWMGPU_PREC_MIXED ? o.rel : 1.0;
         while (true) {
             int nk = std::min(chunk, max_it - k);
             if (kl + nk < 2) nk = 2 - kl;

@@ -1,0 +1,599 @@
+// service.cpp -- the batched power-method service (include/pwmsvc.h).
+//
+// Host side of the serving loop: a FIFO queue, admission against live-slot
+// and HBM budgets, per-solve phase control (FP32 / BF16 bulk, FP64
+// refinement), the per-class device tables the batched kernels read
+// (batch.h), and one round per pwmsvc_step: the three class branches
+// (FP64, FP32, BF16) run as parallel streams inside one captured CUDA graph.
+// Matrices are built (generated or uploaded, then planned) on each request's
+// own stream, so admissions overlap the previous round on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "batch.h"
+#include "internal.h"
+#include "matrix_impl.h"
+#include "pwmsvc.h"
+
+using namespace pwmgpu;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+enum { kClsF64 = 0, kClsF32 = 1, kClsBF16 = 2, kNumCls = 3 };
+
+// Residual at which a mixed solve leaves the FP32 / BF16 phase (as in
+// pwmgpu_solve).
+constexpr double kSvcSwitchRel = 2e-6;
+
+struct Req {
+    int64_t id = 0;
+    pwmsvc_request spec{};
+    std::vector<int32_t> rs, ci;
+    std::vector<double> vals, x0;
+    int state = PWMSVC_QUEUED;
+    int error = PWMGPU_OK;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    pwmgpu_matrix* m = nullptr;
+    size_t est = 0, bytes = 0;
+    int n = 0;
+    int cls = kClsF64;
+    bool low = false;
+    int slot = -1;
+    const void* valp_low = nullptr;
+    int iterations = 0, iterations_low = 0, rounds_in_phase = 0, converged = 0;
+    double prev_rel = 1.0, rel = INFINITY, lambda = 0.0;
+    std::vector<double> u;
+};
+
+struct ClassDev {
+    BatchTable* dT = nullptr;
+    BatchSlot* d_slots = nullptr;
+    size_t slots_cap = 0;
+    double* tile_part = nullptr;
+    size_t tile_cap = 0;
+    double* red_part = nullptr;
+    size_t red_cap = 0;
+    double* res_part = nullptr;
+    size_t res_cap = 0;
+};
+
+int grow(double** p, size_t* cap, size_t need) {
+    if (*cap >= need && *p) return PWMGPU_OK;
+    size_t c = std::max(need, *cap * 2);
+    dfree(*p);
+    *cap = 0;
+    TRY(dalloc(p, c));
+    *cap = c;
+    return PWMGPU_OK;
+}
+
+// Device bytes of a solve: CRS row starts, the lane-interleaved plan (columns,
+// FP64 values, records, masks, coordinates, carries), the CRS arrays while
+// the plan is built, FP64 vectors, and FP32 values + vectors for a
+// low-precision phase.
+size_t solve_bytes(long long nor, long long nnz, int precision) {
+    const long long nsub = (nor + nnz + 32 * kMliIpt - 1) / (32 * kMliIpt);
+    const long long elems = nnz + 7 * nsub + 16;
+    long long b = 4 * (nor + 1) + 12 * elems + nsub * (32 + 64 + 8 + 8) + 12 * nnz + 2 * 8 * (nor + 16) + 65536;
+    if (precision != PWMGPU_PREC_F64) b += 4 * elems + 2 * 4 * (nor + 16);
+    return (size_t)b;
+}
+
+}  // namespace
+
+struct pwmsvc {
+    pwmsvc_config cfg{};
+    int device = 0, sm_count = 1;
+    cudaStream_t stream = nullptr;
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr}, ev0 = nullptr, ev1 = nullptr;
+    Clock::time_point t0;
+    int64_t next_id = 1;
+    std::deque<Req*> queue;
+    std::vector<Req*> live;
+    std::map<int64_t, std::unique_ptr<Req>> all;
+    size_t in_use = 0;
+    SlotState* d_states = nullptr;
+    SlotState* h_states = nullptr;
+    std::vector<int> free_states;
+    int* d_status = nullptr;
+    ClassDev cls[kNumCls];
+    bool dirty = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int64_t submitted = 0, finished = 0, failed = 0, rounds = 0;
+    double gpu_ms = 0.0;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    void release() {
+        for (auto& kv : all)
+            if (kv.second->m) pwmgpu_destroy(kv.second->m);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto& c : cls) {
+            dfree(c.dT);
+            dfree(c.d_slots);
+            dfree(c.tile_part);
+            dfree(c.red_part);
+            dfree(c.res_part);
+        }
+        dfree(d_states);
+        dfree(d_status);
+        if (h_states) cudaFreeHost(h_states);
+        for (cudaEvent_t e : {fork_ev, join_ev[0], join_ev[1], ev0, ev1})
+            if (e) cudaEventDestroy(e);
+        for (cudaStream_t s : {stream, side[0], side[1]})
+            if (s) cudaStreamDestroy(s);
+    }
+};
+
+namespace {
+
+// Build the request's matrix and start vector on its own stream.
+int admit(pwmsvc* S, Req* r) {
+    const pwmsvc_request& q = r->spec;
+    TRY(pwmgpu_create(PWMGPU_FMT_MERGE, 1, &r->m));
+    pwmgpu_matrix* m = r->m;
+    if (q.source == PWMSVC_SRC_POISSON) {
+        TRY(pwmgpu_generate_poisson(m, q.grid_m, q.grid_n));
+    } else if (q.source == PWMSVC_SRC_RANDOM) {
+        TRY(pwmgpu_generate_random(m, q.n, q.seed, q.length_dist, q.mean_len, q.sigma, q.max_len, q.band_permille,
+                                   q.band_half));
+    } else {
+        TRY(pwmgpu_load_csr(m, q.nor, q.nor, q.nnz, r->rs.data(), r->ci.data(), r->vals.data()));
+        r->rs.clear();
+        r->rs.shrink_to_fit();
+        r->ci.clear();
+        r->ci.shrink_to_fit();
+        r->vals.clear();
+        r->vals.shrink_to_fit();
+    }
+    r->n = m->M.nor;
+    if (r->n == 0) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    TRY(ensure_vectors(m));
+    if (!r->x0.empty()) {
+        CU(cudaMemcpyAsync(m->dx, r->x0.data(), sizeof(double) * (size_t)r->n, cudaMemcpyHostToDevice, m->stream));
+    } else {
+        CU(launch_fill_uniform(m->dx, r->n, q.x0_seed, m->sm_count, m->stream));
+    }
+    r->low = q.precision != PWMGPU_PREC_F64;
+    r->cls = kClsF64;
+    if (r->low) {
+        int cfg = kCfgF32, pg = 0;
+        TRY(ensure_low_values(m, q.precision == PWMGPU_PREC_MIXED, &cfg, &r->valp_low, &pg));
+        TRY(ensure_fvectors(m));
+        CU(launch_convert_f64_f32(m->dx, m->fx, r->n, m->sm_count, m->stream));
+        r->cls = cfg == kCfgBF16 ? kClsBF16 : kClsF32;
+    }
+    CU(cudaStreamSynchronize(m->stream));
+    r->bytes = solve_bytes(m->M.nor, m->M.nnz, q.precision);
+    return PWMGPU_OK;
+}
+
+int reset_state(pwmsvc* S, int slot) {
+    CU(cudaMemsetAsync(S->d_states + slot, 0, sizeof(SlotState), S->stream));
+    return PWMGPU_OK;
+}
+
+int rebuild_tables(pwmsvc* S) {
+    for (int c = 0; c < kNumCls; ++c) {
+        ClassDev& D = S->cls[c];
+        std::vector<BatchSlot> hs;
+        int tiles = 0, red = 0, res = 0;
+        for (Req* r : S->live) {
+            if (r->cls != c) continue;
+            pwmgpu_matrix* m = r->m;
+            BatchSlot b{};
+            b.row_start = m->M.row_start;
+            b.colp = m->P.colp;
+            b.valp = r->low ? r->valp_low : (const void*)m->P.valp;
+            b.rec = m->P.rec;
+            b.masks = m->P.masks;
+            b.subc = m->P.subc;
+            b.X = r->low ? (void*)m->fx : (void*)m->dx;
+            b.Y = r->low ? (void*)m->fy : (void*)m->dy;
+            b.carries = m->carries;
+            b.nor = m->M.nor;
+            b.nsub = m->P.nsub;
+            b.tile0 = tiles;
+            b.nred = (b.nsub + kRedTiles - 1) / kRedTiles;
+            b.red0 = red;
+            b.nres = (b.nor + kResRows - 1) / kResRows;
+            b.res0 = res;
+            b.state = r->slot;
+            tiles += b.nsub;
+            red += b.nred;
+            res += b.nres;
+            hs.push_back(b);
+        }
+        if (D.slots_cap < hs.size() || !D.d_slots) {
+            dfree(D.d_slots);
+            D.slots_cap = 0;
+            TRY(dalloc(&D.d_slots, std::max<size_t>(hs.size(), 64)));
+            D.slots_cap = std::max<size_t>(hs.size(), 64);
+        }
+        TRY(grow(&D.tile_part, &D.tile_cap, 2 * (size_t)tiles + 2));
+        TRY(grow(&D.red_part, &D.red_cap, 2 * (size_t)red + 2));
+        TRY(grow(&D.res_part, &D.res_cap, (size_t)res + 1));
+        if (!hs.empty())
+            CU(cudaMemcpyAsync(D.d_slots, hs.data(), hs.size() * sizeof(BatchSlot), cudaMemcpyHostToDevice,
+                               S->stream));
+        BatchTable T{};
+        T.nslots = (int)hs.size();
+        T.ntiles = tiles;
+        T.nred = red;
+        T.nres = res;
+        T.slots = D.d_slots;
+        T.states = S->d_states;
+        T.tile_part = D.tile_part;
+        T.red_part = D.red_part;
+        T.res_part = D.res_part;
+        T.status = S->d_status;
+        // pageable source: the copy is staged before the call returns
+        CU(cudaMemcpyAsync(D.dT, &T, sizeof T, cudaMemcpyHostToDevice, S->stream));
+        CU(cudaStreamSynchronize(S->stream));
+    }
+    S->dirty = false;
+    return PWMGPU_OK;
+}
+
+// The round: three class branches forked from S->stream.
+int enqueue_round(pwmsvc* S) {
+    const int C = S->cfg.round_iterations;
+    CU(cudaEventRecord(S->fork_ev, S->stream));
+    CU(cudaStreamWaitEvent(S->side[0], S->fork_ev, 0));
+    CU(cudaStreamWaitEvent(S->side[1], S->fork_ev, 0));
+    CU(launch_batch_round(kCfgF64, S->cls[kClsF64].dT, C, S->sm_count, S->stream));
+    CU(launch_batch_round(kCfgF32, S->cls[kClsF32].dT, C, S->sm_count, S->side[0]));
+    CU(launch_batch_round(kCfgBF16, S->cls[kClsBF16].dT, C, S->sm_count, S->side[1]));
+    CU(cudaEventRecord(S->join_ev[0], S->side[0]));
+    CU(cudaEventRecord(S->join_ev[1], S->side[1]));
+    CU(cudaStreamWaitEvent(S->stream, S->join_ev[0], 0));
+    CU(cudaStreamWaitEvent(S->stream, S->join_ev[1], 0));
+    return PWMGPU_OK;
+}
+
+int run_round(pwmsvc* S) {
+    if (S->cfg.use_graph && !S->gexec) {
+        CU(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_round(S);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(S->stream, &g);
+        if (rc != PWMGPU_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "round capture: %s", cudaGetErrorString(e));
+        S->graph = g;
+        CU(cudaGraphInstantiate(&S->gexec, S->graph, 0));
+    }
+    CU(cudaEventRecord(S->ev0, S->stream));
+    if (S->gexec) {
+        CU(cudaGraphLaunch(S->gexec, S->stream));
+    } else {
+        TRY(enqueue_round(S));
+    }
+    CU(cudaEventRecord(S->ev1, S->stream));
+    return PWMGPU_OK;
+}
+
+// Normalised u = v_{k-1} / ||v_{k-1}|| (the vector lambda and the residual
+// belong to) into the request's host copy, then free the device memory.
+int retire(pwmsvc* S, Req* r, int state) {
+    pwmgpu_matrix* m = r->m;
+    if (state == PWMSVC_DONE && r->spec.keep_vector) {
+        const SlotState& st = S->h_states[r->slot];
+        const int k = st.k;
+        double* prev64;
+        if (r->low) {
+            float* prev = (k & 1) ? m->fx : m->fy;
+            CU(launch_convert_f32_f64(prev, m->dx, r->n, m->sm_count, S->stream));
+            prev64 = m->dx;
+        } else {
+            prev64 = (k & 1) ? m->dx : m->dy;
+        }
+        CU(launch_power_finalize_f64(prev64, &S->d_states[r->slot].nsq_prev, nullptr, nullptr, r->n, m->sm_count,
+                                     S->stream));
+        r->u.resize((size_t)r->n);
+        CU(cudaMemcpyAsync(r->u.data(), prev64, sizeof(double) * (size_t)r->n, cudaMemcpyDeviceToHost, S->stream));
+        CU(cudaStreamSynchronize(S->stream));
+    }
+    pwmgpu_destroy(m);
+    r->m = nullptr;
+    S->in_use -= std::min(S->in_use, r->bytes);
+    if (r->slot >= 0) S->free_states.push_back(r->slot);
+    r->slot = -1;
+    r->state = state;
+    r->t_done = S->now();
+    if (state == PWMSVC_DONE) ++S->finished;
+    else ++S->failed;
+    S->dirty = true;
+    return PWMGPU_OK;
+}
+
+// Per-solve decisions after a round (the stopping and phase rules of
+// pwmgpu_solve, at round granularity).
+int after_round(pwmsvc* S, int* finished) {
+    const int C = S->cfg.round_iterations;
+    std::vector<Req*> keep;
+    for (Req* r : S->live) {
+        const SlotState& st = S->h_states[r->slot];
+        const pwmsvc_request& q = r->spec;
+        r->iterations += C;
+        if (r->low) r->iterations_low += C;
+        ++r->rounds_in_phase;
+        const double nsq = st.nsq_prev;
+        const bool finite = std::isfinite(st.lambda) && std::isfinite(st.res2) && nsq > 0.0 && std::isfinite(nsq);
+        if (!finite || st.lambda == 0.0) {
+            r->error = PWMGPU_ERR_NUMERIC;
+            TRY(retire(S, r, PWMSVC_FAILED));
+            ++*finished;
+            continue;
+        }
+        r->lambda = st.lambda;
+        r->rel = std::sqrt(st.res2 / nsq) / std::fabs(st.lambda);
+        bool done = false;
+        if (!r->low || q.precision == PWMGPU_PREC_F32) {
+            if (r->rel <= q.tol) {
+                r->converged = 1;
+                done = true;
+            } else if (r->iterations >= q.max_it) {
+                done = true;
+            }
+        } else {
+            // mixed: leave the low-precision phase at the switch residual, when
+            // it stops falling, or when only the FP64 reserve is left
+            const int reserve = std::max(2, std::min(64, q.max_it / 4));
+            const bool stalled = r->rounds_in_phase >= 2 && r->rel >= 0.7 * r->prev_rel;
+            if (r->rel <= std::max(q.tol, kSvcSwitchRel) || stalled || r->iterations >= q.max_it - reserve) {
+                pwmgpu_matrix* m = r->m;
+                float* newest = (st.k & 1) ? m->fy : m->fx;
+                CU(launch_convert_f32_f64(newest, m->dx, r->n, m->sm_count, S->stream));
+                TRY(reset_state(S, r->slot));
+                r->low = false;
+                r->cls = kClsF64;
+                r->rounds_in_phase = 0;
+                S->dirty = true;
+            }
+        }
+        r->prev_rel = r->rel;
+        if (done) {
+            TRY(retire(S, r, PWMSVC_DONE));
+            ++*finished;
+        } else {
+            keep.push_back(r);
+        }
+    }
+    S->live.swap(keep);
+    return PWMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pwmsvc_create(const pwmsvc_config* cfg, pwmsvc** out) {
+    if (!out) return fail(PWMGPU_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    pwmsvc_config c = cfg ? *cfg : pwmsvc_config{};
+    if (c.max_live <= 0) c.max_live = 1024;
+    if (c.round_iterations == 0) c.round_iterations = 8;
+    if (c.round_iterations < 2) return fail(PWMGPU_ERR_INVALID, "round_iterations must be >= 2");
+    std::unique_ptr<pwmsvc> S(new pwmsvc());
+    S->cfg = c;
+    S->t0 = Clock::now();
+    int rc = PWMGPU_OK;
+    do {
+        cudaError_t e = cudaGetDevice(&S->device);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&S->sm_count, cudaDevAttrMultiProcessorCount, S->device);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->side[0], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->side[1], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->fork_ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->join_ev[0], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->join_ev[1], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&S->ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&S->ev1);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "pwmsvc_create: %s", cudaGetErrorString(e)); break; }
+        if (S->cfg.hbm_budget_bytes == 0) {
+            size_t f = 0, t = 0;
+            e = cudaMemGetInfo(&f, &t);
+            if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "cudaMemGetInfo: %s", cudaGetErrorString(e)); break; }
+            S->cfg.hbm_budget_bytes = (size_t)(0.9 * (double)f);
+        }
+        if ((rc = dalloc(&S->d_states, (size_t)c.max_live)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&S->d_status, 4)) != PWMGPU_OK) break;
+        e = cudaMallocHost((void**)&S->h_states, sizeof(SlotState) * (size_t)c.max_live);
+        if (e != cudaSuccess) { S->h_states = nullptr; rc = fail(PWMGPU_ERR_NOMEM, "cudaMallocHost failed"); break; }
+        for (auto& D : S->cls)
+            if ((rc = dalloc(&D.dT, 1)) != PWMGPU_OK) break;
+        if (rc != PWMGPU_OK) break;
+        for (int i = c.max_live - 1; i >= 0; --i) S->free_states.push_back(i);
+        e = cudaMemsetAsync(S->d_states, 0, sizeof(SlotState) * (size_t)c.max_live, S->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(S->d_status, 0, 4 * sizeof(int), S->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "pwmsvc_create: %s", cudaGetErrorString(e)); break; }
+        batch_prepare(S->sm_count);
+        if ((rc = rebuild_tables(S.get())) != PWMGPU_OK) break;
+    } while (0);
+    if (rc != PWMGPU_OK) {
+        S->release();
+        return rc;
+    }
+    *out = S.release();
+    return PWMGPU_OK;
+}
+
+int pwmsvc_destroy(pwmsvc* s) {
+    if (!s) return PWMGPU_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->release();
+    delete s;
+    return PWMGPU_OK;
+}
+
+int pwmsvc_submit(pwmsvc* s, const pwmsvc_request* q, int64_t* id) {
+    if (!s || !q) return fail(PWMGPU_ERR_INVALID, "null service or request");
+    if (q->max_it < 2) return fail(PWMGPU_ERR_INVALID, "max_it must be at least 2");
+    if (!(q->tol >= 0.0)) return fail(PWMGPU_ERR_INVALID, "tol must be >= 0");
+    if (q->precision != PWMGPU_PREC_F64 && q->precision != PWMGPU_PREC_F32 && q->precision != PWMGPU_PREC_MIXED)
+        return fail(PWMGPU_ERR_INVALID, "unknown precision %d", q->precision);
+    std::unique_ptr<Req> r(new Req());
+    r->spec = *q;
+    long long nor = 0, nnz = 0;
+    switch (q->source) {
+        case PWMSVC_SRC_CSR:
+            if (q->nor < 1 || q->nnz < 0 || !q->row_start || (q->nnz > 0 && (!q->col_ind || !q->vals)))
+                return fail(PWMGPU_ERR_INVALID, "bad CSR request");
+            nor = q->nor;
+            nnz = q->nnz;
+            r->rs.assign(q->row_start, q->row_start + nor + 1);
+            r->ci.assign(q->col_ind, q->col_ind + nnz);
+            r->vals.assign(q->vals, q->vals + nnz);
+            break;
+        case PWMSVC_SRC_POISSON:
+            if (q->grid_m < 1 || q->grid_n < 1) return fail(PWMGPU_ERR_INVALID, "bad Poisson grid");
+            nor = (long long)q->grid_m * q->grid_n;
+            nnz = (long long)q->grid_n * (q->grid_m + 2LL * (q->grid_m - 1)) + 2LL * (q->grid_n - 1) * q->grid_m;
+            break;
+        case PWMSVC_SRC_RANDOM:
+            if (q->n < 1 || !(q->mean_len > 0.0)) return fail(PWMGPU_ERR_INVALID, "bad random-matrix request");
+            nor = q->n;
+            nnz = (long long)std::ceil(q->n * std::min((double)q->n, q->mean_len) * 1.1) + 64;
+            break;
+        default:
+            return fail(PWMGPU_ERR_INVALID, "unknown source %d", q->source);
+    }
+    r->spec.row_start = nullptr;
+    r->spec.col_ind = nullptr;
+    r->spec.vals = nullptr;
+    if (q->x0) r->x0.assign(q->x0, q->x0 + nor);
+    r->spec.x0 = nullptr;
+    r->n = (int)nor;
+    r->est = solve_bytes(nor, nnz, q->precision);
+    if (r->est > s->cfg.hbm_budget_bytes)
+        return fail(PWMGPU_ERR_BUDGET, "request needs about %zu bytes, more than the service's HBM budget (%zu)",
+                    r->est, s->cfg.hbm_budget_bytes);
+    r->id = s->next_id++;
+    r->t_submit = s->now();
+    if (id) *id = r->id;
+    s->queue.push_back(r.get());
+    s->all[r->id] = std::move(r);
+    ++s->submitted;
+    return PWMGPU_OK;
+}
+
+int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
+    if (!s) return fail(PWMGPU_ERR_INVALID, "null service");
+    int fin = 0;
+    // admission: FIFO while slots and the HBM budget allow
+    while (!s->queue.empty() && (int)s->live.size() < s->cfg.max_live && !s->free_states.empty()) {
+        Req* r = s->queue.front();
+        if (!s->live.empty() && s->in_use + r->est > s->cfg.hbm_budget_bytes) break;
+        s->queue.pop_front();
+        r->t_admit = s->now();
+        r->slot = s->free_states.back();
+        s->free_states.pop_back();
+        int rc = admit(s, r);
+        if (rc == PWMGPU_OK) rc = reset_state(s, r->slot);
+        if (rc != PWMGPU_OK) {
+            r->error = rc;
+            if (r->m) pwmgpu_destroy(r->m);
+            r->m = nullptr;
+            s->free_states.push_back(r->slot);
+            r->slot = -1;
+            r->state = PWMSVC_FAILED;
+            r->t_done = s->now();
+            ++s->failed;
+            ++fin;
+            continue;
+        }
+        r->state = PWMSVC_RUNNING;
+        s->in_use += r->bytes;
+        s->live.push_back(r);
+        s->dirty = true;
+    }
+    if (!s->live.empty()) {
+        if (s->dirty) TRY(rebuild_tables(s));
+        TRY(run_round(s));
+        CU(cudaMemcpyAsync(s->h_states, s->d_states, sizeof(SlotState) * (size_t)s->cfg.max_live,
+                           cudaMemcpyDeviceToHost, s->stream));
+        int status = 0;
+        CU(cudaMemcpyAsync(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        CU(cudaStreamSynchronize(s->stream));
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->gpu_ms += ms;
+        ++s->rounds;
+        if (status != PWMGPU_OK) return fail(status, "a bounded device wait timed out in a service round");
+        TRY(after_round(s, &fin));
+    }
+    if (live) *live = (int32_t)s->live.size();
+    if (queued) *queued = (int32_t)s->queue.size();
+    if (finished) *finished = fin;
+    return PWMGPU_OK;
+}
+
+int pwmsvc_result(pwmsvc* s, int64_t id, pwmsvc_result_info* out, double* u) {
+    if (!s || !out) return fail(PWMGPU_ERR_INVALID, "null service or output");
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return fail(PWMGPU_ERR_INVALID, "unknown request %lld", (long long)id);
+    const Req* r = it->second.get();
+    std::memset(out, 0, sizeof *out);
+    out->state = r->state;
+    out->n = r->n;
+    out->iterations = r->iterations;
+    out->iterations_low = r->iterations_low;
+    out->converged = r->converged;
+    out->precision = r->spec.precision;
+    out->error = r->error;
+    out->lambda = r->lambda;
+    out->residual = r->rel;
+    out->t_submit = r->t_submit;
+    out->t_admit = r->t_admit;
+    out->t_done = r->t_done;
+    if (u) {
+        if (r->state != PWMSVC_DONE || r->u.empty())
+            return fail(PWMGPU_ERR_STATE, "request %lld has no eigenvector (not finished or keep_vector = 0)",
+                        (long long)id);
+        std::memcpy(u, r->u.data(), sizeof(double) * r->u.size());
+    }
+    return PWMGPU_OK;
+}
+
+int pwmsvc_release(pwmsvc* s, int64_t id) {
+    if (!s) return fail(PWMGPU_ERR_INVALID, "null service");
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return fail(PWMGPU_ERR_INVALID, "unknown request %lld", (long long)id);
+    if (it->second->state != PWMSVC_DONE && it->second->state != PWMSVC_FAILED)
+        return fail(PWMGPU_ERR_STATE, "request %lld is still queued or running", (long long)id);
+    s->all.erase(it);
+    return PWMGPU_OK;
+}
+
+int pwmsvc_stats(pwmsvc* s, pwmsvc_stats_info* out) {
+    if (!s || !out) return fail(PWMGPU_ERR_INVALID, "null service or output");
+    std::memset(out, 0, sizeof *out);
+    out->submitted = s->submitted;
+    out->finished = s->finished;
+    out->failed = s->failed;
+    out->rounds = s->rounds;
+    out->live = (int32_t)s->live.size();
+    out->queued = (int32_t)s->queue.size();
+    out->hbm_in_use = s->in_use;
+    out->hbm_budget = s->cfg.hbm_budget_bytes;
+    out->gpu_round_ms = s->gpu_ms;
+    return PWMGPU_OK;
+}
+
+}  // extern "C"
