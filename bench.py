@@ -17,6 +17,7 @@ oracle, OpenMP over all host cores) on the same workload.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -244,12 +245,192 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
     return out
 
 
+def _batch_specs(rng, count=128):
+    """The 256-matrix batch: 128 Poisson grids with side uniform in
+    [32, 1024] and 128 random matrices with N log-uniform in [1e3, 1e6],
+    Poisson(8) row lengths, uniform columns, values in (0, 1]."""
+    specs = []
+    for i in range(count):
+        side = int(rng.integers(32, 1025))
+        specs.append(("poisson", dict(m=side, n=side)))
+    for i in range(count):
+        n = int(round(10 ** rng.uniform(3, 6)))
+        specs.append(("random", dict(n=n, seed=1000 + i, length_dist=1, mean_len=8.0, sigma=0.0, max_len=64,
+                                     band_permille=0, band_half=0)))
+    return specs
+
+
+def _stream_specs(rng, count):
+    """Serving stream requests: N log-uniform in [1e4, 4e6]; half Poisson
+    grids (side = round(sqrt(N))), half lognormal-row random matrices."""
+    specs = []
+    for i in range(count):
+        n = int(round(10 ** rng.uniform(4, math.log10(4e6))))
+        if i % 2 == 0:
+            side = max(2, int(round(math.sqrt(n))))
+            specs.append(("poisson", dict(m=side, n=side)))
+        else:
+            specs.append(("random", dict(n=n, seed=5000 + i, length_dist=0, mean_len=16.0, sigma=1.2,
+                                         max_len=20000, band_permille=300, band_half=4096)))
+    return specs
+
+
+def _submit(svc, kind, kw, precision, max_it, tol):
+    if kind == "poisson":
+        return svc.submit_poisson(kw["m"], kw["n"], max_it=max_it, tol=tol, precision=precision, x0_seed=11)
+    return svc.submit_random(max_it=max_it, tol=tol, precision=precision, x0_seed=11, **kw)
+
+
+def seeded_uniform(n, seed):
+    """The service's seeded start vector (x0_seed): x[i] = (mix(seed +
+    g (i + 1)) >> 11) 2^-53 with the splitmix64 finaliser, in numpy."""
+    z = np.uint64(seed) + np.uint64(0x9e3779b97f4a7c15) * np.arange(1, n + 1, dtype=np.uint64)
+    z ^= z >> np.uint64(30)
+    z *= np.uint64(0xbf58476d1ce4e5b9)
+    z ^= z >> np.uint64(27)
+    z *= np.uint64(0x94d049bb133111eb)
+    z ^= z >> np.uint64(31)
+    return (z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def _one_at_a_time(pwm, kind, kw, max_it, tol):
+    M = pwm.CRSCuda(1)
+    if kind == "poisson":
+        M.generatePoissonMatrix(kw["m"], kw["n"], 1)
+    else:
+        M.generateRandom(**kw)
+    x = seeded_uniform(M.dims()[0], 11)  # the service's start vector for x0_seed = 11
+    return M.solve(x, max_it, tol, pwm.PREC_F64)
+
+
+def _stream_run(submit_fn, arrivals, step_fn, idle_fn):
+    """Drive arrivals on the wall clock; returns per-request latency (s)."""
+    t0 = time.perf_counter()
+    i = 0
+    while True:
+        now = time.perf_counter() - t0
+        while i < len(arrivals) and arrivals[i] <= now:
+            submit_fn(i, t0)
+            i += 1
+        busy = step_fn()
+        if not busy:
+            if i >= len(arrivals):
+                break
+            wait = arrivals[i] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(min(wait, 0.01))
+    return idle_fn(t0)
+
+
+def serving(pwm, args):
+    """Batch (256 uneven matrices) and serving-stream workloads: the batched
+    service in mixed precision and in FP64 (one launch per power step for all
+    live solves, graph-captured rounds) against the plain FP64 merge-path
+    path solving one request at a time (pwmgpu_solve per matrix)."""
+    from thesis_spmv_gb300 import service as S
+    tol, max_it = 1e-10, 2000
+    out = {}
+
+    # ---- the 256-matrix batch, all submitted at once ----
+    specs = _batch_specs(np.random.default_rng(20261203), args.batch_count)
+    batch = {}
+    arms = (("service_mixed", pwm.PREC_MIXED), ("service_fp64", pwm.PREC_F64))
+    if args.batch_only:
+        arms = (("service_fp64", pwm.PREC_F64),)
+    for name, prec in arms:
+        svc = S.Service(hbm_budget_bytes=150 << 30, round_iterations=8)
+        t0 = time.perf_counter()
+        ids = [_submit(svc, k, kw, prec, max_it, tol) for k, kw in specs]
+        svc.run_until_idle()
+        el = time.perf_counter() - t0
+        res = [svc.result(i) for i in ids]
+        batch[name] = {"seconds": round(el, 3), "solves_per_s": round(len(ids) / el, 2),
+                       "converged": int(sum(r.converged for r in res)),
+                       "steps_total": int(sum(r.iterations for r in res)),
+                       "steps_low_precision": int(sum(r.iterations_low for r in res)),
+                       "rounds": int(svc.stats().rounds), "gpu_round_ms": round(svc.stats().gpu_round_ms, 1)}
+        if name == "service_mixed":
+            lam_mixed = [r.lambda_ for r in res]
+        else:
+            lam64 = [r.lambda_ for r in res]
+        svc.close()
+    if args.batch_only:
+        return {"batch_256": batch}
+    t0 = time.perf_counter()
+    one = [_one_at_a_time(pwm, k, kw, max_it, tol) for k, kw in specs]
+    el = time.perf_counter() - t0
+    batch["one_at_a_time_fp64"] = {"seconds": round(el, 3), "solves_per_s": round(len(specs) / el, 2),
+                                   "converged": int(sum(r.converged for r in one)),
+                                   "steps_total": int(sum(r.iterations for r in one))}
+    diffs = [abs(a - b) / abs(b) for a, b in zip(lam_mixed, lam64)]
+    batch["lambda_rel_diff_mixed_vs_fp64"] = {"max": max(diffs), "median": float(np.median(diffs))}
+    batch["speedup_service_mixed_vs_one_at_a_time_fp64"] = round(
+        batch["service_mixed"]["solves_per_s"] / batch["one_at_a_time_fp64"]["solves_per_s"], 3)
+    out["batch_256"] = dict(workload="128 Poisson grids (side U[32,1024]) + 128 random (N log-uniform [1e3,1e6], "
+                                     "Poisson(8) rows); tol 1e-10 or 2000 steps", **batch)
+
+    # ---- serving stream: Poisson arrivals at a few rates ----
+    stream = {}
+    R = args.stream_requests
+    specs = _stream_specs(np.random.default_rng(7), R)
+    for rate in args.stream_rates:
+        arr = np.cumsum(np.random.default_rng(int(rate)).exponential(1.0 / rate, R))
+        arr -= arr[0]
+        row = {}
+        for name, prec in (("service_mixed", pwm.PREC_MIXED), ("service_fp64", pwm.PREC_F64)):
+            svc = S.Service(hbm_budget_bytes=150 << 30, round_iterations=8)
+            t_create = time.perf_counter()
+            ids = {}
+
+            def submit_fn(i, t0, svc=svc, ids=ids, prec=prec):
+                k, kw = specs[i]
+                ids[i] = _submit(svc, k, kw, prec, max_it, tol)
+
+            def step_fn(svc=svc):
+                live, queued, _ = svc.step()
+                return live > 0 or queued > 0
+
+            def idle_fn(t0, svc=svc, ids=ids, arr=arr, t_create=t_create):
+                lat = []
+                for i, rid in ids.items():
+                    r = svc.result(rid)
+                    lat.append(r.t_done + (t_create - t0) - arr[i])
+                return np.array(lat)
+
+            lat = _stream_run(submit_fn, arr, step_fn, idle_fn)
+            row[name] = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
+                         "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
+                         "solves_per_s": round(R / max(float(np.max(lat + arr)), 1e-9), 2)}
+            svc.close()
+        # plain FP64 path, one request at a time in arrival order
+        done_t = []
+        t0 = time.perf_counter()
+        for i, (k, kw) in enumerate(specs):
+            now = time.perf_counter() - t0
+            if arr[i] > now:
+                time.sleep(arr[i] - now)
+            _one_at_a_time(pwm, k, kw, max_it, tol)
+            done_t.append(time.perf_counter() - t0)
+        lat = np.array(done_t) - arr
+        row["one_at_a_time_fp64"] = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
+                                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
+                                     "solves_per_s": round(R / max(done_t[-1], 1e-9), 2)}
+        stream["rate_%g_per_s" % rate] = row
+    out["serving_stream"] = dict(workload="%d requests, N log-uniform [1e4, 4e6], half Poisson grids, half "
+                                          "lognormal-row random; Poisson arrivals; tol 1e-10 or 2000 steps; HBM "
+                                          "budget 150 GB" % R, **stream)
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import thesis_spmv_gb300 as pwm
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
+    if args.batch_only:
+        print(json.dumps(serving(pwm, args)))
+        return
     grid_side = args.grid
     M = pwm.CRSCuda(1)
     M.generatePoissonMatrix(grid_side, grid_side, 1)
@@ -322,6 +503,8 @@ def run_ours(args, world, rank, local):
     e2e_gbs = B * world / e2e_s / 1e9 if e2e_steps else None
 
     extra = None if args.no_extra else irregular_and_solves(pwm, torch, dev, stream, args)
+    if not args.no_serving and rank == 0:
+        extra = dict(extra or {}, **serving(pwm, args))
 
     peak, peak_kind = measured_peaks()
     traffic = profile_traffic().get("k_merge_spmv_f64_poisson4096")
@@ -375,6 +558,13 @@ def main():
     ap.add_argument("--grid", type=int, default=GRID, help="Poisson grid side (default 4096)")
     ap.add_argument("--no-extra", action="store_true", help="skip the irregular matrix and the solves")
     ap.add_argument("--solves", type=int, default=20, help="timed solves per precision")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batch and serving-stream workloads")
+    ap.add_argument("--batch-count", type=int, default=128,
+                    help="Poisson grids and random matrices in the batch (128 each)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the 256-matrix batch through the FP64 service (a profiling case)")
+    ap.add_argument("--stream-requests", type=int, default=48)
+    ap.add_argument("--stream-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -141,8 +141,9 @@ int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
  * (||u|| = 1), the normalised iterate after iterations - 1 SpMVs (the last
  * SpMV computes A u for lambda and the residual).  The residual test runs
  * every chunk of iterations inside the persistent kernel (FP64 reductions);
- * MIXED runs FP32 (BF16 values where exact) until the residual reaches 2e-6
- * or stops falling, then FP64 to tol. */
+ * MIXED runs FP32 (BF16 values where exact) until the residual reaches 2e-6,
+ * stops falling below 1e-4 (the FP32 rounding floor), or only the FP64
+ * reserve of min(64, max_it/4) iterations is left; then FP64 to tol. */
 typedef struct {
     int32_t iterations;     /* total SpMVs performed */
     int32_t iterations_low; /* of which in the FP32/BF16 phase */

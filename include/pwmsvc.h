@@ -11,7 +11,8 @@
  * at the matrix boundaries), followed by a residual pass; with use_graph the
  * round is one CUDA graph.  Each solve keeps its matrix and iterates resident
  * in HBM until it retires.  Mixed precision runs the FP32 (BF16 values where
- * exact) phase until the residual reaches 2e-6 or stops falling, then FP64.
+ * exact) phase as pwmgpu_solve does (to a residual of 2e-6, the FP32 floor,
+ * or the FP64 reserve), then FP64.
  * Sums over a solve's rows run in a fixed order over its own sub-tiles, so a
  * solve gives the same bits alone and in any mix.
  *

@@ -222,3 +222,24 @@ def test_invalid_csr_rejected(pwm):
         M.loadCSR(3, 3, np.array([0, 2, 1, 3]), np.array([0, 1, 1]), np.ones(3))  # decreasing row_start
     with pytest.raises(pwm.PwmGpuError):
         M.mv(np.ones(3), np.zeros(3))  # nothing loaded
+
+
+@pytest.mark.parametrize("scale", [1e150, 1e-150, 1e30])
+@pytest.mark.parametrize("mode", ["fused", "multi"])
+def test_power_extreme_scales(pwm, scale, mode):
+    """Entries of size 1e150 / 1e-150: the iterate's norm leaves the rescale
+    window within an iteration or two, so the exact power-of-two rescale must
+    keep it finite; results equal the oracle's, which normalises every
+    iteration (CRS.hpp:118-130)."""
+    A = _random_csr(3000, 5, 17)
+    A.data = (np.abs(A.data) + 0.01) * scale
+    M = _gpu_matrix(pwm, A)
+    M.set_power_mode(pwm.POWER_FUSED if mode == "fused" else pwm.POWER_MULTI)
+    x0 = np.random.default_rng(3).random(A.nor)
+    for it in (7, 30):
+        xg, yg = x0.copy(), np.zeros(A.nor)
+        M.powerIteration(xg, yg, it)
+        xr, yr = O.power(A, x0, it)
+        assert np.all(np.isfinite(xg)) and np.all(np.isfinite(yg))
+        np.testing.assert_allclose(xg, xr, rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(yg, yr, rtol=1e-10, atol=1e-13)

@@ -13,8 +13,7 @@ Checks: the permutation is a bijection into [base, base + nkw) and vector
 slots are 16-byte aligned; bases never overlap and stay inside the
 allocation; row-end masks, first rows and flags reproduce the CRS structure;
 a step-by-step simulation of the kernel (fast and general paths, carries,
-k_merge_fixup) reproduces the oracle's y = A x within the row bound and
-counts every row's square exactly once (power-method epilogue).
+k_merge_fixup) reproduces the oracle's y = A x within the row bound.
 """
 import numpy as np
 import pytest
@@ -101,12 +100,11 @@ def plan(A, IPT):
 
 def simulate(A, x, IPT):
     """The kernel (fast path unless the sub-tile holds an empty row) and
-    k_merge_fixup; returns y and per-row counts of squares summed."""
+    k_merge_fixup; returns y."""
     sc, valp, colp, masks, meta = plan(A, IPT)
     rs, nor = A.row_start, A.nor
     ns = len(sc) - 1
     y = np.full(nor, np.nan)
-    counted = np.zeros(nor, np.int64)
     carries = np.zeros(ns)
     for s in range(ns):
         (rw0, kw0), (rw1, kw1) = sc[s], sc[s + 1]
@@ -124,8 +122,6 @@ def simulate(A, x, IPT):
         # rows [rw0, fr) carry no nonzeros in this sub-tile
         for r in range(rw0, fr):
             y[r] = 0.0
-            if rs[r] == rs[r + 1]:
-                counted[r] += 1
         # first rows: exclusive prefix of popcounts (fast) or search (general)
         pc = [bin(l[4]).count("1") for l in lanes]
         crow, cval, hval = [], [], [None] * 32
@@ -145,7 +141,6 @@ def simulate(A, x, IPT):
                 a = row_of(rs, b0, rw0, rw1) if cnt else rw1
                 head_open = cnt > 0 and rs[a] < b0
             to_head = head_open and lane > 0
-            count = not head_open
             acc = 0.0
             for j in range(IPT):
                 if j < q:
@@ -156,15 +151,11 @@ def simulate(A, x, IPT):
                             to_head = False
                         else:
                             y[a] = acc
-                            if count:
-                                counted[a] += 1
-                        count = True
                         acc = 0.0
                         a += 1
                         if has_empty:  # general path: pass empty rows
                             while a < rw1 and rs[a + 1] == rs[a]:
                                 y[a] = 0.0
-                                counted[a] += 1
                                 a += 1
             if cnt == 0:
                 a = rw1
@@ -184,8 +175,6 @@ def simulate(A, x, IPT):
                     if rs[a] < b0u:
                         assert hval[u] is not None
                         y[a] = hval[u] + tot
-                        if rs[a] >= kw0:
-                            counted[a] += 1
                     else:
                         assert tot == 0.0
                 elif a < nor:
@@ -201,8 +190,7 @@ def simulate(A, x, IPT):
             n += 1
         if sc[n][1] > rs[r]:
             y[r] = y[r] + tot
-            counted[r] += 1
-    return y, counted
+    return y
 
 
 def _random_csr(n, mean_len, seed, noc=None, empty_frac=0.0, dense_rows=0, dense_len=0):
@@ -265,13 +253,10 @@ def test_layout(IPT, name):
 def test_algorithm_simulation(IPT, name):
     A = MATRICES[name]()
     x = np.random.default_rng(1).uniform(-1, 1, A.noc)
-    y, counted = simulate(A, x, IPT)
+    y = simulate(A, x, IPT)
     ref = O.crs_mv(A, x)
     assert not np.isnan(y).any()
     assert np.all(np.abs(y - ref) <= O.row_error_bound(A, x) + 1e-300)
-    nz = np.diff(A.row_start) > 0
-    assert np.all(counted[nz] == 1), np.nonzero(counted[nz] != 1)[0][:10]
-    assert np.all(counted <= 1)
 
 
 def test_poisson_row_start_closed_form():

@@ -4,14 +4,16 @@
 //
 // Per step, for every slot j of a class table (see batch.h):
 //   k_batch_spmv    v_{k+1} = 2^{e_k} A_j v_k over all slots' sub-tiles
-//                   (merge-path sub-tiles, TMA-staged, the power epilogue of
-//                   the single-matrix kernel) and per-sub-tile partial sums
-//                   of ||v_{k+1}||^2 (and v_k . v_{k+1} on a round's last step)
-//   k_batch_reduce  carries of each slot (fix-up), then per-slot sums over
-//                   its sub-tiles in a fixed order; the slot's last CTA
-//                   advances the slot state (k, ||v||^2)
+//                   (merge-path sub-tiles, TMA-staged; e_k is an exact
+//                   rescale, nonzero only when the norm leaves a wide window)
+//   k_batch_fixup   the carries of each slot's sub-tiles
+//   k_batch_norm    ||v_{k+1}||^2 (and v_k . v_{k+1} on a round's last step)
+//                   per slot, over fixed row chunks in a fixed order; the
+//                   slot's last CTA advances the slot state (k, ||v||^2)
 // and once per round
 //   k_batch_resid   lambda and ||A u - lambda u||^2 of u = v_{k-1}/||v_{k-1}||.
+// The SpMV keeps one FP64 FMA per nonzero and no other FP64 work (GB300's
+// FP64 pipe is 2 operations per clock per SM); the sums are row passes.
 // Grids are fixed (graph-captured rounds); the kernels read the table's
 // sizes from device memory, so one graph serves every composition.
 #include <cuda_bf16.h>
@@ -34,26 +36,55 @@ __device__ __forceinline__ int find_slot(const BatchSlot* __restrict__ slots, in
     int lo = 0, hi = nslots - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        const int key = FIELD == 0 ? __ldg(&slots[mid].tile0) : FIELD == 1 ? __ldg(&slots[mid].red0)
-                                                                            : __ldg(&slots[mid].res0);
+        const int key = FIELD == 0 ? __ldg(&slots[mid].tile0) : FIELD == 1 ? __ldg(&slots[mid].fix0)
+                                                                            : __ldg(&slots[mid].row0);
         if (key <= v) lo = mid;
         else hi = mid - 1;
     }
     return lo;
 }
 
+// What a warp needs of a sub-tile's slot, loaded one sub-tile ahead.
+struct SlotRegs {
+    const int32_t* row_start;
+    const void* X;
+    const void* Y;
+    void* carries;
+    int nor, tile0, k;
+    double nsq;
+};
+
+__device__ __forceinline__ void load_slot(const BatchTable& T, int j, SlotRegs& r) {
+    const BatchSlot* d = T.slots + j;
+    r.row_start = d->row_start;
+    r.X = d->X;
+    r.Y = d->Y;
+    r.carries = d->carries;
+    r.nor = d->nor;
+    r.tile0 = d->tile0;
+    const SlotState* st = T.states + d->state;
+    r.k = st->k;
+    r.nsq = st->nsq;
+}
+
+// Lane 0: the TMA copies of global sub-tile g (slot j, its record r1).
 template <typename VT, int IPT>
-__device__ __forceinline__ void issue_global(unsigned char* st, uint64_t* bar, const BatchSlot* slots, int nslots,
-                                             int g, uint64_t pol) {
-    const int j = find_slot<0>(slots, nslots, g);
-    const BatchSlot& d = slots[j];
-    const int s = g - d.tile0;
-    issue_subtile<VT, IPT>(st, bar, s, __ldg(d.rec + 2LL * s + 1), d.rec, d.masks, d.colp,
-                           static_cast<const VT*>(d.valp), pol);
+__device__ __forceinline__ void issue_global(unsigned char* st, uint64_t* bar, const BatchSlot* slots, int j, int g,
+                                             int4 r1, uint64_t pol) {
+    const BatchSlot* d = slots + j;
+    issue_subtile<VT, IPT>(st, bar, g - d->tile0, r1, d->rec, d->masks, d->colp, static_cast<const VT*>(d->valp),
+                           pol);
+}
+
+// Slot and record of global sub-tile g (for a later issue_global).
+__device__ __forceinline__ int4 prefetch_rec(const BatchTable& T, int g, int& j) {
+    j = __ldg(T.tile_slot + g);
+    const BatchSlot* d = T.slots + j;
+    return __ldg(d->rec + 2LL * (g - d->tile0) + 1);
 }
 
 template <typename VT, typename XT, typename AT, int NT, int IPT>
-__global__ void __launch_bounds__(NT) k_batch_spmv(const BatchTable* __restrict__ Tp, int want_dot) {
+__global__ void __launch_bounds__(NT, 4) k_batch_spmv(const BatchTable* __restrict__ Tp) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
     constexpr int NS = kBatchStages;
@@ -72,52 +103,59 @@ __global__ void __launch_bounds__(NT) k_batch_spmv(const BatchTable* __restrict_
     AT* cval = cval_s + 32 * w;
     AT* hval = hval_s + 32 * w;
     const uint64_t pol = policy_evict_first();
+    int pj = 0;
+    int4 pref = make_int4(0, 0, 0, 0);
     if (lane == 0) {
         for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
         fence_mbar_init();
-        for (int k = 0; k < NS && k < n; ++k)
-            issue_global<VT, IPT>(stages + k * S::BYTES, &bars[w][k], T.slots, T.nslots, gw + k * tw, pol);
+        for (int k = 0; k < NS && k < n; ++k) {
+            int j;
+            const int4 r1 = prefetch_rec(T, gw + k * tw, j);
+            issue_global<VT, IPT>(stages + k * S::BYTES, &bars[w][k], T.slots, j, gw + k * tw, r1, pol);
+        }
+        if (n > NS) pref = prefetch_rec(T, gw + NS * tw, pj);
     }
     __syncwarp();
+    int jc = __ldg(T.tile_slot + gw);
+    int jcur = -1;  // slot whose fields are in `cur` (consecutive sub-tiles of a warp often share it)
+    SlotRegs cur;
     int i = 0;
     for (; i < n; ++i) {
         const int k = i % NS;
         const int g = gw + i * tw;
         unsigned char* st = stages + k * S::BYTES;
+        // the slot's fields (when the slot changes) and the next sub-tile's
+        // slot: loads in flight during the wait
+        if (jc != jcur) {
+            load_slot(T, jc, cur);
+            jcur = jc;
+        }
+        const int jn = i + 1 < n ? __ldg(T.tile_slot + g + tw) : 0;
         const bool ok = mbar_wait_bounded(&bars[w][k], (uint32_t)(i / NS) & 1u, T.status);
         if (!__all_sync(0xffffffffu, ok)) break;
-        const int j = find_slot<0>(T.slots, T.nslots, g);
-        const BatchSlot& d = T.slots[j];
-        const SlotState& ss_ = T.states[d.state];
-        const int kit = ss_.k;
-        const int e = kit > 0 ? pow2_exponent_from_nsq(ss_.nsq) : 0;
-        const XT* in = static_cast<const XT*>((kit & 1) ? d.Y : d.X);
-        XT* out = static_cast<XT*>((kit & 1) ? d.X : d.Y);
-        const int s = g - d.tile0;
+        const int e = cur.k > 0 ? pow2_rescale_exponent(cur.nsq, rescale_window<XT>()) : 0;
+        const XT* in = static_cast<const XT*>((cur.k & 1) ? cur.Y : cur.X);
+        XT* out = const_cast<XT*>(static_cast<const XT*>((cur.k & 1) ? cur.X : cur.Y));
+        const int s = g - cur.tile0;
+        AT* car = static_cast<AT*>(cur.carries);
         AT xv[IPT];
         gather_subtile<VT, XT, AT, IPT>(st, in, xv);
-        double sq = 0.0, dd = 0.0;
-        if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
-            finish_subtile<MODE_POWER, true, VT, XT, AT, IPT>(s, st, xv, d.row_start, out, static_cast<AT*>(d.carries),
-                                                              d.nor, e, sq, crow, cval, hval, want_dot ? in : nullptr,
-                                                              &dd);
+        const bool general = reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral;
+        if (general)
+            finish_subtile<MODE_POWER, true, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
+                                                              cval, hval);
         else
-            finish_subtile<MODE_POWER, false, VT, XT, AT, IPT>(s, st, xv, d.row_start, out,
-                                                               static_cast<AT*>(d.carries), d.nor, e, sq, crow, cval,
-                                                               hval, want_dot ? in : nullptr, &dd);
-        for (int o = 16; o > 0; o >>= 1) {
-            sq += __shfl_down_sync(0xffffffffu, sq, o);
-            dd += __shfl_down_sync(0xffffffffu, dd, o);
-        }
+            finish_subtile<MODE_POWER, false, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
+                                                               cval, hval);
         if (lane == 0) {
-            T.tile_part[2LL * g] = sq;
-            T.tile_part[2LL * g + 1] = dd;
             if (i + NS < n) {
                 fence_proxy_async();
-                issue_global<VT, IPT>(st, &bars[w][k], T.slots, T.nslots, g + NS * tw, pol);
+                issue_global<VT, IPT>(st, &bars[w][k], T.slots, pj, g + NS * tw, pref, pol);
+                if (i + NS + 1 < n) pref = prefetch_rec(T, g + (NS + 1) * tw, pj);
             }
         }
         __syncwarp();
+        jc = jn;
     }
     if (i < n) {  // timed out: let this warp's copies in flight land first
         if (lane == 0)
@@ -127,43 +165,65 @@ __global__ void __launch_bounds__(NT) k_batch_spmv(const BatchTable* __restrict_
     }
 }
 
+// tile_slot[g] = the slot owning global sub-tile g (one CTA per slot).
+__global__ void k_tile_slots(const BatchTable* __restrict__ Tp) {
+    const BatchTable T = *Tp;
+    for (int j = blockIdx.x; j < T.nslots; j += gridDim.x) {
+        const int t0 = T.slots[j].tile0, nt = T.slots[j].nsub;
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) T.tile_slot[t0 + t] = j;
+    }
+}
+
 template <typename XT, typename AT>
-__global__ void __launch_bounds__(256) k_batch_reduce(const BatchTable* __restrict__ Tp, int want_dot) {
+__global__ void __launch_bounds__(256) k_batch_fixup(const BatchTable* __restrict__ Tp) {
+    const BatchTable T = *Tp;
+    for (int c = blockIdx.x; c < T.nfix; c += gridDim.x) {
+        const int j = find_slot<1>(T.slots, T.nslots, c);
+        const BatchSlot& d = T.slots[j];
+        const SlotState* stt = T.states + d.state;
+        const int kit = stt->k;
+        const int e = kit > 0 ? pow2_rescale_exponent(stt->nsq, rescale_window<XT>()) : 0;
+        XT* out = static_cast<XT*>((kit & 1) ? d.X : d.Y);
+        const int lo = (c - d.fix0) * kFixTiles;
+        const int hi = min(d.nsub, lo + kFixTiles);
+        const AT* car = static_cast<const AT*>(d.carries);
+        fixup_pass<MODE_POWER, XT, AT>(d.row_start, d.subc, d.nor, d.nsub, out, car, e, lo + threadIdx.x, hi,
+                                       blockDim.x);
+    }
+}
+
+template <typename XT>
+__global__ void __launch_bounds__(256) k_batch_norm(const BatchTable* __restrict__ Tp, int want_dot) {
     __shared__ double red[32];
     __shared__ int last;
     const BatchTable T = *Tp;
-    for (int c = blockIdx.x; c < T.nred; c += gridDim.x) {
-        const int j = find_slot<1>(T.slots, T.nslots, c);
+    for (int c = blockIdx.x; c < T.nrow; c += gridDim.x) {
+        const int j = find_slot<2>(T.slots, T.nslots, c);
         const BatchSlot& d = T.slots[j];
         SlotState* stt = T.states + d.state;
         const int kit = stt->k;
-        const int e = kit > 0 ? pow2_exponent_from_nsq(stt->nsq) : 0;
         const XT* in = static_cast<const XT*>((kit & 1) ? d.Y : d.X);
-        XT* out = static_cast<XT*>((kit & 1) ? d.X : d.Y);
-        const int lo = (c - d.red0) * kRedTiles;
-        const int hi = min(d.nsub, lo + kRedTiles);
+        const XT* out = static_cast<const XT*>((kit & 1) ? d.X : d.Y);
+        const int lo = (c - d.row0) * kRowChunk;
+        const int hi = min(d.nor, lo + kRowChunk);
         double sq = 0.0, dd = 0.0;
-        fixup_pass<MODE_POWER, XT, AT>(d.row_start, d.subc, d.nor, d.nsub, out, static_cast<const AT*>(d.carries), e,
-                                       sq, want_dot ? in : nullptr, &dd, lo + threadIdx.x, hi, blockDim.x);
-        for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
-            sq += T.tile_part[2LL * (d.tile0 + t)];
-            dd += T.tile_part[2LL * (d.tile0 + t) + 1];
-        }
+        if (want_dot) norm_rows<XT, true>(out, in, lo, hi, threadIdx.x, blockDim.x, sq, dd);
+        else norm_rows<XT, false>(out, in, lo, hi, threadIdx.x, blockDim.x, sq, dd);
         sq = block_sum<256>(sq, red);
-        dd = block_sum<256>(dd, red);
+        if (want_dot) dd = block_sum<256>(dd, red);
         if (threadIdx.x == 0) {
-            T.red_part[2LL * c] = sq;
-            T.red_part[2LL * c + 1] = dd;
+            T.row_part[2LL * c] = sq;
+            T.row_part[2LL * c + 1] = dd;
             __threadfence();
-            last = atomicAdd(&stt->red_count, 1u) == (unsigned)d.nred - 1u;
+            last = atomicAdd(&stt->norm_count, 1u) == (unsigned)d.nrow - 1u;
         }
         __syncthreads();
         if (last && threadIdx.x < 32) {
             __threadfence();
             double s0 = 0.0, s1 = 0.0;
-            for (int q = threadIdx.x; q < d.nred; q += 32) {
-                s0 += __ldcg(T.red_part + 2LL * (d.red0 + q));
-                s1 += __ldcg(T.red_part + 2LL * (d.red0 + q) + 1);
+            for (int q = threadIdx.x; q < d.nrow; q += 32) {
+                s0 += __ldcg(T.row_part + 2LL * (d.row0 + q));
+                s1 += __ldcg(T.row_part + 2LL * (d.row0 + q) + 1);
             }
             for (int o = 16; o > 0; o >>= 1) {
                 s0 += __shfl_down_sync(0xffffffffu, s0, o);
@@ -174,7 +234,7 @@ __global__ void __launch_bounds__(256) k_batch_reduce(const BatchTable* __restri
                 stt->nsq = s0;
                 if (want_dot) stt->dot = s1;
                 stt->k = kit + 1;
-                stt->red_count = 0u;
+                stt->norm_count = 0u;
             }
         }
         __syncthreads();
@@ -186,18 +246,18 @@ __global__ void __launch_bounds__(256) k_batch_resid(const BatchTable* __restric
     __shared__ double red[32];
     __shared__ int last;
     const BatchTable T = *Tp;
-    for (int c = blockIdx.x; c < T.nres; c += gridDim.x) {
+    for (int c = blockIdx.x; c < T.nrow; c += gridDim.x) {
         const int j = find_slot<2>(T.slots, T.nslots, c);
         const BatchSlot& d = T.slots[j];
         SlotState* stt = T.states + d.state;
         const int kit = stt->k;  // >= 2 after a round
         const double nsq_prev = stt->nsq_prev;
-        const int e = kit - 1 > 0 ? pow2_exponent_from_nsq(nsq_prev) : 0;
+        const int e = kit - 1 > 0 ? pow2_rescale_exponent(nsq_prev, rescale_window<XT>()) : 0;
         const double lam = scale_pow2(stt->dot, -e) / nsq_prev;
         const XT* cur = static_cast<const XT*>((kit & 1) ? d.Y : d.X);
         const XT* prev = static_cast<const XT*>((kit & 1) ? d.X : d.Y);
-        const int lo = (c - d.res0) * kResRows;
-        const int hi = min(d.nor, lo + kResRows);
+        const int lo = (c - d.row0) * kRowChunk;
+        const int hi = min(d.nor, lo + kRowChunk);
         double rr = 0.0;
         for (int r = lo + threadIdx.x; r < hi; r += blockDim.x) {
             const double dl = scale_pow2((double)cur[r], -e) - lam * (double)prev[r];
@@ -207,13 +267,13 @@ __global__ void __launch_bounds__(256) k_batch_resid(const BatchTable* __restric
         if (threadIdx.x == 0) {
             T.res_part[c] = rr;
             __threadfence();
-            last = atomicAdd(&stt->res_count, 1u) == (unsigned)d.nres - 1u;
+            last = atomicAdd(&stt->res_count, 1u) == (unsigned)d.nrow - 1u;
         }
         __syncthreads();
         if (last && threadIdx.x < 32) {
             __threadfence();
             double s0 = 0.0;
-            for (int q = threadIdx.x; q < d.nres; q += 32) s0 += __ldcg(T.res_part + d.res0 + q);
+            for (int q = threadIdx.x; q < d.nrow; q += 32) s0 += __ldcg(T.res_part + d.row0 + q);
             for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
             if (threadIdx.x == 0) {
                 stt->lambda = lam;
@@ -254,8 +314,9 @@ struct BatchKernels {
         return occ * sm_count;
     }
     static cudaError_t step(const BatchTable* T, int want_dot, int sm_count, cudaStream_t st) {
-        k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid(sm_count), kBatchNT, SMEM, st>>>(T, want_dot);
-        k_batch_reduce<XT, AT><<<2 * sm_count, 256, 0, st>>>(T, want_dot);
+        k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid(sm_count), kBatchNT, SMEM, st>>>(T);
+        k_batch_fixup<XT, AT><<<2 * sm_count, 256, 0, st>>>(T);
+        k_batch_norm<XT><<<4 * sm_count, 256, 0, st>>>(T, want_dot);
         return cudaGetLastError();
     }
 };
@@ -281,6 +342,12 @@ cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_c
     }
     if (cfg == kCfgF64) k_batch_resid<double><<<2 * sm_count, 256, 0, st>>>(T);
     else k_batch_resid<float><<<2 * sm_count, 256, 0, st>>>(T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_slots(const BatchTable* T, int nslots, cudaStream_t st) {
+    if (nslots <= 0) return cudaSuccess;
+    k_tile_slots<<<nslots < 1024 ? nslots : 1024, 256, 0, st>>>(T);
     return cudaGetLastError();
 }
 

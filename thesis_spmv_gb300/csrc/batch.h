@@ -15,8 +15,8 @@
 
 namespace pwmgpu {
 
-constexpr int kRedTiles = 2048;   // sub-tiles per reduction chunk
-constexpr int kResRows = 32768;   // rows per residual chunk
+constexpr int kFixTiles = 2048;   // sub-tiles per fix-up chunk
+constexpr int kRowChunk = 32768;  // rows per norm / residual chunk
 
 struct BatchSlot {
     const int32_t* row_start;
@@ -30,8 +30,8 @@ struct BatchSlot {
     void* carries;
     int nor, nsub;
     int tile0;       // first global sub-tile
-    int red0, nred;  // reduction chunks [red0, red0 + nred)
-    int res0, nres;  // residual chunks [res0, res0 + nres)
+    int fix0, nfix;  // fix-up chunks [fix0, fix0 + nfix) (kFixTiles sub-tiles each)
+    int row0, nrow;  // row chunks [row0, row0 + nrow) (kRowChunk rows each)
     int state;       // index into the state array
     int pad;
 };
@@ -45,16 +45,16 @@ struct SlotState {
     double dot;         // v_{k-1} . v_k, from the last step of a round
     double lambda;      // Rayleigh quotient of u = v_{k-1} / ||v_{k-1}||
     double res2;        // ||A u - lambda u||^2 * ||v_{k-1}||^2
-    unsigned int red_count, res_count;  // last-CTA counters (zero between kernels)
+    unsigned int norm_count, res_count;  // last-CTA counters (zero between kernels)
 };
 
 struct BatchTable {
-    int nslots, ntiles, nred, nres;
+    int nslots, ntiles, nfix, nrow;
     const BatchSlot* slots;
     SlotState* states;
-    double* tile_part;  // 2 per global sub-tile: sum of squares, dot
-    double* red_part;   // 2 per reduction chunk
-    double* res_part;   // 1 per residual chunk
+    int* tile_slot;     // slot of each global sub-tile
+    double* row_part;   // 2 per row chunk: sum of squares, dot
+    double* res_part;   // 1 per row chunk
     int* status;
 };
 

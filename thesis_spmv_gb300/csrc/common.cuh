@@ -137,6 +137,28 @@ __host__ __device__ __forceinline__ int pow2_exponent_from_nsq(double nsq) {
     return -fl;
 }
 
+// Exponent of the power method's rescale for an iterate with squared norm
+// nsq: 0 (no rescale) while nsq stays within [2^-window, 2^window], else the
+// exponent that brings the norm into [1, 2).  Rescaling by powers of two is
+// exact, so the schedule does not change the normalised iterates; it only
+// keeps them clear of overflow and underflow.  window: 256 for FP64 vectors,
+// 32 for FP32 vectors.
+__host__ __device__ __forceinline__ int pow2_rescale_exponent(double nsq, int window) {
+    long long bits;
+#ifdef __CUDA_ARCH__
+    bits = __double_as_longlong(nsq);
+#else
+    std::memcpy(&bits, &nsq, sizeof bits);
+#endif
+    const int ex = (int)((bits >> 52) & 0x7FF) - 1023;  // unbiased exponent
+    if (bits > 0 && ex >= -window && ex < window) return 0;
+    return pow2_exponent_from_nsq(nsq);
+}
+template <typename XT>
+__host__ __device__ __forceinline__ int rescale_window() {
+    return sizeof(XT) == 4 ? 32 : 256;
+}
+
 // ---- value conversions ---------------------------------------------------
 template <typename T> __device__ __forceinline__ double to_f64(T v);
 template <> __device__ __forceinline__ double to_f64<double>(double v) { return v; }

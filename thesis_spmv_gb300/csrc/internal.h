@@ -70,16 +70,18 @@ cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const 
 cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
-                              const void* x, void* y, void* carries, const double* nsq_in, double* partials,
-                              int* status, cudaStream_t st);
+                              const void* x, void* y, void* carries, const double* nsq_in, int* status,
+                              cudaStream_t st);
+// Carries of the merge SpMV into y (MODE_POWER: times the rescale factor of
+// nsq_in).
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
-                                   const double* carries, const double* nsq_in, const double* spmv_partials,
-                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
-                                   double* nsq_out, cudaStream_t st);
+                                   const double* carries, const double* nsq_in, int fix_grid, cudaStream_t st);
 cudaError_t launch_merge_fixup_f32(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, float* y,
-                                   const float* carries, const double* nsq_in, const double* spmv_partials,
-                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
-                                   double* nsq_out, cudaStream_t st);
+                                   const float* carries, const double* nsq_in, int fix_grid, cudaStream_t st);
+// out[0] = ||y||^2 and, when x is given, out[1] = x . y (deterministic;
+// partials: 2 per CTA of `grid`; counter zero between launches).
+cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, double* partials, unsigned int* counter,
+                                  double* out, int grid, cudaStream_t st);
 cudaError_t launch_power_finalize_f64(double* last, const double* nsq_last, double* prev, const double* nsq_prev,
                                       int n, int sm_count, cudaStream_t st);
 cudaError_t launch_poisson_crs(int m, int n, int32_t* row_start, int32_t* col, double* val, int sm_count,
@@ -113,6 +115,7 @@ cudaError_t launch_inclusive_scan(int32_t* a, long long n, int32_t* scratch, cud
 struct BatchTable;
 void batch_prepare(int sm_count);
 cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st);
+cudaError_t launch_tile_slots(const BatchTable* T, int nslots, cudaStream_t st);
 cudaError_t launch_fill_uniform(double* x, int n, uint64_t seed, int sm_count, cudaStream_t st);
 
 // Record the calling thread's last error message (pwmgpu_last_error).

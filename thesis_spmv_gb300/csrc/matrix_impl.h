@@ -148,5 +148,6 @@ int build_plan(pwmgpu_matrix* m);
 int ensure_vectors(pwmgpu_matrix* m);
 int ensure_fvectors(pwmgpu_matrix* m);
 int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** valp, int* pgrid);
+bool low_precision_floor(double rel, double prev_rel);
 
 }  // namespace pwmgpu

@@ -132,7 +132,6 @@ struct MergeArgs {
     XT* y;
     AT* carries;           // one per sub-tile
     const double* nsq_in;  // MODE_POWER: ||x||^2 (source of the 2^e rescale), or null for e = 0
-    double* partials;      // MODE_POWER: per-CTA sum of squares
     int* status;
 };
 
@@ -146,8 +145,7 @@ constexpr int kMliStages = 2;
 template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH>
 __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
                                           XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
-                                          AT* cval, AT* hval, uint32_t& ticket, int e, double& sumsq,
-                                          const XT* __restrict__ xdot, double* dot, uint64_t pol) {
+                                          AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol) {
     using S = WarpStage<VT, IPT>;
     constexpr int NS = kMliStages;
     constexpr int W = NT / 32;
@@ -176,11 +174,11 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         AT xv[IPT];
         gather_subtile<VT, XT, AT, IPT, XCOH>(st, x, xv);
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
-            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, sumsq, crow,
-                                                        cval, hval, xdot, dot);
+            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow, cval,
+                                                        hval);
         else
-            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, sumsq,
-                                                         crow, cval, hval, xdot, dot);
+            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow, cval,
+                                                         hval);
         // every lane is done with this stage (finish_subtile ends with a warp
         // barrier): refill it with the warp's sub-tile i + NS
         if (lane == 0 && i + NS < n) {
@@ -214,23 +212,17 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     __shared__ int crow[NT];
     __shared__ AT cval[NT];
     __shared__ AT hval[NT];
-    __shared__ double red[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
+    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     if (lane == 0) {
         for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
         fence_mbar_init();
     }
     __syncwarp();
     uint32_t ticket = 0;
-    double sumsq = 0.0, dot = 0.0;
-    warp_pass<MODE, VT, XT, AT, NT, IPT, false>(a, a.x, a.y, smem_raw + (size_t)w * NS * S::BYTES, bars[w], crow + 32 * w,
-                                         cval + 32 * w, hval + 32 * w, ticket, e, sumsq, nullptr, &dot,
-                                         policy_evict_first());
-    if (MODE == MODE_POWER) {
-        double t = block_sum<NT>(sumsq, red);
-        if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
-    }
+    unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
+    warp_pass<MODE, VT, XT, AT, NT, IPT, false>(a, a.x, a.y, stages, bars[w], crow + 32 * w, cval + 32 * w,
+                                                hval + 32 * w, ticket, e, policy_evict_first());
 }
 
 template <typename XT, typename AT>
@@ -240,44 +232,52 @@ struct FixArgs {
     int nor, num_tiles;
     XT* y;
     const AT* carries;
-    const double* nsq_in;
-    const double* spmv_partials;
-    int n_spmv_partials;
-    double* fix_partials;
-    unsigned int* counter;
-    double* nsq_out;
+    const double* nsq_in;  // MODE_POWER: ||x||^2, source of the rescale exponent
 };
 
-// Stand-alone fix-up kernel; MODE_POWER finishes ||y||^2 with one
-// deterministic reduction over all partials by the last CTA.
+// Stand-alone fix-up kernel (one thread per sub-tile).
 template <int MODE, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
+    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, a.num_tiles, stride);
+}
+
+// ||y||^2 (and x . y with DOT) with one deterministic reduction: per-CTA
+// partials, then the last CTA sums them in order.  out[0] = sum y^2,
+// out[1] = sum x y.
+template <typename XT, bool DOT>
+__global__ void __launch_bounds__(256) k_power_norm(const XT* __restrict__ y, const XT* __restrict__ x, int n,
+                                                    double* partials, unsigned int* counter, double* out) {
     __shared__ double red[32];
     __shared__ bool am_last;
-    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_exponent_from_nsq(*a.nsq_in) : 0;
-    double sumsq = 0.0, dot = 0.0;
-    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, sumsq, nullptr, &dot,
-                             blockIdx.x * blockDim.x + threadIdx.x, a.num_tiles, gridDim.x * blockDim.x);
-    if (MODE != MODE_POWER) return;
-    double t = block_sum<256>(sumsq, red);
+    double ss = 0.0, dd = 0.0;
+    norm_rows<XT, DOT>(y, x, 0, n, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, ss, dd);
+    ss = block_sum<256>(ss, red);
+    if (DOT) dd = block_sum<256>(dd, red);
     if (threadIdx.x == 0) {
-        a.fix_partials[blockIdx.x] = t;
+        partials[2 * blockIdx.x] = ss;
+        partials[2 * blockIdx.x + 1] = dd;
         __threadfence();
-        unsigned prev = atomicAdd(a.counter, 1u);
-        am_last = (prev == gridDim.x - 1);
+        am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (am_last && threadIdx.x < 32) {
         __threadfence();
-        // lane l sums partials l, l+32, ... in order; then a fixed shuffle tree
         const int l = threadIdx.x;
-        double s = 0.0;
-        for (int i = l; i < a.n_spmv_partials; i += 32) s += __ldcg(a.spmv_partials + i);
-        for (int i = l; i < (int)gridDim.x; i += 32) s += __ldcg(a.fix_partials + i);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        double s0 = 0.0, s1 = 0.0;
+        for (int i = l; i < (int)gridDim.x; i += 32) {
+            s0 += __ldcg(partials + 2 * i);
+            s1 += __ldcg(partials + 2 * i + 1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_down_sync(0xffffffffu, s0, o);
+            s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        }
         if (l == 0) {
-            *a.nsq_out = s;
-            *a.counter = 0u;
+            out[0] = s0;
+            if (DOT) out[1] = s1;
+            *counter = 0u;
         }
     }
 }
@@ -345,13 +345,19 @@ __device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
 // ---------------------------------------------------------------------------
 // K5: the power-method step fused into one persistent kernel (cooperative
 // launch).  Iteration k (k0 <= k < k0 + nk):
-//   v_{k+1} = 2^{e_k} A v_k         (SpMV; e_k from ||v_k||^2, exact rescale)
-//   ||v_{k+1}||^2                    (epilogue + fix-up, deterministic)
-//   v_k . v_{k+1} on the last iteration when `result` is set, then the
-//   Rayleigh quotient lambda_k = 2^{-e_k} v_k.v_{k+1} / ||v_k||^2 and the
-//   eigen-residual ||2^{-e_k} v_{k+1} - lambda_k v_k||^2 (one more pass)
-// Vectors ping-pong: iteration k reads X when k is even, Y when odd.  Two grid
-// barriers per iteration (SpMV | fix-up | reduction).  The normalisation of
+//   v_{k+1} = 2^{e_k} A v_k         (SpMV pass; e_k from ||v_k||^2: an exact
+//                                     rescale, applied only when the norm
+//                                     leaves a wide window)
+//   carries of v_{k+1}               (fix-up pass)
+//   ||v_{k+1}||^2                    (row pass, deterministic)
+//   v_k . v_{k+1} in the same row pass on the last iteration when `result`
+//   is set, then the Rayleigh quotient lambda_k = 2^{-e_k} v_k.v_{k+1} /
+//   ||v_k||^2 and the eigen-residual ||2^{-e_k} v_{k+1} - lambda_k v_k||^2
+// Vectors ping-pong: iteration k reads X when k is even, Y when odd.  Three
+// grid barriers per iteration (SpMV | fix-up | row pass | total).  Keeping
+// the squares out of the SpMV pass keeps its FP64 work at one FMA per
+// nonzero (GB300's FP64 pipe is 2 operations per clock per SM).  The
+// normalisation of
 // the reference (y /= ||y||, Util/VectorUtill.hpp:34-41) is carried by the
 // exponent and applied once at the end (k_power_finalize).  All reductions
 // are FP64 and in a fixed order, whatever the vector type.
@@ -416,20 +422,22 @@ __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p
     double nsq_cur = p.k0 > 0 ? p.nsq[p.k0] : 0.0;
     double nsq_last = 0.0;
     int e = 0;
+    unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
+    const int tid = blockIdx.x * NT + threadIdx.x, nthr = gridDim.x * NT;
     for (int k = p.k0; k < p.k0 + p.nk; ++k) {
         const XT* in = (k & 1) ? p.Y : p.X;
         XT* out = (k & 1) ? p.X : p.Y;
-        e = k > 0 ? pow2_exponent_from_nsq(nsq_cur) : 0;
+        e = k > 0 ? pow2_rescale_exponent(nsq_cur, rescale_window<XT>()) : 0;
         nsq_last = nsq_cur;
         const bool want_dot = p.result && k == p.k0 + p.nk - 1;
-        double ss = 0.0, dd = 0.0;
-        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true>(a, in, out, smem_raw + (size_t)w * NS * S::BYTES, bars[w],
-                                                   crow + 32 * w, cval + 32 * w, hval + 32 * w, ticket, e, ss,
-                                                   want_dot ? in : nullptr, &dd, pol);
+        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true>(a, in, out, stages, bars[w], crow + 32 * w, cval + 32 * w,
+                                                         hval + 32 * w, ticket, e, pol);
         if (!grid_sync(p.barrier, a.status)) return;
-        fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, ss,
-                                       want_dot ? in : nullptr, &dd, blockIdx.x * NT + threadIdx.x, a.nsub,
-                                       gridDim.x * NT);
+        fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub, nthr);
+        if (!grid_sync(p.barrier, a.status)) return;
+        double ss = 0.0, dd = 0.0;
+        if (want_dot) norm_rows<XT, true>(out, in, 0, a.nor, tid, nthr, ss, dd);
+        else norm_rows<XT, false>(out, in, 0, a.nor, tid, nthr, ss, dd);
         const double t_ss = block_sum<NT>(ss, red);
         const double t_dd = block_sum<NT>(dd, red);
         if (threadIdx.x == 0) {
@@ -657,7 +665,7 @@ struct MergeKernels {
                              unsigned int* barrier, int* status, cudaStream_t st) {
         power_occ();
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
-                                 nullptr, (AT*)carries, nullptr, nullptr, status},
+                                 nullptr, (AT*)carries, nullptr, status},
                                 P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier};
         cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned int), st);
         if (e != cudaSuccess) return e;
@@ -669,11 +677,11 @@ struct MergeKernels {
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
-                            const void* x, void* y, void* carries, const double* nsq_in, double* partials,
-                            int* status, cudaStream_t st) {
+                            const void* x, void* y, void* carries, const double* nsq_in, int* status,
+                            cudaStream_t st) {
         geom();
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub,
-                                (const XT*)x, (XT*)y, (AT*)carries, nsq_in, partials, status};
+                                (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status};
         if (mode == MODE_POWER)
             k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT><<<grid, NT, SMEM, st>>>(a);
         else
@@ -776,42 +784,40 @@ cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, in
 }
 
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
-                              const void* x, void* y, void* carries, const double* nsq_in, double* partials,
-                              int* status, cudaStream_t st) {
+                              const void* x, void* y, void* carries, const double* nsq_in, int* status,
+                              cudaStream_t st) {
     if (P.nsub == 0) return cudaSuccess;
     switch (cfg) {
-        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
-        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
-        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, partials, status, st);
+        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
+        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
+        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
     }
 }
 
 template <typename XT, typename AT>
 static cudaError_t fixup_impl(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, XT* y,
-                              const AT* carries, const double* nsq_in, const double* spmv_partials, int n_spmv,
-                              double* fix_partials, int fix_grid, unsigned int* counter, double* nsq_out,
-                              cudaStream_t st) {
-    FixArgs<XT, AT> a{M.row_start, tiles, M.nor, num_tiles, y, carries, nsq_in, spmv_partials, n_spmv,
-                      fix_partials, counter, nsq_out};
+                              const AT* carries, const double* nsq_in, int fix_grid, cudaStream_t st) {
+    FixArgs<XT, AT> a{M.row_start, tiles, M.nor, num_tiles, y, carries, nsq_in};
     if (mode == MODE_POWER) k_merge_fixup<MODE_POWER, XT, AT><<<fix_grid, 256, 0, st>>>(a);
     else k_merge_fixup<MODE_SPMV, XT, AT><<<fix_grid, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
-                                   const double* carries, const double* nsq_in, const double* spmv_partials,
-                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
-                                   double* nsq_out, cudaStream_t st) {
-    return fixup_impl<double, double>(mode, M, tiles, num_tiles, y, carries, nsq_in, spmv_partials, n_spmv,
-                                      fix_partials, fix_grid, counter, nsq_out, st);
+                                   const double* carries, const double* nsq_in, int fix_grid, cudaStream_t st) {
+    return fixup_impl<double, double>(mode, M, tiles, num_tiles, y, carries, nsq_in, fix_grid, st);
 }
 
 cudaError_t launch_merge_fixup_f32(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, float* y,
-                                   const float* carries, const double* nsq_in, const double* spmv_partials,
-                                   int n_spmv, double* fix_partials, int fix_grid, unsigned int* counter,
-                                   double* nsq_out, cudaStream_t st) {
-    return fixup_impl<float, float>(mode, M, tiles, num_tiles, y, carries, nsq_in, spmv_partials, n_spmv,
-                                    fix_partials, fix_grid, counter, nsq_out, st);
+                                   const float* carries, const double* nsq_in, int fix_grid, cudaStream_t st) {
+    return fixup_impl<float, float>(mode, M, tiles, num_tiles, y, carries, nsq_in, fix_grid, st);
+}
+
+cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, double* partials, unsigned int* counter,
+                                  double* out, int grid, cudaStream_t st) {
+    if (x) k_power_norm<double, true><<<grid, 256, 0, st>>>(y, x, n, partials, counter, out);
+    else k_power_norm<double, false><<<grid, 256, 0, st>>>(y, x, n, partials, counter, out);
+    return cudaGetLastError();
 }
 
 int fixup_grid(int num_tiles, int sm_count) {

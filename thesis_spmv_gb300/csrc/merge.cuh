@@ -179,22 +179,14 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 // Second half: FMAs over the staged values, row completion, carries.
 //   x, y      input / output vectors
 //   carries   carries[s] = partial sum of the sub-tile's unfinished last row
-//   e         power-of-two exponent applied to stored rows (MODE_POWER)
-//   sumsq     per-lane running sum of squares (MODE_POWER); each row is
-//             counted exactly once, by whoever writes its final value:
-//               * the lane that completes it, if the row began in that lane;
-//               * the first lane of the carry run, if the row began in an
-//                 earlier lane of this sub-tile;
-//               * k_merge_fixup, if the row began in an earlier sub-tile.
+//   e         MODE_POWER: rows are stored times 2^e (exact rescale of the
+//             power method's iterate; a warp-uniform skip when e == 0)
 //   crow, cval, hval   this warp's 32-entry shared scratch
-//   xdot, dot when xdot is set (MODE_POWER), dot also sums x[r]*y[r] over the
-//             same rows: the Rayleigh quotient's numerator for a square A
 template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT>
 __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, const AT (&xv)[IPT],
                                                const int32_t* __restrict__ row_start, XT* __restrict__ y,
-                                               AT* __restrict__ carries, int nor, int e, double& sumsq, int* crow,
-                                               AT* cval, AT* hval, const XT* __restrict__ xdot = nullptr,
-                                               double* dot = nullptr) {
+                                               AT* __restrict__ carries, int nor, int e, int* crow, AT* cval,
+                                               AT* hval) {
     using S = WarpStage<VT, IPT>;
     const int lane = threadIdx.x & 31;
     const int4 r0 = reinterpret_cast<const int4*>(st)[0];
@@ -235,25 +227,16 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
     // ---- FMAs: one per nonzero, warp-uniform trip count ----
     AT acc = AT(0);
     bool to_head = head_open && lane > 0;  // first completed row goes to hval
-    bool count = !head_open;               // its square is final here
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
         if (j < q) {
             acc = fma((AT)vr[j], xv[j], acc);
             if ((mask >> j) & 1u) {
                 AT v = acc;
-                if (MODE == MODE_POWER) v = scale_pow2(v, e);
-                if (to_head) {
-                    hval[lane] = v;
-                } else {
-                    y[a] = (XT)v;
-                    if (MODE == MODE_POWER && count) {
-                        sumsq = fma((double)v, (double)v, sumsq);
-                        if (xdot) *dot = fma((double)__ldcg(xdot + a), (double)v, *dot);
-                    }
-                }
+                if (MODE == MODE_POWER && e != 0) v = scale_pow2(v, e);
+                if (to_head) hval[lane] = v;
+                else y[a] = (XT)v;
                 to_head = false;
-                count = true;
                 acc = AT(0);
                 ++a;
                 if (GENERAL) {  // empty rows: written as 0 as the lane passes them
@@ -281,16 +264,7 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
             // left its part in hval[u] and the total is written here.
             const int rs_a = __ldg(row_start + a);
             const int b0u = kw0 + u * qm + (u < rem ? u : rem);
-            if (rs_a < b0u) {
-                const AT v = hval[u] + (MODE == MODE_POWER ? scale_pow2(sum, e) : sum);
-                y[a] = (XT)v;
-                // final now if the row began in this sub-tile; otherwise
-                // k_merge_fixup adds the earlier sub-tiles' carries and counts it
-                if (MODE == MODE_POWER && rs_a >= kw0) {
-                    sumsq = fma((double)v, (double)v, sumsq);
-                    if (xdot) *dot = fma((double)__ldcg(xdot + a), (double)v, *dot);
-                }
-            }
+            if (rs_a < b0u) y[a] = (XT)(hval[u] + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
         } else if (a < nor) {
             carries[s] = sum;  // a == rw1: the sub-tile's unfinished row
         }
@@ -304,16 +278,14 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
 // One thread per sub-tile; the first sub-tile of a run of sub-tiles ending in
 // the same row adds the run in order (deterministic).  The run's row r is
 // completed (and its partial written) by the first sub-tile after the run; the
-// carry is real only if that sub-tile started inside row r.  MODE_POWER also
-// sums the squares (and, with xdot, x[r]*y[r]) of the rows fixed here.
-// Threads take the first sub-tiles t = t0, t0 + stride, ... < t_end (a run
-// starting before t_end may extend past it).
+// carry is real only if that sub-tile started inside row r.  MODE_POWER adds
+// the carries times 2^e.  Threads take the first sub-tiles t = t0, t0 +
+// stride, ... < t_end (a run starting before t_end may extend past it).
 // ---------------------------------------------------------------------------
 template <int MODE, typename XT, typename AT>
 __device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start, const int2* __restrict__ tiles,
                                            int nor, int num_tiles, XT* __restrict__ y, const AT* __restrict__ carries,
-                                           int e, double& sumsq, const XT* __restrict__ xdot, double* dot, int t0,
-                                           int t_end, int stride) {
+                                           int e, int t0, int t_end, int stride) {
     for (int t = t0; t < t_end; t += stride) {
         const int r = tiles[t + 1].x;
         if (r >= nor) continue;
@@ -323,17 +295,42 @@ __device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start
         int n = t + 1;
         while (n < num_tiles && tiles[n + 1].x == r) sum += __ldcg(carries + n++);
         // sub-tile n starts at (r, tiles[n].y) and completes row r
-        if (tiles[n].y > row_start[r]) {
-            AT v;
-            if (MODE == MODE_POWER) v = (AT)__ldcg(y + r) + scale_pow2(sum, e);
-            else v = (AT)__ldcg(y + r) + sum;
-            y[r] = (XT)v;
-            if (MODE == MODE_POWER) {
-                sumsq = fma((double)v, (double)v, sumsq);
-                if (xdot) *dot = fma((double)xdot[r], (double)v, *dot);
-            }
+        if (tiles[n].y > row_start[r])
+            y[r] = (XT)((AT)__ldcg(y + r) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+    }
+}
+
+// Sum of squares of y[i] (and, with DOT, sum of x[i] * y[i]) over rows
+// i = lo + t0, lo + t0 + stride, ... < hi, in FP64 (loads through L2: y was
+// just written, possibly by other CTAs).
+// Four rows per step with independent loads and accumulators (combined as
+// (s0 + s1) + (s2 + s3) at the end: a fixed order for a fixed launch shape).
+template <typename XT, bool DOT>
+__device__ __forceinline__ void norm_rows(const XT* __restrict__ y, const XT* __restrict__ x, int lo, int hi, int t0,
+                                          int stride, double& ss, double& dd) {
+    double s[4] = {0.0, 0.0, 0.0, 0.0}, d[4] = {0.0, 0.0, 0.0, 0.0};
+    int i = lo + t0;
+    for (; i + 3 * stride < hi; i += 4 * stride) {
+        double v[4], w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[u] = (double)__ldcg(y + i + u * stride);
+            if (DOT) w[u] = (double)__ldcg(x + i + u * stride);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            s[u] = fma(v[u], v[u], s[u]);
+            if (DOT) d[u] = fma(w[u], v[u], d[u]);
         }
     }
+    double sr = 0.0, dr = 0.0;  // the last (up to 3) rows
+    for (; i < hi; i += stride) {
+        const double v = (double)__ldcg(y + i);
+        sr = fma(v, v, sr);
+        if (DOT) dr = fma((double)__ldcg(x + i), v, dr);
+    }
+    ss += ((s[0] + s[1]) + (s[2] + s[3])) + sr;
+    if (DOT) dd += ((d[0] + d[1]) + (d[2] + d[3])) + dr;
 }
 
 template <int NT>

@@ -193,8 +193,7 @@ extern "C" int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nn
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = launch_merge_fixup_f64(kModeSpmv, M, subc, nsub, y, carries, nullptr, nullptr, 0, nullptr,
-                                   fixup_grid(nsub, sms), nullptr, nullptr, st);
+        e = launch_merge_fixup_f64(kModeSpmv, M, subc, nsub, y, carries, nullptr, fixup_grid(nsub, sms), st);
     }
     if (e != cudaSuccess) return nfail(PWMGPU_ERR_CUDA, "pwmgpu_mv_csr_device_noalloc: %s", cudaGetErrorString(e));
     return PWMGPU_OK;

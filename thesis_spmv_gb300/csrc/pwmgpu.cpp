@@ -156,20 +156,22 @@ namespace {
 
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->num_tiles == 0) return PWMGPU_OK;
-    CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, nullptr,
-                         m->status, m->stream));
-    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, nullptr, 0, nullptr,
-                              m->fix_grid, nullptr, nullptr, m->stream));
+    CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, m->status,
+                         m->stream));
+    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, m->fix_grid,
+                              m->stream));
     return PWMGPU_OK;
 }
 
-// One power-method step on device vectors: out = 2^e(nsq_in) * A in, and
-// nsq_out = ||out||^2 (deterministic).
+// One power-method step on device vectors: out = 2^e(nsq_in) * A in (SpMV +
+// fix-up), then nsq_out = ||out||^2 (row pass, deterministic).
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
     CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
-                         m->partials, m->status, m->stream));
-    CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in, m->partials,
-                              m->grid, m->fix_partials, m->fix_grid, m->counter, nsq_out, m->stream));
+                         m->status, m->stream));
+    CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in, m->fix_grid,
+                              m->stream));
+    CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, nsq_out,
+                             dot_grid(m->M.nor, m->sm_count), m->stream));
     return PWMGPU_OK;
 }
 
@@ -295,6 +297,15 @@ int next_chunk(double rel, double prev_rel, int nk, double target) {
 // FP32 rounding floor of the residual (about nnz_row * 2^-24).
 constexpr double kSwitchRel = 2e-6;
 
+}  // namespace
+namespace pwmgpu {
+// The FP32 / BF16 phase has hit its rounding floor: the residual is small
+// (below 1e-4) and no longer falls (less than 10 % over the last check).  A
+// slowly converging solve (residual still large) stays in the fast phase.
+bool low_precision_floor(double rel, double prev_rel) { return rel < 1e-4 && rel >= 0.9 * prev_rel; }
+}  // namespace pwmgpu
+namespace {
+
 int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info) {
     const int N = m->M.nor;
     TRY(ensure_vectors(m));
@@ -330,8 +341,8 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
                 break;
             }
             if (k >= budget) break;
-            // FP32 has stopped converging: refine in FP64 from here
-            if (precision == PWMGPU_PREC_MIXED && nchunks >= 2 && o.rel >= 0.7 * prev) break;
+            // FP32 has reached its rounding floor: refine in FP64 from here
+            if (precision == PWMGPU_PREC_MIXED && nchunks >= 2 && low_precision_floor(o.rel, prev)) break;
             chunk = next_chunk(o.rel, prev, nk, target);
             prev = o.rel;
         }
@@ -733,9 +744,9 @@ int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     const void* valp = nullptr;
     TRY(ensure_low_values(m, false, &cfg, &valp, &pg));
     CU(launch_merge_spmv(kCfgF32, kModeSpmv, m->M, valp, m->P, merge_grid(kCfgF32, m->num_tiles, m->sm_count), dx,
-                         dy, m->carries, nullptr, nullptr, m->status, m->stream));
+                         dy, m->carries, nullptr, m->status, m->stream));
     CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
-                              nullptr, nullptr, 0, nullptr, m->fix_grid, nullptr, nullptr, m->stream));
+                              nullptr, m->fix_grid, m->stream));
     return PWMGPU_OK;
 }
 

@@ -59,10 +59,10 @@ struct ClassDev {
     BatchTable* dT = nullptr;
     BatchSlot* d_slots = nullptr;
     size_t slots_cap = 0;
-    double* tile_part = nullptr;
-    size_t tile_cap = 0;
-    double* red_part = nullptr;
-    size_t red_cap = 0;
+    int* tile_slot = nullptr;
+    size_t slot_cap = 0;
+    double* row_part = nullptr;
+    size_t row_cap = 0;
     double* res_part = nullptr;
     size_t res_cap = 0;
 };
@@ -124,8 +124,8 @@ struct pwmsvc {
         for (auto& c : cls) {
             dfree(c.dT);
             dfree(c.d_slots);
-            dfree(c.tile_part);
-            dfree(c.red_part);
+            dfree(c.tile_slot);
+            dfree(c.row_part);
             dfree(c.res_part);
         }
         dfree(d_states);
@@ -190,7 +190,7 @@ int rebuild_tables(pwmsvc* S) {
     for (int c = 0; c < kNumCls; ++c) {
         ClassDev& D = S->cls[c];
         std::vector<BatchSlot> hs;
-        int tiles = 0, red = 0, res = 0;
+        int tiles = 0, fix = 0, rows = 0;
         for (Req* r : S->live) {
             if (r->cls != c) continue;
             pwmgpu_matrix* m = r->m;
@@ -207,14 +207,14 @@ int rebuild_tables(pwmsvc* S) {
             b.nor = m->M.nor;
             b.nsub = m->P.nsub;
             b.tile0 = tiles;
-            b.nred = (b.nsub + kRedTiles - 1) / kRedTiles;
-            b.red0 = red;
-            b.nres = (b.nor + kResRows - 1) / kResRows;
-            b.res0 = res;
+            b.nfix = (b.nsub + kFixTiles - 1) / kFixTiles;
+            b.fix0 = fix;
+            b.nrow = (b.nor + kRowChunk - 1) / kRowChunk;
+            b.row0 = rows;
             b.state = r->slot;
             tiles += b.nsub;
-            red += b.nred;
-            res += b.nres;
+            fix += b.nfix;
+            rows += b.nrow;
             hs.push_back(b);
         }
         if (D.slots_cap < hs.size() || !D.d_slots) {
@@ -223,25 +223,32 @@ int rebuild_tables(pwmsvc* S) {
             TRY(dalloc(&D.d_slots, std::max<size_t>(hs.size(), 64)));
             D.slots_cap = std::max<size_t>(hs.size(), 64);
         }
-        TRY(grow(&D.tile_part, &D.tile_cap, 2 * (size_t)tiles + 2));
-        TRY(grow(&D.red_part, &D.red_cap, 2 * (size_t)red + 2));
-        TRY(grow(&D.res_part, &D.res_cap, (size_t)res + 1));
+        if (D.slot_cap < (size_t)tiles + 1 || !D.tile_slot) {
+            dfree(D.tile_slot);
+            D.slot_cap = 0;
+            const size_t cap = std::max<size_t>((size_t)tiles + 1, 2 * D.slot_cap);
+            TRY(dalloc(&D.tile_slot, cap));
+            D.slot_cap = cap;
+        }
+        TRY(grow(&D.row_part, &D.row_cap, 2 * (size_t)rows + 2));
+        TRY(grow(&D.res_part, &D.res_cap, (size_t)rows + 1));
         if (!hs.empty())
             CU(cudaMemcpyAsync(D.d_slots, hs.data(), hs.size() * sizeof(BatchSlot), cudaMemcpyHostToDevice,
                                S->stream));
         BatchTable T{};
         T.nslots = (int)hs.size();
         T.ntiles = tiles;
-        T.nred = red;
-        T.nres = res;
+        T.nfix = fix;
+        T.nrow = rows;
         T.slots = D.d_slots;
         T.states = S->d_states;
-        T.tile_part = D.tile_part;
-        T.red_part = D.red_part;
+        T.tile_slot = D.tile_slot;
+        T.row_part = D.row_part;
         T.res_part = D.res_part;
         T.status = S->d_status;
         // pageable source: the copy is staged before the call returns
         CU(cudaMemcpyAsync(D.dT, &T, sizeof T, cudaMemcpyHostToDevice, S->stream));
+        CU(launch_tile_slots(D.dT, T.nslots, S->stream));
         CU(cudaStreamSynchronize(S->stream));
     }
     S->dirty = false;
@@ -355,7 +362,7 @@ int after_round(pwmsvc* S, int* finished) {
             // mixed: leave the low-precision phase at the switch residual, when
             // it stops falling, or when only the FP64 reserve is left
             const int reserve = std::max(2, std::min(64, q.max_it / 4));
-            const bool stalled = r->rounds_in_phase >= 2 && r->rel >= 0.7 * r->prev_rel;
+            const bool stalled = r->rounds_in_phase >= 2 && low_precision_floor(r->rel, r->prev_rel);
             if (r->rel <= std::max(q.tol, kSvcSwitchRel) || stalled || r->iterations >= q.max_it - reserve) {
                 pwmgpu_matrix* m = r->m;
                 float* newest = (st.k & 1) ? m->fy : m->fx;
