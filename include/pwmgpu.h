@@ -178,6 +178,38 @@ int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nnz, const in
                                  const int32_t* col_ind, const double* vals, const double* x, double* y,
                                  void* stream);
 
+/* The CSB arrays of a PWMGPU_FMT_CSB handle, as CSB.hpp:464-567 builds them
+ * (for checks against the reference): beta, block bits, horizontal and
+ * vertical block counts, then ind[nnz] (local row << 16 | local column),
+ * data[nnz], blk_ptr[hb * vb + 1] (block_row * hb + block_col). */
+int pwmgpu_csb_info(const pwmgpu_matrix* m, int32_t* beta, int32_t* block_bits, int32_t* hb, int32_t* vb,
+                    int64_t* nnz);
+int pwmgpu_get_csb(pwmgpu_matrix* m, uint32_t* ind, double* data, int32_t* blk_ptr);
+/* The CO-H arrays of a PWMGPU_FMT_COH handle, as BlockCOH.hpp:319-455 builds
+ * them for `partitions` threads: part_info[9 * partitions] = {first row,
+ * beta, block bits, hb, vb, nnz, blocks, row jumps, block-row jumps} per
+ * partition, then the concatenated row_jump, col_jump[nnz], data[nnz],
+ * block_nnz[blocks], row_jump_block, col_jump_block[blocks]. */
+int pwmgpu_coh_info(const pwmgpu_matrix* m, int32_t* partitions, int64_t* row_jumps, int64_t* blocks,
+                    int64_t* block_row_jumps, int64_t* nnz);
+int pwmgpu_get_coh(pwmgpu_matrix* m, int32_t* part_info, uint16_t* row_jump, uint16_t* col_jump, double* data,
+                   int32_t* block_nnz, int16_t* row_jump_block, int16_t* col_jump_block);
+
+/* Host-side format builders (no device work), the constructions of
+ * CSB.hpp:96-113,464-567 and BlockCOH.hpp:319-455 from CRS arrays.  CSB:
+ * pwmgpu_csb_params gives beta and the block bits (blk_ptr holds
+ * ceil(noc/beta) * ceil(nor/beta) + 1 entries).  CO-H: every output array has
+ * room for nnz entries (part_info for 9 * threads); the counts come back in
+ * partitions, row_jumps, blocks and block_row_jumps. */
+int pwmgpu_csb_params(int32_t nor, int32_t noc, int32_t* beta, int32_t* block_bits);
+int pwmgpu_csb_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                          const double* vals, uint32_t* ind, double* data, int32_t* blk_ptr);
+int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                          const double* vals, int32_t threads, int32_t* partitions, int64_t* row_jumps,
+                          int64_t* blocks, int64_t* block_row_jumps, int32_t* part_info, uint16_t* row_jump,
+                          uint16_t* col_jump, double* data, int32_t* block_nnz, int16_t* row_jump_block,
+                          int16_t* col_jump_block);
+
 /* Tile size (merge items per tile) and tile count used by the SpMV kernel. */
 int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid);
 

@@ -60,6 +60,16 @@ SIGNATURES = {
     "pwmgpu_solve": (C.c_int, [vp, vp, i32, C.c_double, C.c_int, C.POINTER(SolveInfo)]),
     "pwmgpu_merge_partition": (C.c_int, [vp, i32, vp]),
     "pwmgpu_tile_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "pwmgpu_csb_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                                  C.POINTER(i64)]),
+    "pwmgpu_get_csb": (C.c_int, [vp, vp, vp, vp]),
+    "pwmgpu_coh_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
+                                  C.POINTER(i64)]),
+    "pwmgpu_get_coh": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "pwmgpu_csb_params": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
+    "pwmgpu_csb_build_host": (C.c_int, [i32, i32, i64, vp, vp, vp, vp, vp, vp]),
+    "pwmgpu_coh_build_host": (C.c_int, [i32, i32, i64, vp, vp, vp, i32, C.POINTER(i32), C.POINTER(i64),
+                                        C.POINTER(i64), C.POINTER(i64), vp, vp, vp, vp, vp, vp, vp]),
     "pwmgpu_mv_csr_device_noalloc": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp]),
 }
 

@@ -87,6 +87,13 @@ __device__ __forceinline__ uint64_t policy_evict_first() {
     return pol;
 }
 
+// Default L2 policy (for data other CTAs read again, like x windows).
+__device__ __forceinline__ uint64_t policy_evict_normal() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
 // 1D bulk copy global -> shared (TMA engine).  dst, src 16-byte aligned, bytes
 // a non-zero multiple of 16.  Completion is signalled on `bar`.
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar,

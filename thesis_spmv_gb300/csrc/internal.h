@@ -118,6 +118,26 @@ cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_c
 cudaError_t launch_tile_slots(const BatchTable* T, int nslots, cudaStream_t st);
 cudaError_t launch_fill_uniform(double* x, int n, uint64_t seed, int sm_count, cudaStream_t st);
 
+// csb.cu: CSB (CSB.hpp) parameters, host build and SpMV
+void csb_params(int nor, int noc, int* beta, int* bits);
+int csb_window(int nor, int beta, int sm_count);
+int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,
+                   int beta, int bits, std::vector<uint32_t>& ind, std::vector<double>& data,
+                   std::vector<int32_t>& blk_ptr, int S, std::vector<int>& win_ptr, std::vector<int>& unit_data);
+cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* win_ptr, const int* units, int nwin,
+                            int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
+                            int sm_count, cudaStream_t st);
+
+// coh.cu: CO-H (BlockCOH.hpp) host build and SpMV
+int coh_build_host(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,
+                   int threads, std::vector<int32_t>& part_info, std::vector<uint16_t>& row_jump,
+                   std::vector<uint16_t>& col_jump, std::vector<double>& data, std::vector<int32_t>& block_nnz,
+                   std::vector<int16_t>& row_jump_block, std::vector<int16_t>& col_jump_block,
+                   std::vector<int>& parts, std::vector<int>& blocks);
+cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, const uint16_t* row_jump,
+                            const uint16_t* col_jump, const double* data, const double* x, double* y,
+                            const double* nsq_in, int sm_count, cudaStream_t st);
+
 // Record the calling thread's last error message (pwmgpu_last_error).
 void record_error(const char* msg);
 

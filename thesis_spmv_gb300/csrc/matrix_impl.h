@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "internal.h"
 #include "pwmgpu.h"
@@ -92,6 +93,33 @@ struct pwmgpu_matrix {
     unsigned int* barrier = nullptr;  // grid barrier words of the persistent kernel
     double* hres = nullptr;           // pinned host copy of a solve chunk's results
 
+    // CSB format (csb.cu): the reference's arrays plus the window / unit plan
+    struct {
+        int beta = 0, bits = 0, hb = 0, vb = 0, S = 0, nwin = 0;
+        uint32_t* ind = nullptr;
+        double* data = nullptr;
+        int32_t* blk_ptr = nullptr;
+        int* win_ptr = nullptr;
+        int* units = nullptr;
+        std::vector<uint32_t> h_ind;
+        std::vector<double> h_data;
+        std::vector<int32_t> h_blk_ptr;
+    } csb;
+    // CO-H format (coh.cu): the reference's arrays plus partition / block tables
+    struct {
+        int parts = 0;
+        long long nblocks = 0;
+        int* d_parts = nullptr;
+        int* d_blocks = nullptr;
+        uint16_t* row_jump = nullptr;
+        uint16_t* col_jump = nullptr;
+        double* data = nullptr;
+        std::vector<int32_t> part_info, block_nnz;
+        std::vector<uint16_t> h_row_jump, h_col_jump;
+        std::vector<double> h_data;
+        std::vector<int16_t> row_jump_block, col_jump_block;
+    } coh;
+
     // host-facing vector buffers
     double* dx = nullptr;
     double* dy = nullptr;
@@ -111,6 +139,18 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(P.valp);
         P = MliPlan();
         pwmgpu::dfree(val32);
+        pwmgpu::dfree(csb.ind);
+        pwmgpu::dfree(csb.data);
+        pwmgpu::dfree(csb.blk_ptr);
+        pwmgpu::dfree(csb.win_ptr);
+        pwmgpu::dfree(csb.units);
+        csb = decltype(csb)();
+        pwmgpu::dfree(coh.d_parts);
+        pwmgpu::dfree(coh.d_blocks);
+        pwmgpu::dfree(coh.row_jump);
+        pwmgpu::dfree(coh.col_jump);
+        pwmgpu::dfree(coh.data);
+        coh = decltype(coh)();
         if (valbf) cudaFree(valbf);
         valbf = nullptr;
         bf16_exact = -1;

@@ -69,7 +69,81 @@ namespace {
 // arrays are released afterwards; row_start stays (fix-up, general path).
 }  // namespace
 namespace pwmgpu {
+// CSB / CO-H formats: build the format's arrays on the host from the CRS
+// arrays (which stay on the device for pwmgpu_get_csr), upload them.
+int build_format(pwmgpu_matrix* m) {
+    const int nor = m->M.nor, noc = m->M.noc;
+    const long long nnz = m->M.nnz;
+    std::vector<int32_t> rs((size_t)nor + 1), ci((size_t)std::max(nnz, 1LL));
+    std::vector<double> va((size_t)std::max(nnz, 1LL));
+    CU(cudaMemcpyAsync(rs.data(), m->M.row_start, sizeof(int32_t) * ((size_t)nor + 1), cudaMemcpyDeviceToHost,
+                       m->stream));
+    if (nnz > 0) {
+        CU(cudaMemcpyAsync(ci.data(), m->M.col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToHost, m->stream));
+        CU(cudaMemcpyAsync(va.data(), m->M.val, sizeof(double) * (size_t)nnz, cudaMemcpyDeviceToHost, m->stream));
+    }
+    CU(cudaStreamSynchronize(m->stream));
+    if (m->format == PWMGPU_FMT_CSB) {
+        auto& c = m->csb;
+        csb_params(std::max(nor, 1), std::max(noc, 1), &c.beta, &c.bits);
+        c.hb = (noc + c.beta - 1) / c.beta;
+        c.vb = (nor + c.beta - 1) / c.beta;
+        c.S = csb_window(nor, c.beta, m->sm_count);
+        c.nwin = (nor + c.S - 1) / c.S;
+        std::vector<int> win_ptr, units;
+        csb_build_host(nor, noc, nnz, rs.data(), ci.data(), va.data(), c.beta, c.bits, c.h_ind, c.h_data,
+                       c.h_blk_ptr, c.S, win_ptr, units);
+        TRY(dalloc(&c.ind, (size_t)nnz + 4));
+        TRY(dalloc(&c.data, (size_t)nnz + 4));
+        TRY(dalloc(&c.blk_ptr, c.h_blk_ptr.size()));
+        TRY(dalloc(&c.win_ptr, win_ptr.size()));
+        TRY(dalloc(&c.units, units.size() + 4));
+        if (nnz > 0) {
+            CU(cudaMemcpyAsync(c.ind, c.h_ind.data(), sizeof(uint32_t) * (size_t)nnz, cudaMemcpyHostToDevice,
+                               m->stream));
+            CU(cudaMemcpyAsync(c.data, c.h_data.data(), sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice,
+                               m->stream));
+        }
+        CU(cudaMemcpyAsync(c.blk_ptr, c.h_blk_ptr.data(), sizeof(int32_t) * c.h_blk_ptr.size(),
+                           cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(c.win_ptr, win_ptr.data(), sizeof(int) * win_ptr.size(), cudaMemcpyHostToDevice,
+                           m->stream));
+        if (!units.empty())
+            CU(cudaMemcpyAsync(c.units, units.data(), sizeof(int) * units.size(), cudaMemcpyHostToDevice, m->stream));
+    } else {
+        auto& c = m->coh;
+        std::vector<int> parts, blocks;
+        c.parts = coh_build_host(nor, noc, nnz, rs.data(), ci.data(), va.data(), m->partitions, c.part_info,
+                                 c.h_row_jump, c.h_col_jump, c.h_data, c.block_nnz, c.row_jump_block,
+                                 c.col_jump_block, parts, blocks);
+        c.nblocks = (long long)c.block_nnz.size();
+        TRY(dalloc(&c.d_parts, parts.size()));
+        TRY(dalloc(&c.d_blocks, blocks.size() + 8));
+        TRY(dalloc(&c.row_jump, c.h_row_jump.size() + 8));
+        TRY(dalloc(&c.col_jump, c.h_col_jump.size() + 8));
+        TRY(dalloc(&c.data, c.h_data.size() + 4));
+        CU(cudaMemcpyAsync(c.d_parts, parts.data(), sizeof(int) * parts.size(), cudaMemcpyHostToDevice, m->stream));
+        if (!blocks.empty())
+            CU(cudaMemcpyAsync(c.d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+        if (!c.h_row_jump.empty())
+            CU(cudaMemcpyAsync(c.row_jump, c.h_row_jump.data(), sizeof(uint16_t) * c.h_row_jump.size(),
+                               cudaMemcpyHostToDevice, m->stream));
+        if (!c.h_col_jump.empty())
+            CU(cudaMemcpyAsync(c.col_jump, c.h_col_jump.data(), sizeof(uint16_t) * c.h_col_jump.size(),
+                               cudaMemcpyHostToDevice, m->stream));
+        if (!c.h_data.empty())
+            CU(cudaMemcpyAsync(c.data, c.h_data.data(), sizeof(double) * c.h_data.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+    }
+    CU(cudaStreamSynchronize(m->stream));
+    TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)2 * dot_grid(m->M.nor, m->sm_count) + 64));
+    m->loaded = true;
+    return PWMGPU_OK;
+}
+
 int build_plan(pwmgpu_matrix* m) {
+    if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
     const long long total = (long long)m->M.nor + m->M.nnz;
     const MergeGeom g = merge_geometry(m->cfg);
     m->tm = g.wm;
@@ -154,7 +228,23 @@ int check_sizes(long long nor, long long noc, long long nnz) {
 }  // namespace pwmgpu
 namespace {
 
+// y = 2^e(nsq_in) A x with the CSB or CO-H kernel (nsq_in null: e = 0).
+int spmv_format(pwmgpu_matrix* m, const double* dx, double* dy, const double* nsq_in) {
+    if (m->M.nor == 0) return PWMGPU_OK;
+    if (m->format == PWMGPU_FMT_CSB) {
+        const auto& c = m->csb;
+        CU(launch_csb_spmv(c.ind, c.data, c.win_ptr, c.units, c.nwin, c.S, m->M.nor, m->M.noc, dx, dy, nsq_in,
+                           m->status, m->sm_count, m->stream));
+    } else {
+        const auto& c = m->coh;
+        CU(launch_coh_spmv(c.d_parts, c.parts, c.d_blocks, c.row_jump, c.col_jump, c.data, dx, dy, nsq_in,
+                           m->sm_count, m->stream));
+    }
+    return PWMGPU_OK;
+}
+
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
+    if (m->format != PWMGPU_FMT_MERGE) return spmv_format(m, dx, dy, nullptr);
     if (m->num_tiles == 0) return PWMGPU_OK;
     CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, m->status,
                          m->stream));
@@ -183,6 +273,21 @@ bool use_fused(const pwmgpu_matrix* m, int pgrid) {
 int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
     if (it <= 0 || m->M.nor == 0) return PWMGPU_OK;
     TRY(ensure_nsq(m, (size_t)it + 1));
+    if (m->format != PWMGPU_FMT_MERGE) {
+        // the format's SpMV (with the rescale) and the row-pass norm per step
+        for (int k = 0; k < it; ++k) {
+            const double* in = (k % 2 == 0) ? dx : dy;
+            double* out = (k % 2 == 0) ? dy : dx;
+            TRY(spmv_format(m, in, out, k ? m->nsq + k : nullptr));
+            CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, m->nsq + k + 1,
+                                     dot_grid(m->M.nor, m->sm_count), m->stream));
+        }
+        double* last = (it % 2 == 1) ? dy : dx;
+        double* prev = (it % 2 == 1) ? dx : dy;
+        CU(launch_power_finalize_f64(last, m->nsq + it, it >= 2 ? prev : nullptr, m->nsq + it - 1, m->M.nor,
+                                     m->sm_count, m->stream));
+        return PWMGPU_OK;
+    }
     if (m->power_mode == PWMGPU_POWER_FUSED && m->pgrid == 0)
         return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident on this device");
     if (use_fused(m, m->pgrid)) {
@@ -643,7 +748,11 @@ int pwmgpu_get_csr(pwmgpu_matrix* m, int32_t* row_start, int32_t* col_ind, doubl
     if (!row_start || (m->M.nnz > 0 && (!col_ind || !vals))) return fail(PWMGPU_ERR_INVALID, "null output array");
     CU(cudaMemcpyAsync(row_start, m->M.row_start, sizeof(int32_t) * ((size_t)m->M.nor + 1), cudaMemcpyDeviceToHost,
                        m->stream));
-    if (m->M.nnz > 0) {
+    if (m->M.nnz > 0 && m->format != PWMGPU_FMT_MERGE) {
+        // the CSB / CO-H handles keep the CRS arrays
+        CU(cudaMemcpyAsync(col_ind, m->M.col, sizeof(int32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+        CU(cudaMemcpyAsync(vals, m->M.val, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+    } else if (m->M.nnz > 0) {
         // back from the lane-interleaved storage to CRS order
         int32_t* dc = nullptr;
         double* dv = nullptr;
@@ -738,6 +847,7 @@ int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* n
 int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
     if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_UNSUPPORTED, "FP32 SpMV runs on the merge format");
     if (m->M.nor > 0 && (!dx || !dy)) return fail(PWMGPU_ERR_INVALID, "null vector");
     if (m->num_tiles == 0) return PWMGPU_OK;
     int cfg = kCfgF32, pg = 0;
@@ -770,8 +880,137 @@ int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int pr
         return fail(PWMGPU_ERR_INVALID, "unknown precision %d", precision);
     if (m->power_mode == PWMGPU_POWER_MULTI)
         return fail(PWMGPU_ERR_UNSUPPORTED, "the solve runs on the fused power kernel only");
+    if (m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_UNSUPPORTED, "the solve runs on the merge format");
     std::memset(info, 0, sizeof *info);
     return solve(m, x, max_it, tol, precision, info);
+}
+
+int pwmgpu_csb_info(const pwmgpu_matrix* m, int32_t* beta, int32_t* block_bits, int32_t* hb, int32_t* vb,
+                    int64_t* nnz) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded || m->format != PWMGPU_FMT_CSB) return fail(PWMGPU_ERR_STATE, "no CSB matrix loaded");
+    if (beta) *beta = m->csb.beta;
+    if (block_bits) *block_bits = m->csb.bits;
+    if (hb) *hb = m->csb.hb;
+    if (vb) *vb = m->csb.vb;
+    if (nnz) *nnz = m->M.nnz;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_get_csb(pwmgpu_matrix* m, uint32_t* ind, double* data, int32_t* blk_ptr) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded || m->format != PWMGPU_FMT_CSB) return fail(PWMGPU_ERR_STATE, "no CSB matrix loaded");
+    const auto& c = m->csb;
+    if (!blk_ptr || (m->M.nnz > 0 && (!ind || !data))) return fail(PWMGPU_ERR_INVALID, "null output array");
+    if (m->M.nnz > 0) {
+        CU(cudaMemcpyAsync(ind, c.ind, sizeof(uint32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+        CU(cudaMemcpyAsync(data, c.data, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+    }
+    CU(cudaMemcpyAsync(blk_ptr, c.blk_ptr, sizeof(int32_t) * c.h_blk_ptr.size(), cudaMemcpyDeviceToHost, m->stream));
+    CU(cudaStreamSynchronize(m->stream));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_coh_info(const pwmgpu_matrix* m, int32_t* partitions, int64_t* row_jumps, int64_t* blocks,
+                    int64_t* block_row_jumps, int64_t* nnz) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded || m->format != PWMGPU_FMT_COH) return fail(PWMGPU_ERR_STATE, "no CO-H matrix loaded");
+    const auto& c = m->coh;
+    if (partitions) *partitions = c.parts;
+    if (row_jumps) *row_jumps = (int64_t)c.h_row_jump.size();
+    if (blocks) *blocks = c.nblocks;
+    if (block_row_jumps) *block_row_jumps = (int64_t)c.row_jump_block.size();
+    if (nnz) *nnz = m->M.nnz;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_get_coh(pwmgpu_matrix* m, int32_t* part_info, uint16_t* row_jump, uint16_t* col_jump, double* data,
+                   int32_t* block_nnz, int16_t* row_jump_block, int16_t* col_jump_block) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded || m->format != PWMGPU_FMT_COH) return fail(PWMGPU_ERR_STATE, "no CO-H matrix loaded");
+    const auto& c = m->coh;
+    if (!part_info) return fail(PWMGPU_ERR_INVALID, "null output array");
+    auto put = [](auto* dst, const auto& v) {
+        if (dst && !v.empty()) std::memcpy(dst, v.data(), sizeof(v[0]) * v.size());
+    };
+    put(part_info, c.part_info);
+    // the device copies are the ones the kernel reads: return those
+    if (row_jump && !c.h_row_jump.empty())
+        CU(cudaMemcpyAsync(row_jump, c.row_jump, sizeof(uint16_t) * c.h_row_jump.size(), cudaMemcpyDeviceToHost,
+                           m->stream));
+    if (col_jump && !c.h_col_jump.empty())
+        CU(cudaMemcpyAsync(col_jump, c.col_jump, sizeof(uint16_t) * c.h_col_jump.size(), cudaMemcpyDeviceToHost,
+                           m->stream));
+    if (data && !c.h_data.empty())
+        CU(cudaMemcpyAsync(data, c.data, sizeof(double) * c.h_data.size(), cudaMemcpyDeviceToHost, m->stream));
+    CU(cudaStreamSynchronize(m->stream));
+    put(block_nnz, c.block_nnz);
+    put(row_jump_block, c.row_jump_block);
+    put(col_jump_block, c.col_jump_block);
+    return PWMGPU_OK;
+}
+
+int pwmgpu_csb_params(int32_t nor, int32_t noc, int32_t* beta, int32_t* block_bits) {
+    if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    int b = 0, bits = 0;
+    csb_params(nor, noc, &b, &bits);
+    if (beta) *beta = b;
+    if (block_bits) *block_bits = bits;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_csb_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                          const double* vals, uint32_t* ind, double* data, int32_t* blk_ptr) {
+    TRY(check_sizes(nor, noc, nnz));
+    if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    if (!row_start || !blk_ptr || (nnz > 0 && (!col_ind || !vals || !ind || !data)))
+        return fail(PWMGPU_ERR_INVALID, "null array");
+    int beta = 0, bits = 0;
+    csb_params(nor, noc, &beta, &bits);
+    std::vector<uint32_t> vi;
+    std::vector<double> vd;
+    std::vector<int32_t> vb;
+    std::vector<int> wp, un;
+    csb_build_host(nor, noc, nnz, row_start, col_ind, vals, beta, bits, vi, vd, vb, std::min(beta, 1024), wp, un);
+    if (nnz > 0) {
+        std::memcpy(ind, vi.data(), sizeof(uint32_t) * (size_t)nnz);
+        std::memcpy(data, vd.data(), sizeof(double) * (size_t)nnz);
+    }
+    std::memcpy(blk_ptr, vb.data(), sizeof(int32_t) * vb.size());
+    return PWMGPU_OK;
+}
+
+int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                          const double* vals, int32_t threads, int32_t* partitions, int64_t* row_jumps,
+                          int64_t* blocks, int64_t* block_row_jumps, int32_t* part_info, uint16_t* row_jump,
+                          uint16_t* col_jump, double* data, int32_t* block_nnz, int16_t* row_jump_block,
+                          int16_t* col_jump_block) {
+    TRY(check_sizes(nor, noc, nnz));
+    if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    if (!row_start || !part_info || (nnz > 0 && (!col_ind || !vals)))
+        return fail(PWMGPU_ERR_INVALID, "null array");
+    std::vector<int32_t> pi, bn;
+    std::vector<uint16_t> rj, cj;
+    std::vector<double> d;
+    std::vector<int16_t> rjb, cjb;
+    std::vector<int> parts, blks;
+    const int T = coh_build_host(nor, noc, nnz, row_start, col_ind, vals, std::max(threads, 1), pi, rj, cj, d, bn,
+                                 rjb, cjb, parts, blks);
+    if (partitions) *partitions = T;
+    if (row_jumps) *row_jumps = (int64_t)rj.size();
+    if (blocks) *blocks = (int64_t)bn.size();
+    if (block_row_jumps) *block_row_jumps = (int64_t)rjb.size();
+    auto put = [](auto* dst, const auto& v) {
+        if (dst && !v.empty()) std::memcpy(dst, v.data(), sizeof(v[0]) * v.size());
+    };
+    put(part_info, pi);
+    put(row_jump, rj);
+    put(col_jump, cj);
+    put(data, d);
+    put(block_nnz, bn);
+    put(row_jump_block, rjb);
+    put(col_jump_block, cjb);
+    return PWMGPU_OK;
 }
 
 }  // extern "C"

@@ -238,6 +238,40 @@ class CudaSparseMatrix:
         return a.value, b.value, c.value
 
 
+    def getCSB(self):
+        """The CSB arrays (CSB.hpp:464-567) of a CSBCuda handle: dict(ind,
+        data, blk_ptr, beta, block_bits, hb, vb)."""
+        L = _lib.lib()
+        beta, bits, hb, vb, nnz = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
+        check(L.pwmgpu_csb_info(self._h, C.byref(beta), C.byref(bits), C.byref(hb), C.byref(vb), C.byref(nnz)),
+              "pwmgpu_csb_info")
+        ind = np.zeros(max(nnz.value, 1), np.uint32)
+        data = np.zeros(max(nnz.value, 1), _F64)
+        blk = np.zeros(hb.value * vb.value + 1, _I32)
+        check(L.pwmgpu_get_csb(self._h, _ptr(ind), _ptr(data), _ptr(blk)), "pwmgpu_get_csb")
+        return dict(ind=ind[:nnz.value], data=data[:nnz.value], blk_ptr=blk, beta=beta.value,
+                    block_bits=bits.value, hb=hb.value, vb=vb.value)
+
+    def getCOH(self):
+        """The CO-H arrays (BlockCOH.hpp:319-455) of a COHCuda handle."""
+        L = _lib.lib()
+        T, nrj, nblk, nrjb, nnz = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(L.pwmgpu_coh_info(self._h, C.byref(T), C.byref(nrj), C.byref(nblk), C.byref(nrjb), C.byref(nnz)),
+              "pwmgpu_coh_info")
+        part = np.zeros(9 * T.value, _I32)
+        rj = np.zeros(max(nrj.value, 1), np.uint16)
+        cj = np.zeros(max(nnz.value, 1), np.uint16)
+        d = np.zeros(max(nnz.value, 1), _F64)
+        bn = np.zeros(max(nblk.value, 1), _I32)
+        rjb = np.zeros(max(nrjb.value, 1), np.int16)
+        cjb = np.zeros(max(nblk.value, 1), np.int16)
+        check(L.pwmgpu_get_coh(self._h, _ptr(part), _ptr(rj), _ptr(cj), _ptr(d), _ptr(bn), _ptr(rjb), _ptr(cjb)),
+              "pwmgpu_get_coh")
+        return dict(threads=T.value, part_info=part, row_jump=rj[:nrj.value], col_jump=cj[:nnz.value],
+                    data=d[:nnz.value], block_nnz=bn[:nblk.value], row_jump_block=rjb[:nrjb.value],
+                    col_jump_block=cjb[:nblk.value])
+
+
 class CRSCuda(CudaSparseMatrix):
     """Merge-path CRS on the GPU (drop-in beside CRS_Merge, method 12)."""
     FORMAT = FMT_MERGE
