@@ -189,6 +189,14 @@ def run_reference(args, world, rank):
     }))
 
 
+def coh_partitions(n, nnz, sm_count):
+    """CO-H partition count (the reference's thread count) for the GPU: a warp
+    per partition, at least 32 per SM, and about 2000 rows each on average so
+    most partitions fit their warp's 2048-row shared-memory window (nnz is
+    unused: more partitions mean more, emptier blocks)."""
+    return max(32 * sm_count, -(-n // 2000))
+
+
 IRREGULAR = dict(n=4194304, seed=20261203, length_dist=0, mean_len=16.0, sigma=1.2, max_len=20000,
                  band_permille=300, band_half=4096)
 
@@ -220,6 +228,25 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
     out = {"irregular": {"workload": "lognormal_rows_n4194304_mean16_sigma1.2_band30pct", "N": N, "nnz": nnz,
                          "spmv_ms": round(ms, 5), "spmv_gb_s": round(B / (ms * 1e-3) / 1e9, 2),
                          "frac_of_measured_hbm": round(B / (ms * 1e-3) / 1e9 / measured_peaks()[0], 4)}}
+    # the same matrix in the CSB and CO-H formats (the reference's methods 9 and
+    # 10): device SpMV time, GB/s on the CRS algorithmic bytes
+    rs, ci, dv = M.getCSR()
+    fm = {}
+    for name, cls in (("csb", pwm.CSBCuda), ("coh", pwm.COHCuda)):
+        F = cls(coh_partitions(N, nnz, torch.cuda.get_device_properties(dev).multi_processor_count))
+        F.set_stream(stream.cuda_stream)
+        F.loadCSR(N, N, rs, ci, dv)
+        for _ in range(3):
+            F.mv_device(x.data_ptr(), y.data_ptr())
+        e0.record(stream)
+        for _ in range(50):
+            F.mv_device(x.data_ptr(), y.data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        fms = e0.elapsed_time(e1) / 50
+        fm[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
+        del F
+    out["irregular"]["formats"] = fm
     x0 = np.random.default_rng(20261203).random(N)
     solves = {}
     lam = {}
@@ -466,6 +493,26 @@ def run_ours(args, world, rank, local):
     ms = ms_total / args.steps
     value = B * world / (ms * 1e-3) / 1e9
 
+    # ---- the same Poisson matrix in the CSB and CO-H formats ----
+    formats = {}
+    if not args.no_extra:
+        for name, cls in (("csb", pwm.CSBCuda), ("coh", pwm.COHCuda)):
+            F = cls(coh_partitions(N, nnz, torch.cuda.get_device_properties(dev).multi_processor_count))
+            F.set_stream(stream.cuda_stream)
+            F.generatePoissonMatrix(grid_side, grid_side, 1)
+            for _ in range(3):
+                F.mv_device(dx.data_ptr(), dy.data_ptr())
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(50):
+                F.mv_device(dx.data_ptr(), dy.data_ptr())
+            f1.record(stream)
+            f1.synchronize()
+            fms = f0.elapsed_time(f1) / 50
+            formats[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
+            del F
+
     # ---- power method: 500 iterations (reference powerIteration semantics),
     #      fused persistent kernel and two kernels per iteration ----
     p_it = args.power_iters
@@ -532,6 +579,8 @@ def run_ours(args, world, rank, local):
                             "kernels": "k_merge_spmv + k_merge_fixup per iteration"}},
         "clocks": clk.summary(),
     }
+    if formats:
+        result["formats_poisson"] = formats
     if extra:
         result.update(extra)
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -19,9 +19,11 @@
 // rows from a warp prefix sum of the row jumps, staged in shared memory).  A
 // lane accumulates its runs of equal rows with one FMA per nonzero; a run
 // that crosses lanes is summed by the lane where it starts (lane order) and
-// one crossing the chunk end is carried.  Rows are written by one lane at a
-// time and blocks in order: no atomics, a fixed summation order (per row,
-// Hilbert block order, as in the reference).
+// one crossing the chunk end is carried.  A partition of at most kCohWinRows
+// rows accumulates its rows in a shared-memory window (written to y once at
+// the end); a larger one adds into y directly.  Rows are written by one lane
+// at a time and blocks in order: no atomics, a fixed summation order (per
+// row, Hilbert block order, as in the reference).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,8 +40,9 @@ namespace pwmgpu {
 
 namespace {
 
-constexpr int kCohK = 8;      // elements per lane per chunk
-constexpr int kCohWarps = 4;  // warps per CTA
+constexpr int kCohK = 8;           // elements per lane per chunk
+constexpr int kCohWarps = 4;       // warps per CTA
+constexpr int kCohWinRows = 2048;  // rows of a warp's shared-memory y window
 
 // BlockCOH.hpp:79-114 rowColToHilbert: index of cell (row, col) on the
 // Hilbert curve over a size x size grid.
@@ -77,7 +80,9 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
     __shared__ int multi_s[kCohWarps][32];
     __shared__ int carry_row_s[kCohWarps];
     __shared__ double carry_s[kCohWarps];
+    extern __shared__ double ywin_s[];  // kCohWarps x kCohWinRows
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double* ywin = ywin_s + (size_t)w * kCohWinRows;
     int* rbuf = rbuf_s[w];
     int* frow = frow_s[w];
     int* crow = crow_s[w];
@@ -93,13 +98,15 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
         const int nb = __ldg(&parts[2 * p + 1].x);
         const int trs = pa.x, nrows = pa.y, bits = pa.z, b0 = pa.w;
         const int beta = 1 << bits;
-        for (int r = lane; r < nrows; r += 32) y[trs + r] = 0.0;
+        const bool win = nrows <= kCohWinRows;
+        double* yp = win ? ywin : y + trs;  // the partition's rows
+        for (int r = lane; r < nrows; r += 32) yp[r] = 0.0;
         __syncwarp();
         for (int b = b0; b < b0 + nb; ++b) {
             // blocks[2b] = {block row, block col, first element, first row jump}, blocks[2b+1].x = nnz
             const int4 ba = __ldg(blocks + 2 * b);
             const int n = __ldg(&blocks[2 * b + 1].x);
-            double* yb = y + trs + (long long)ba.x * beta;
+            double* yb = yp + (long long)ba.x * beta;
             const double* xb = x + (long long)ba.y * beta;
             const long long eb = ba.z;
             const uint16_t* rj = row_jump + ba.w;
@@ -230,6 +237,9 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
             if (lane == 0 && carry_row >= 0) yb[carry_row] = yb[carry_row] + (e != 0 ? scale_pow2(carry, e) : carry);
             __syncwarp();
         }
+        if (win)
+            for (int r = lane; r < nrows; r += 32) y[trs + r] = ywin[r];
+        __syncwarp();
     }
 }
 
@@ -402,9 +412,15 @@ cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, con
                             const uint16_t* col_jump, const double* data, const double* x, double* y,
                             const double* nsq_in, int sm_count, cudaStream_t st) {
     if (nparts <= 0) return cudaSuccess;
+    constexpr int kWinBytes = kCohWarps * kCohWinRows * (int)sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_coh_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kWinBytes);
+        attr = true;
+    }
     long long grid = (nparts + kCohWarps - 1) / kCohWarps;
     if (grid > (long long)sm_count * 16) grid = (long long)sm_count * 16;
-    k_coh_spmv<<<(int)grid, 32 * kCohWarps, 0, st>>>(reinterpret_cast<const int4*>(parts), nparts,
+    k_coh_spmv<<<(int)grid, 32 * kCohWarps, kWinBytes, st>>>(reinterpret_cast<const int4*>(parts), nparts,
                                                     reinterpret_cast<const int4*>(blocks), row_jump, col_jump, data,
                                                     x, y, nsq_in);
     return cudaGetLastError();

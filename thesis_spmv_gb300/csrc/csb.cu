@@ -11,11 +11,14 @@
 // block inside an aligned S x S sub-square form one contiguous range.  Rows
 // are cut into windows of S rows; one CTA owns a window: it zeroes an S-row
 // y window in shared memory, walks its sub-squares ("units": every block of
-// the block row, every column window), stages each unit's S-column x window
-// in shared memory with a TMA bulk copy (double-buffered, mbarriers), adds
-// each element's product into the y window (shared-memory atomics), and
-// finally writes its rows of y once.  x is reused from shared memory, y is
-// written once per row, and no CTA touches another's rows.  The summation
+// the block row, every column window) and adds each element's product into
+// the y window (shared-memory atomics), then writes its rows of y once.
+// Dense units (at least kDenseUnit elements) stage their S-column x window in
+// shared memory with a TMA bulk copy (double-buffered, mbarriers) and are
+// taken by the whole CTA; sparse units (a random matrix's blocks hold a few
+// elements each) are taken one per warp, gathering x through L1/L2 -- staging
+// 8 KB of x for a handful of elements would cost more than it saves.  y is
+// written once per row and no CTA touches another's rows.  The summation
 // order within a row follows the order the atomics land in (the per-row
 // error bound holds for any order).
 #include <cuda_runtime.h>
@@ -35,6 +38,7 @@ namespace {
 
 constexpr int kCsbNT = 256;
 constexpr int kCsbMaxS = 1024;
+constexpr int kDenseUnit = 256;  // elements from which a unit's x window is staged
 
 // Spread the low 16 bits of v to the even bit positions.
 inline uint64_t spread16(uint64_t v) {
@@ -55,6 +59,8 @@ struct Unit {
     int pad;
 };
 
+// win_ptr[2w] = the window's first unit, win_ptr[2w+1] = its first dense
+// unit, win_ptr[2w+2] = the next window's first unit.
 __global__ void __launch_bounds__(kCsbNT) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
                                                      const int* __restrict__ win_ptr, const int4* __restrict__ units,
                                                      int nwin, int S, int nor, int noc, const double* __restrict__ x,
@@ -90,10 +96,22 @@ __global__ void __launch_bounds__(kCsbNT) k_csb_spmv(const uint32_t* __restrict_
             if (tid == 0) mbar_arrive(&bar[b]);
         }
     };
+    const int lane = tid & 31, warp = tid >> 5;
     for (int w = blockIdx.x; w < nwin; w += gridDim.x) {
-        const int u0 = __ldg(win_ptr + w), u1 = __ldg(win_ptr + w + 1);
+        const int us = __ldg(win_ptr + 2 * w), u0 = __ldg(win_ptr + 2 * w + 1), u1 = __ldg(win_ptr + 2 * w + 2);
         for (int i = tid; i < S; i += kCsbNT) ys[i] = 0.0;
         if (u0 < u1) stage(u0, 0);
+        __syncthreads();  // ys zeroed
+        // sparse units: one per warp, x gathered through L1 / L2
+        for (int u = us + warp; u < u0; u += kCsbNT / 32) {
+            const int4 un = __ldg(units + u);
+            const double* xw = x + un.z;
+            for (int k = un.x + lane; k < un.y; k += 32) {
+                const uint32_t id = __ldg(ind + k);
+                const int r = (int)(id >> 16) & (S - 1), c = (int)(id & 0xFFFFu) & (S - 1);
+                atomicAdd(&ys[r], __ldg(data + k) * __ldg(xw + c));
+            }
+        }
         bool ok = true;
         for (int u = u0; u < u1; ++u) {
             const int b = (u - u0) & 1;
@@ -194,19 +212,22 @@ int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
     }
     for (auto& t : th) t.join();
     for (size_t b = 0; b + 1 < blk_ptr.size(); ++b) blk_ptr[b + 1] += blk_ptr[b];
-    win_ptr.assign((size_t)nwin + 1, 0);
-    for (int w = 0; w < nwin; ++w) win_ptr[(size_t)w + 1] = win_ptr[(size_t)w] + (int)units_per_win[(size_t)w].size();
-    unit_data.resize((size_t)win_ptr[(size_t)nwin] * 4);
+    // per window: sparse units first, then dense ones (win_ptr holds both starts)
+    win_ptr.assign(2 * (size_t)nwin + 1, 0);
+    unit_data.clear();
+    int o = 0;
     for (int w = 0; w < nwin; ++w) {
-        int o = win_ptr[(size_t)w];
-        for (const Unit& u : units_per_win[(size_t)w]) {
-            unit_data[(size_t)o * 4 + 0] = u.lo;
-            unit_data[(size_t)o * 4 + 1] = u.hi;
-            unit_data[(size_t)o * 4 + 2] = u.c0;
-            unit_data[(size_t)o * 4 + 3] = 0;
-            ++o;
+        win_ptr[2 * (size_t)w] = o;
+        for (int dense = 0; dense < 2; ++dense) {
+            if (dense) win_ptr[2 * (size_t)w + 1] = o;
+            for (const Unit& u : units_per_win[(size_t)w]) {
+                if ((u.hi - u.lo >= kDenseUnit) != (dense == 1)) continue;
+                unit_data.insert(unit_data.end(), {u.lo, u.hi, u.c0, 0});
+                ++o;
+            }
         }
     }
+    win_ptr[2 * (size_t)nwin] = o;
     return 0;
 }
 
