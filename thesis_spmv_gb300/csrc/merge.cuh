@@ -252,19 +252,22 @@ __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, c
 
     // ---- carries: the first lane of each run of lanes ending in the same
     //      row adds the run (lane order) to the row ----
-    crow[lane] = a;
+    // crow holds the lane's last row, with the top bit set when the lane's
+    // first row began before the lane (head_open): the leader of a run needs
+    // that flag of the lane completing the row, and reads it here instead of
+    // comparing row_start in global memory.
+    crow[lane] = a | (head_open && cnt > 0 ? (int)0x80000000u : 0);
     cval[lane] = acc;
     __syncwarp();
-    if (lane == 0 || crow[lane - 1] != a) {
+    if (lane == 0 || (crow[lane - 1] & 0x7fffffff) != a) {
         AT sum = acc;
         int u = lane + 1;
-        for (; u < 32 && crow[u] == a; ++u) sum += cval[u];
+        int cu = 0;
+        for (; u < 32 && ((cu = crow[u]) & 0x7fffffff) == a; ++u) sum += cval[u];
         if (a < rw1) {
             // Lane u completes row a.  If the row began before lane u, lane u
             // left its part in hval[u] and the total is written here.
-            const int rs_a = __ldg(row_start + a);
-            const int b0u = kw0 + u * qm + (u < rem ? u : rem);
-            if (rs_a < b0u) y[a] = (XT)(hval[u] + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+            if (cu < 0) y[a] = (XT)(hval[u] + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
         } else if (a < nor) {
             carries[s] = sum;  // a == rw1: the sub-tile's unfinished row
         }
