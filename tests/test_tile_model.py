@@ -6,8 +6,9 @@ sub-tiles of WM = 32*IPT items, one per warp; sub-tile s spans the nonzeros
 [kw0, kw1) and hands lane l the contiguous range [kw0 + start_l, + cnt_l)
 (qm = nkw // 32, rem = nkw % 32, cnt_l = qm + (l < rem)).  Each array is
 stored per sub-tile at an 8-element-aligned base so that element j of lane l
-sits at mli_pos(l, j, qm, V): full V-blocks first (one 16-byte vector load per
-lane per block, coalesced across the warp), then a compact scalar tail.
+sits at mli_pos(l, j, qm, V) with V = 1 (the kernel's lane_vec): slot j of
+all lanes contiguous, j * 32 + l, the partial last slot for lanes < rem only.
+The general V (16-byte blocks, then a scalar tail) is checked too.
 
 Checks: the permutation is a bijection into [base, base + nkw) and vector
 slots are 16-byte aligned; bases never overlap and stay inside the
@@ -21,6 +22,7 @@ import pytest
 from oracle import pyoracle as O
 
 BIG = 2 ** 31 - 1
+LANE_VEC = 1  # merge.cuh lane_vec<T>()
 
 
 def mli_pos(lane, j, qm, V):
@@ -89,7 +91,7 @@ def plan(A, IPT):
                     a += 1
                 if a < rw1 and b + 1 == rs[a + 1]:
                     m |= 1 << j
-                pv, pc = mli_pos(lane, j, qm, 2), mli_pos(lane, j, qm, 4)
+                pv, pc = mli_pos(lane, j, qm, LANE_VEC), mli_pos(lane, j, qm, LANE_VEC)
                 assert np.isnan(valp[base + pv]) and colp[base + pc] == -1
                 valp[base + pv] = A.data[b]
                 colp[base + pc] = A.col_ind[b]
@@ -116,8 +118,8 @@ def simulate(A, x, IPT):
         lanes = []
         for lane in range(32):
             b0, cnt, _, _ = lane_range(kw0, kw1, lane)
-            vv = [valp[base + mli_pos(lane, j, qm, 2)] if j < cnt else 0.0 for j in range(IPT)]
-            xv = [x[colp[base + mli_pos(lane, j, qm, 4)]] if j < cnt else 0.0 for j in range(IPT)]
+            vv = [valp[base + mli_pos(lane, j, qm, LANE_VEC)] if j < cnt else 0.0 for j in range(IPT)]
+            xv = [x[colp[base + mli_pos(lane, j, qm, LANE_VEC)]] if j < cnt else 0.0 for j in range(IPT)]
             lanes.append((b0, cnt, vv, xv, int(masks[s, lane])))
         # rows [rw0, fr) carry no nonzeros in this sub-tile
         for r in range(rw0, fr):
@@ -238,7 +240,7 @@ def test_layout(IPT, name):
             assert mli_base(sc[s + 1][1], s + 1) >= base + nkw  # no overlap
         qm = nkw >> 5
         assert (nkw + 31) >> 5 <= IPT
-        for V in (2, 4, 8):
+        for V in (1, 2, 4, 8):
             pos = sorted(mli_pos(l, j, qm, V) for l in range(32) for j in range(lane_range(kw0, kw1, l)[1]))
             assert pos == list(range(nkw))  # bijection onto [0, nkw)
             for l in range(32):

@@ -64,8 +64,8 @@ __global__ void k_mli_plan(const int32_t* __restrict__ row_start, const int32_t*
                 const int b = b0 + j;
                 while (a < rw1 && row_start[a + 1] <= b) ++a;  // past empty rows
                 if (a < rw1 && b + 1 == row_start[a + 1]) m |= 1u << j;
-                colp[base + mli_pos(lane, j, qm, 4)] = col[b];
-                valp[base + mli_pos(lane, j, qm, 2)] = val[b];
+                colp[base + mli_pos(lane, j, qm, lane_vec<int32_t>())] = col[b];
+                valp[base + mli_pos(lane, j, qm, lane_vec<double>())] = val[b];
             }
         }
         masks[(long long)s * 32 + lane] = (uint16_t)m;
@@ -86,13 +86,13 @@ __global__ void k_mli_convert(const double* __restrict__ valp, const int2* __res
                               const int4* __restrict__ rec, int nsub, T* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
-    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int V = lane_vec<T>();
     for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
         const int nkw = subc[s + 1].y - subc[s].y;
         const int qm = nkw >> 5, rem = nkw & 31;
         const int cnt = qm + (lane < rem ? 1 : 0);
         const long long base = rec[2LL * s + 1].z;
-        for (int j = 0; j < cnt; ++j) out[base + mli_pos(lane, j, qm, V)] = (T)valp[base + mli_pos(lane, j, qm, 2)];
+        for (int j = 0; j < cnt; ++j) out[base + mli_pos(lane, j, qm, V)] = (T)valp[base + mli_pos(lane, j, qm, lane_vec<double>())];
     }
 }
 
@@ -109,8 +109,8 @@ __global__ void k_mli_unpermute(const int32_t* __restrict__ colp, const double* 
         const int b0 = kw0 + lane * qm + (lane < rem ? lane : rem);
         const long long base = rec[2LL * s + 1].z;
         for (int j = 0; j < cnt; ++j) {
-            col[b0 + j] = colp[base + mli_pos(lane, j, qm, 4)];
-            val[b0 + j] = valp[base + mli_pos(lane, j, qm, 2)];
+            col[b0 + j] = colp[base + mli_pos(lane, j, qm, lane_vec<int32_t>())];
+            val[b0 + j] = valp[base + mli_pos(lane, j, qm, lane_vec<double>())];
         }
     }
 }

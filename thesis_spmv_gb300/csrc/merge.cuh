@@ -22,10 +22,14 @@
 //    values) into its own two shared-memory stages -- no CTA-wide
 //    coordination at all: while sub-tile i is processed, i+1 is loading.
 //  * Values and column indices of sub-tile s are stored from an 8-element-
-//    aligned base so that element j of lane l sits at mli_pos(l, j, qm, V):
-//    first the full blocks of V = 16/sizeof(T) elements, one 16-byte vector
-//    per lane per block, consecutive across the warp (each warp load is one
-//    coalesced 512-byte request); then a compact scalar tail.
+//    aligned base so that element j of lane l sits at mli_pos(l, j, qm, V)
+//    with V = lane_vec<T>() = 1: slot j of all 32 lanes is contiguous (j * 32
+//    + l), the partial last slot holds lanes < rem only, so the span is
+//    exactly nkw elements.  The global reads are the TMA bulk copies of the
+//    whole span (16-byte granules); in shared memory every lane reads its
+//    slot j with one conflict-free scalar load and no tail handling.  (The
+//    general form, V = 16 / sizeof(T) blocks of one 16-byte vector per lane
+//    plus a scalar tail, cost more instructions per slot than it saved.)
 //  * Per lane, a 16-bit mask marks the elements that end a row (precomputed
 //    from row_start), so no row-pointer search runs per SpMV: a lane's first
 //    row is the sub-tile's first row plus a warp prefix sum of mask popcounts.
@@ -94,9 +98,27 @@ __device__ __forceinline__ int row_of(const int32_t* __restrict__ row_start, int
 // shared memory: 16-byte vector loads for the full blocks (consecutive lanes
 // read consecutive 16-byte chunks: conflict-free), scalar loads for the
 // tail; zeros beyond cnt.
+// Width (elements) of the vector blocks of the lane-interleaved layout for
+// element type T: 1 stores element j of lane l at j * 32 + l (every slot one
+// conflict-free scalar load, no tail), 16 / sizeof(T) uses 16-byte blocks
+// followed by a scalar tail.
+template <typename T>
+__host__ __device__ constexpr int lane_vec() {
+    return 1;
+}
+
 template <typename T, int IPT>
 __device__ __forceinline__ void load_lane(const T* p, int qm, int cnt, int lane, T (&out)[IPT]) {
-    constexpr int V = 16 / (int)sizeof(T);
+    constexpr int V = lane_vec<T>();
+    if (V == 1) {
+        const int q = qm + (__any_sync(0xffffffffu, cnt > qm) ? 1 : 0);  // warp-uniform slot count
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            out[j] = T(0);
+            if (j < q && j < cnt) out[j] = p[j * 32 + lane];
+        }
+        return;
+    }
     constexpr int NB = (IPT + V - 1) / V;
     const int B = qm / V;
     union Vec {
