@@ -210,6 +210,16 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
                           uint16_t* col_jump, double* data, int32_t* block_nnz, int16_t* row_jump_block,
                           int16_t* col_jump_block);
 
+/* The merge kernels' launch variant the load-time tuner picked for this
+ * matrix (prefer_l1: 0 = most resident CTAs, 1 = a smaller shared-memory
+ * carveout leaving more L1 for the x gathers; both compute the same bits),
+ * the SpMV and persistent-power grids, and the two timings compared
+ * (tuned_ms[2], ms per SpMV; 0 when the matrix was too small to tune). */
+int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* grid, int32_t* power_grid,
+                         float* tuned_ms);
+/* Override the tuner's choice (prefer_l1 0 or 1) for later launches. */
+int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1);
+
 /* Tile size (merge items per tile) and tile count used by the SpMV kernel. */
 int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid);
 

@@ -6,9 +6,9 @@ sub-tiles of WM = 32*IPT items, one per warp; sub-tile s spans the nonzeros
 [kw0, kw1) and hands lane l the contiguous range [kw0 + start_l, + cnt_l)
 (qm = nkw // 32, rem = nkw % 32, cnt_l = qm + (l < rem)).  Each array is
 stored per sub-tile at an 8-element-aligned base so that element j of lane l
-sits at mli_pos(l, j, qm, V) with V = 1 (the kernel's lane_vec): slot j of
-all lanes contiguous, j * 32 + l, the partial last slot for lanes < rem only.
-The general V (16-byte blocks, then a scalar tail) is checked too.
+sits at mli_pos(l, j, qm, V) with V = 2 (the kernel's lane_vec): 2-element
+vector blocks consecutive across the warp, then a scalar tail of at most two
+slots (the partial last slot for lanes < rem only).  Other V are checked too.
 
 Checks: the permutation is a bijection into [base, base + nkw) and vector
 slots are 16-byte aligned; bases never overlap and stay inside the
@@ -22,7 +22,7 @@ import pytest
 from oracle import pyoracle as O
 
 BIG = 2 ** 31 - 1
-LANE_VEC = 1  # merge.cuh lane_vec<T>()
+LANE_VEC = 2  # merge.cuh lane_vec<T>()
 
 
 def mli_pos(lane, j, qm, V):

@@ -49,20 +49,23 @@ struct MliPlan {
 };
 long long mli_storage_elems(long long nnz, long long nsub);
 
-MergeGeom merge_geometry(int cfg);
-int merge_grid(int cfg, int nsub, int sm_count);
+// l1: launch variant of the merge kernels (0: most resident CTAs; 1: a
+// smaller shared-memory carveout, more L1 for irregular gathers).
+MergeGeom merge_geometry(int cfg, int l1 = 0);
+int merge_grid(int cfg, int nsub, int sm_count, int l1 = 0);
 int fixup_grid(int num_tiles, int sm_count);
 int dot_grid(long long n, int sm_count);
 // Persistent power-method kernel (cooperative launch): grid size for a
 // matrix with nsub sub-tiles, 0 if the kernel cannot be made co-resident.
-int power_persistent_grid(int cfg, int nsub, int sm_count);
+int power_persistent_grid(int cfg, int nsub, int sm_count, int l1 = 0);
 // Iterations k0 .. k0+nk-1 on X/Y (ping-pong; v_k in X for even k), nsq[k]
 // = ||v_k||^2 (nsq[k0] read when k0 > 0), result (5 doubles, or null):
 // {lambda, residual^2, ||v_k||^2, v_k.v_{k+1}, e_k} of the last iteration.
 // partials: 2 doubles per CTA; barrier: 2 words (zeroed here).
 cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                                     void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
-                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st);
+                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st,
+                                    int l1 = 0);
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
                                    int2* out, cudaStream_t st);
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
@@ -71,7 +74,7 @@ cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_coun
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st);
+                              cudaStream_t st, int l1 = 0);
 // Carries of the merge SpMV into y (MODE_POWER: times the rescale factor of
 // nsq_in).
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,

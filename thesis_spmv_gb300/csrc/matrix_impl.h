@@ -71,6 +71,10 @@ struct pwmgpu_matrix {
     int tm = 0, num_tiles = 0, grid = 1, fix_grid = 1;
     // persistent power kernel grids per configuration (0: not launchable)
     int pgrid = 0, pgrid32 = 0, pgridbf = 0;
+    // launch variant picked by the load-time tuner (0: most resident CTAs,
+    // 1: more L1), and the timings it compared (ms per SpMV)
+    int l1 = 0;
+    float tune_ms[2] = {0.f, 0.f};
     int power_mode = PWMGPU_POWER_AUTO;
     MliPlan P;
     // lane-interleaved FP32 / BF16 copies of the values (lazy)

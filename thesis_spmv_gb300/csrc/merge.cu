@@ -202,7 +202,10 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
     return true;
 }
 
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT>
+// L1: launch variant (0: shared-memory-heavy carveout, most resident CTAs;
+// 1: a smaller carveout that leaves more L1 for the x gathers); the code is
+// the same, the two instances carry different function attributes.
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0>
 __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
@@ -398,7 +401,7 @@ __device__ __forceinline__ void grid_total2(const double* partials, double* tota
     __syncthreads();
 }
 
-template <typename VT, typename XT, typename AT, int NT, int IPT>
+template <typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0>
 __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
@@ -629,41 +632,52 @@ __global__ void k_bf16_exact(const double* __restrict__ v, long long n, int* fla
 long long mli_storage_elems(long long nnz, long long nsub) { return mli_size(nnz, nsub); }
 
 // Kernel configurations (threads per CTA, items per lane).
+// Shared-memory carveout (percent of the maximum) of the L1-preferring launch
+// variant: room for 4 CTAs' stages, the rest of the 256 KB as L1.
+constexpr int kL1Carveout = 72;
+
 template <typename VT, typename XT, typename AT, int NT, int IPT>
 struct MergeKernels {
     static constexpr int SMEM = (NT / 32) * kMliStages * WarpStage<VT, IPT>::BYTES;
 
-    static MergeGeom geom() {
-        static int occ = -1;
-        if (occ < 0) {
-            auto k = k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT>;
-            auto kp = k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT>;
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-            cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-            int o = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM);
-            occ = o > 0 ? o : 1;
+    template <typename K>
+    static int setup(K k, int l1) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+        if (l1) cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, kL1Carveout);
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM) != cudaSuccess) o = 0;
+        return o;
+    }
+
+    static MergeGeom geom(int l1 = 0) {
+        static int occ[2] = {-1, -1};
+        if (occ[l1] < 0) {
+            int o;
+            if (l1) {
+                setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 1>, 1);
+                o = setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 1>, 1);
+            } else {
+                setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 0>, 0);
+                o = setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 0>, 0);
+            }
+            occ[l1] = o > 0 ? o : 1;
         }
-        return MergeGeom{32 * IPT, NT / 32, SMEM, occ, NT};
+        return MergeGeom{32 * IPT, NT / 32, SMEM, occ[l1], NT};
     }
 
     // resident CTAs per SM of the persistent power kernel (0: cannot launch)
-    static int power_occ() {
-        static int occ = -1;
-        if (occ < 0) {
-            auto k = k_power_persistent<VT, XT, AT, NT, IPT>;
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-            int o = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM) != cudaSuccess) o = 0;
-            occ = o;
-        }
-        return occ;
+    static int power_occ(int l1 = 0) {
+        static int occ[2] = {-1, -1};
+        if (occ[l1] < 0)
+            occ[l1] = l1 ? setup(k_power_persistent<VT, XT, AT, NT, IPT, 1>, 1)
+                         : setup(k_power_persistent<VT, XT, AT, NT, IPT, 0>, 0);
+        return occ[l1];
     }
 
     static cudaError_t power(const DevMatrix& M, const void* valp, const MliPlan& P, int grid, void* X, void* Y,
                              void* carries, int k0, int nk, double* nsq, double* result, double* partials,
-                             unsigned int* barrier, int* status, cudaStream_t st) {
-        power_occ();
+                             unsigned int* barrier, int* status, cudaStream_t st, int l1) {
+        power_occ(l1);
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
                                  nullptr, (AT*)carries, nullptr, status},
                                 P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier};
@@ -672,20 +686,28 @@ struct MergeKernels {
         void* args[] = {&p};
         // cooperative launch: fails instead of running if the grid cannot be
         // co-resident, so the grid barriers cannot wait on unscheduled CTAs
-        return cudaLaunchCooperativeKernel((const void*)k_power_persistent<VT, XT, AT, NT, IPT>, dim3(grid),
-                                           dim3(NT), args, SMEM, st);
+        const void* k = l1 ? (const void*)k_power_persistent<VT, XT, AT, NT, IPT, 1>
+                           : (const void*)k_power_persistent<VT, XT, AT, NT, IPT, 0>;
+        return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(NT), args, SMEM, st);
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                            cudaStream_t st) {
-        geom();
+                            cudaStream_t st, int l1) {
+        geom(l1);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub,
                                 (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status};
-        if (mode == MODE_POWER)
-            k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT><<<grid, NT, SMEM, st>>>(a);
-        else
-            k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT><<<grid, NT, SMEM, st>>>(a);
+        if (l1) {
+            if (mode == MODE_POWER)
+                k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 1><<<grid, NT, SMEM, st>>>(a);
+            else
+                k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 1><<<grid, NT, SMEM, st>>>(a);
+        } else {
+            if (mode == MODE_POWER)
+                k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 0><<<grid, NT, SMEM, st>>>(a);
+            else
+                k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 0><<<grid, NT, SMEM, st>>>(a);
+        }
         return cudaGetLastError();
     }
 };
@@ -697,28 +719,28 @@ using CfgF64 = MergeKernels<double, double, double, 128, kMliIpt>;
 using CfgF32 = MergeKernels<float, float, float, 128, kMliIpt>;
 using CfgBF16 = MergeKernels<__nv_bfloat16, float, float, 128, kMliIpt>;
 
-MergeGeom merge_geometry(int cfg) {
+MergeGeom merge_geometry(int cfg, int l1) {
     switch (cfg) {
-        case kCfgF32: return CfgF32::geom();
-        case kCfgBF16: return CfgBF16::geom();
-        default: return CfgF64::geom();
+        case kCfgF32: return CfgF32::geom(l1);
+        case kCfgBF16: return CfgBF16::geom(l1);
+        default: return CfgF64::geom(l1);
     }
 }
 
-int merge_grid(int cfg, int nsub, int sm_count) {
-    MergeGeom g = merge_geometry(cfg);
+int merge_grid(int cfg, int nsub, int sm_count, int l1) {
+    MergeGeom g = merge_geometry(cfg, l1);
     long long ctas = (nsub + g.w - 1) / g.w;
     long long grid = (long long)g.occ * sm_count;
     if (grid > ctas) grid = ctas;
     return grid > 0 ? (int)grid : 1;
 }
 
-int power_persistent_grid(int cfg, int nsub, int sm_count) {
+int power_persistent_grid(int cfg, int nsub, int sm_count, int l1) {
     int occ;
     switch (cfg) {
-        case kCfgF32: occ = CfgF32::power_occ(); break;
-        case kCfgBF16: occ = CfgBF16::power_occ(); break;
-        default: occ = CfgF64::power_occ(); break;
+        case kCfgF32: occ = CfgF32::power_occ(l1); break;
+        case kCfgBF16: occ = CfgBF16::power_occ(l1); break;
+        default: occ = CfgF64::power_occ(l1); break;
     }
     if (occ <= 0) return 0;
     const MergeGeom g = merge_geometry(cfg);
@@ -730,16 +752,18 @@ int power_persistent_grid(int cfg, int nsub, int sm_count) {
 
 cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                                     void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
-                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st) {
+                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st, int l1) {
     if (nk <= 0) return cudaSuccess;
     switch (cfg) {
         case kCfgF32:
-            return CfgF32::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st);
+            return CfgF32::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st,
+                                 l1);
         case kCfgBF16:
             return CfgBF16::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status,
-                                  st);
+                                  st, l1);
         default:
-            return CfgF64::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st);
+            return CfgF64::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st,
+                                 l1);
     }
 }
 
@@ -785,12 +809,12 @@ cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, in
 
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st) {
+                              cudaStream_t st, int l1) {
     if (P.nsub == 0) return cudaSuccess;
     switch (cfg) {
-        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
-        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
-        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st);
+        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
+        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
+        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
     }
 }
 

@@ -23,13 +23,15 @@
 //    coordination at all: while sub-tile i is processed, i+1 is loading.
 //  * Values and column indices of sub-tile s are stored from an 8-element-
 //    aligned base so that element j of lane l sits at mli_pos(l, j, qm, V)
-//    with V = lane_vec<T>() = 1: slot j of all 32 lanes is contiguous (j * 32
-//    + l), the partial last slot holds lanes < rem only, so the span is
-//    exactly nkw elements.  The global reads are the TMA bulk copies of the
-//    whole span (16-byte granules); in shared memory every lane reads its
-//    slot j with one conflict-free scalar load and no tail handling.  (The
-//    general form, V = 16 / sizeof(T) blocks of one 16-byte vector per lane
-//    plus a scalar tail, cost more instructions per slot than it saved.)
+//    with V = lane_vec<T>() = 2 for every array: pairs of slots (2b, 2b+1)
+//    of all 32 lanes form one contiguous block of 2-element vectors (one
+//    vector load per lane: 16 bytes for FP64 values, 8 for column indices,
+//    conflict-free and consecutive across the warp), then a tail of at most
+//    two scalar slots (the partial last one holds lanes < rem only), so the
+//    span is exactly nkw elements.  The global reads are the TMA bulk copies
+//    of the whole span.  (Wider blocks -- 16 bytes of column indices -- need a
+//    tail of up to four scalars per lane that costs more than it saves;
+//    scalar-only slots double the loads of full sub-tiles.)
 //  * Per lane, a 16-bit mask marks the elements that end a row (precomputed
 //    from row_start), so no row-pointer search runs per SpMV: a lane's first
 //    row is the sub-tile's first row plus a warp prefix sum of mask popcounts.
@@ -42,6 +44,7 @@
 // sub-tile's own unfinished row goes to carries[s] for k_merge_fixup.
 #pragma once
 #include <climits>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -102,9 +105,12 @@ __device__ __forceinline__ int row_of(const int32_t* __restrict__ row_start, int
 // element type T: 1 stores element j of lane l at j * 32 + l (every slot one
 // conflict-free scalar load, no tail), 16 / sizeof(T) uses 16-byte blocks
 // followed by a scalar tail.
+#ifndef PWMGPU_LANE_VEC
+#define PWMGPU_LANE_VEC 2
+#endif
 template <typename T>
 __host__ __device__ constexpr int lane_vec() {
-    return 1;
+    return PWMGPU_LANE_VEC;
 }
 
 template <typename T, int IPT>
@@ -116,6 +122,32 @@ __device__ __forceinline__ void load_lane(const T* p, int qm, int cnt, int lane,
         for (int j = 0; j < IPT; ++j) {
             out[j] = T(0);
             if (j < q && j < cnt) out[j] = p[j * 32 + lane];
+        }
+        return;
+    }
+    if (V == 2 && IPT % 2 == 0) {
+        // block b < B: one 2-element vector load; block b == B: the tail (at
+        // most 2 elements, scalar); later blocks: zeros.  B is warp-uniform.
+        const int B = qm / 2;
+        union Vec2 {
+            typename std::conditional<sizeof(T) == 8, uint4, typename std::conditional<sizeof(T) == 4, uint2,
+                                                                                        unsigned int>::type>::type u;
+            T t[2];
+        };
+#pragma unroll
+        for (int b = 0; b < IPT / 2; ++b) {
+            if (b < B) {
+                Vec2 v;
+                v.u = *reinterpret_cast<const decltype(v.u)*>(p + b * 64 + lane * 2);
+                out[2 * b] = v.t[0];
+                out[2 * b + 1] = v.t[1];
+            } else if (b == B) {
+                out[2 * b] = (2 * b < cnt) ? p[64 * B + lane] : T(0);
+                out[2 * b + 1] = (2 * b + 1 < cnt) ? p[64 * B + 32 + lane] : T(0);
+            } else {
+                out[2 * b] = T(0);
+                out[2 * b + 1] = T(0);
+            }
         }
         return;
     }

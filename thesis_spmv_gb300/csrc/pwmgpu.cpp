@@ -142,6 +142,49 @@ int build_format(pwmgpu_matrix* m) {
     return PWMGPU_OK;
 }
 
+// Load-time tuner of the merge kernels' launch variant: with enough work to
+// measure (at least 8 sub-tiles per resident warp), time a few SpMVs in each
+// variant (x = 0: the timing does not depend on the values) and keep the
+// faster.  The variants compute the same bits; only the shared-memory / L1
+// split and the resident CTA count differ (a Poisson-like matrix gains from
+// more CTAs, gathers spread over a large x from more L1).
+int tune(pwmgpu_matrix* m) {
+    const MergeGeom g = merge_geometry(kCfgF64, 0);
+    if (m->num_tiles < 8 * g.occ * g.w * m->sm_count) return PWMGPU_OK;
+    TRY(ensure_vectors(m));
+    CU(cudaMemsetAsync(m->dx, 0, sizeof(double) * (size_t)std::max(m->M.nor, m->M.noc), m->stream));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    int rc = PWMGPU_OK;
+    for (int v = 0; v < 2 && rc == PWMGPU_OK; ++v) {
+        const int grid = merge_grid(kCfgF64, m->num_tiles, m->sm_count, v);
+        cudaError_t e = cudaSuccess;
+        for (int r = 0; r < 5 && e == cudaSuccess; ++r) {  // one warm-up, four timed
+            if (r == 1) e = cudaEventRecord(e0, m->stream);
+            if (e == cudaSuccess)
+                e = launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, grid, m->dx, m->dy, m->carries,
+                                      nullptr, m->status, m->stream, v);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, m->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&m->tune_ms[v], e0, e1);
+        if (e != cudaSuccess) rc = fail(PWMGPU_ERR_CUDA, "launch tuning: %s", cudaGetErrorString(e));
+        m->tune_ms[v] /= 4.f;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    TRY(rc);
+    TRY(check_status(m));
+    const int v = m->tune_ms[1] < 0.97f * m->tune_ms[0] ? 1 : 0;
+    m->l1 = v;
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, v);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, v);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, v);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, v);
+    return PWMGPU_OK;
+}
+
 int build_plan(pwmgpu_matrix* m) {
     if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
     const long long total = (long long)m->M.nor + m->M.nnz;
@@ -166,6 +209,7 @@ int build_plan(pwmgpu_matrix* m) {
     CU(cudaStreamSynchronize(m->stream));
     dfree(m->M.col);
     dfree(m->M.val);
+    m->l1 = 0;
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
     m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
     m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count);
@@ -178,7 +222,7 @@ int build_plan(pwmgpu_matrix* m) {
     TRY(ensure_cap(&m->fix_partials, &m->fix_cap, (size_t)m->fix_grid + 64));
     CU(cudaStreamSynchronize(m->stream));
     m->loaded = true;
-    return PWMGPU_OK;
+    return tune(m);
 }
 }  // namespace pwmgpu
 namespace {
@@ -247,7 +291,7 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->format != PWMGPU_FMT_MERGE) return spmv_format(m, dx, dy, nullptr);
     if (m->num_tiles == 0) return PWMGPU_OK;
     CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, m->status,
-                         m->stream));
+                         m->stream, m->l1));
     CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, m->fix_grid,
                               m->stream));
     return PWMGPU_OK;
@@ -257,7 +301,7 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
 // fix-up), then nsq_out = ||out||^2 (row pass, deterministic).
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
     CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
-                         m->status, m->stream));
+                         m->status, m->stream, m->l1));
     CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in, m->fix_grid,
                               m->stream));
     CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, nsq_out,
@@ -293,7 +337,7 @@ int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
     if (use_fused(m, m->pgrid)) {
         // K5: all `it` iterations in one persistent launch
         CU(launch_power_persistent(kCfgF64, m->M, m->P.valp, m->P, m->pgrid, dx, dy, m->carries, 0, it, m->nsq,
-                                   nullptr, m->partials, m->barrier, m->status, m->stream));
+                                   nullptr, m->partials, m->barrier, m->status, m->stream, m->l1));
     } else {
         for (int k = 0; k < it; ++k) {
             const double* in = (k % 2 == 0) ? dx : dy;
@@ -374,7 +418,7 @@ struct ChunkOut {
 int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X, void* Y, int k0, int nk,
                 ChunkOut* o) {
     CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
-                               m->partials, m->barrier, m->status, m->stream));
+                               m->partials, m->barrier, m->status, m->stream, m->l1));
     CU(cudaMemcpyAsync(m->hres, m->small, 5 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     TRY(check_status(m));
     const double lam = m->hres[0], r2 = m->hres[1], nsq = m->hres[2];
@@ -853,8 +897,8 @@ int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     int cfg = kCfgF32, pg = 0;
     const void* valp = nullptr;
     TRY(ensure_low_values(m, false, &cfg, &valp, &pg));
-    CU(launch_merge_spmv(kCfgF32, kModeSpmv, m->M, valp, m->P, merge_grid(kCfgF32, m->num_tiles, m->sm_count), dx,
-                         dy, m->carries, nullptr, m->status, m->stream));
+    CU(launch_merge_spmv(kCfgF32, kModeSpmv, m->M, valp, m->P, merge_grid(kCfgF32, m->num_tiles, m->sm_count, m->l1),
+                         dx, dy, m->carries, nullptr, m->status, m->stream, m->l1));
     CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
                               nullptr, m->fix_grid, m->stream));
     return PWMGPU_OK;
@@ -1010,6 +1054,32 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
     put(block_nnz, bn);
     put(row_jump_block, rjb);
     put(col_jump_block, cjb);
+    return PWMGPU_OK;
+}
+
+int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* grid, int32_t* power_grid,
+                         float* tuned_ms) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (prefer_l1) *prefer_l1 = m->l1;
+    if (grid) *grid = m->grid;
+    if (power_grid) *power_grid = m->pgrid;
+    if (tuned_ms) {
+        tuned_ms[0] = m->tune_ms[0];
+        tuned_ms[1] = m->tune_ms[1];
+    }
+    return PWMGPU_OK;
+}
+
+int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (prefer_l1 != 0 && prefer_l1 != 1) return fail(PWMGPU_ERR_INVALID, "prefer_l1 must be 0 or 1");
+    if (!m->loaded || m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_STATE, "no merge-format matrix loaded");
+    CU(cudaStreamSynchronize(m->stream));
+    m->l1 = prefer_l1;
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, prefer_l1);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, prefer_l1);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, prefer_l1);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, prefer_l1);
     return PWMGPU_OK;
 }
 

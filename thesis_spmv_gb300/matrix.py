@@ -232,6 +232,17 @@ class CudaSparseMatrix:
         check(_lib.lib().pwmgpu_merge_partition(self._h, int(parts), _ptr(out)), "merge_partition")
         return out.reshape(parts + 1, 2)
 
+    def launch_config(self):
+        """(prefer_l1, grid, power_grid, (ms variant 0, ms variant 1)) chosen
+        by the load-time tuner."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        ms = (C.c_float * 2)()
+        check(_lib.lib().pwmgpu_launch_config(self._h, C.byref(a), C.byref(b), C.byref(c), ms), "launch_config")
+        return a.value, b.value, c.value, (ms[0], ms[1])
+
+    def set_launch_variant(self, prefer_l1):
+        check(_lib.lib().pwmgpu_set_launch_variant(self._h, int(prefer_l1)), "set_launch_variant")
+
     def tile_info(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         check(_lib.lib().pwmgpu_tile_info(self._h, C.byref(a), C.byref(b), C.byref(c)), "tile_info")
