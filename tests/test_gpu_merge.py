@@ -274,3 +274,31 @@ def test_launch_tuner_variants_same_bits(pwm, kind):
     rs, ci, d = M.getCSR()
     A = O.CRSArrays(n, n, rs, ci, d)
     assert np.all(np.abs(ys[0] - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
+
+
+@pytest.mark.parametrize("kind", ["poisson", "random", "long_rows"])
+def test_pipelined_host_mv_same_bits(pwm, kind):
+    """pwmgpu_mv on host arrays runs pipelined (x up in pieces, the SpMV in
+    chunks, y down per chunk) for matrices large enough; it must give the
+    same bits as the device-resident path."""
+    torch = pytest.importorskip("torch")
+    M = pwm.CRSCuda(1)
+    if kind == "poisson":
+        M.generatePoissonMatrix(700, 900, 1)
+    elif kind == "random":
+        M.generateRandom(600_000, 5, mean_len=12.0)
+    else:  # lognormal rows up to 20000 long: runs of sub-tiles cross chunks
+        M.generateRandom(120_000, 9, mean_len=60.0, sigma=1.6, max_len=20000)
+    n = M.dims()[0]
+    x = np.random.default_rng(7).uniform(-1, 1, n)
+    y = np.full(n, np.nan)
+    M.mv(x, y)
+    dx = torch.tensor(x, device="cuda")
+    dy = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    M.mv_device(dx.data_ptr(), dy.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(y, dy.cpu().numpy())
+    rs, ci, d = M.getCSR()
+    A = O.CRSArrays(n, n, rs, ci, d)
+    assert np.all(np.abs(y - O.crs_mv(A, x)) <= O.row_error_bound(A, x))

@@ -141,6 +141,15 @@ cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, con
                             const uint16_t* col_jump, const double* data, const double* x, double* y,
                             const double* nsq_in, int sm_count, cudaStream_t st);
 
+// Pipelined host-array SpMV: chunk records (4 ints per chunk: first
+// sub-tile, its first row, row-split flag, largest column read), and the
+// SpMV / fix-up over sub-tile ranges.
+cudaError_t launch_pipeline_plan(const int32_t* row_start, const MliPlan& P, int K, int* out, cudaStream_t st);
+cudaError_t launch_merge_spmv_range(const DevMatrix& M, const MliPlan& P, int t0, int t1, int grid, const double* x,
+                                    double* y, double* carries, int* status, cudaStream_t st, int l1);
+cudaError_t launch_merge_fixup_range(const DevMatrix& M, const int2* tiles, int num_tiles, int f0, int f1, double* y,
+                                     const double* carries, cudaStream_t st, int sm_count);
+
 // Record the calling thread's last error message (pwmgpu_last_error).
 void record_error(const char* msg);
 

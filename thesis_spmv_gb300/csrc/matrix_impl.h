@@ -124,6 +124,15 @@ struct pwmgpu_matrix {
         std::vector<int16_t> row_jump_block, col_jump_block;
     } coh;
 
+    // pipelined host-array SpMV (pwmgpu_mv): chunk records, streams, events
+    struct {
+        int K = 0;          // chunks (0: not planned yet, -1: not pipelined)
+        std::vector<int> rec;  // 4 per chunk: first sub-tile, first row, split flag, prefix max column
+        cudaStream_t in = nullptr, out = nullptr;
+        std::vector<cudaEvent_t> ev_x, ev_y;
+        cudaEvent_t ev_start = nullptr;
+    } pipe;
+
     // host-facing vector buffers
     double* dx = nullptr;
     double* dy = nullptr;
@@ -155,6 +164,8 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(coh.col_jump);
         pwmgpu::dfree(coh.data);
         coh = decltype(coh)();
+        pipe.K = 0;
+        pipe.rec.clear();
         if (valbf) cudaFree(valbf);
         valbf = nullptr;
         bf16_exact = -1;
@@ -164,6 +175,15 @@ struct pwmgpu_matrix {
     }
     void release_all() {
         release_matrix();
+        for (cudaEvent_t e : pipe.ev_x) cudaEventDestroy(e);
+        for (cudaEvent_t e : pipe.ev_y) cudaEventDestroy(e);
+        if (pipe.ev_start) cudaEventDestroy(pipe.ev_start);
+        if (pipe.in) cudaStreamDestroy(pipe.in);
+        if (pipe.out) cudaStreamDestroy(pipe.out);
+        pipe.ev_x.clear();
+        pipe.ev_y.clear();
+        pipe.ev_start = nullptr;
+        pipe.in = pipe.out = nullptr;
         pwmgpu::dfree(carries);
         pwmgpu::dfree(partials);
         pwmgpu::dfree(fix_partials);

@@ -133,6 +133,7 @@ struct MergeArgs {
     AT* carries;           // one per sub-tile
     const double* nsq_in;  // MODE_POWER: ||x||^2 (source of the 2^e rescale), or null for e = 0
     int* status;
+    int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
 };
 
 constexpr int kMliStages = 2;
@@ -156,18 +157,18 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
     if (lane == 0) {
         for (int k = 0; k < NS && k < n; ++k) {
             const uint32_t u = ticket + k;
-            const int s = gw + k * tw;
+            const int s = a.tile0 + gw + k * tw;
             issue_subtile<VT, IPT>(stages + (u % NS) * S::BYTES, &bars[u % NS], s, __ldg(a.rec + 2LL * s + 1),
                                    a.rec, a.masks, a.colp, a.valp, pol);
         }
-        if (n > NS) pref = __ldg(a.rec + 2LL * (gw + NS * tw) + 1);
+        if (n > NS) pref = __ldg(a.rec + 2LL * (a.tile0 + gw + NS * tw) + 1);
     }
     __syncwarp();
     int i = 0;
     for (; i < n; ++i) {
         const uint32_t u = ticket + i;
         const int k = u % NS;
-        const int s = gw + i * tw;
+        const int s = a.tile0 + gw + i * tw;
         unsigned char* st = stages + k * S::BYTES;
         const bool ok = mbar_wait_bounded(&bars[k], (u / NS) & 1u, a.status);
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
@@ -236,14 +237,16 @@ struct FixArgs {
     XT* y;
     const AT* carries;
     const double* nsq_in;  // MODE_POWER: ||x||^2, source of the rescale exponent
+    int t_lo = 0, t_hi = -1;  // first sub-tiles of the runs to fix: [t_lo, t_hi) (t_hi < 0: all)
 };
 
 // Stand-alone fix-up kernel (one thread per sub-tile).
 template <int MODE, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
-    const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, a.num_tiles, stride);
+    const int t0 = a.t_lo + blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int t_end = a.t_hi < 0 ? a.num_tiles : a.t_hi;
+    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, t_end, stride);
 }
 
 // ||y||^2 (and x . y with DOT) with one deterministic reduction: per-CTA
@@ -835,6 +838,61 @@ cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* til
 cudaError_t launch_merge_fixup_f32(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, float* y,
                                    const float* carries, const double* nsq_in, int fix_grid, cudaStream_t st) {
     return fixup_impl<float, float>(mode, M, tiles, num_tiles, y, carries, nsq_in, fix_grid, st);
+}
+
+// Chunk records of the pipelined host-array SpMV: chunk c covers sub-tiles
+// [c*nsub/K, (c+1)*nsub/K); out[c] = {first sub-tile, its first row, 1 if
+// that row began in the previous chunk, largest column the chunk reads}.
+// One CTA per chunk.
+__global__ void __launch_bounds__(256) k_pipeline_plan(const int32_t* __restrict__ row_start,
+                                                       const int2* __restrict__ subc, const int4* __restrict__ rec,
+                                                       const int32_t* __restrict__ colp, int nsub, int K,
+                                                       int4* __restrict__ out) {
+    __shared__ int red[256];
+    const int c = blockIdx.x;
+    const int s0 = (int)((long long)nsub * c / K), s1 = (int)((long long)nsub * (c + 1) / K);
+    // the chunk's storage is contiguous (gaps between sub-tiles hold 0)
+    int mx = -1;
+    const int4 a1 = __ldg(rec + 2LL * s0 + 1), b1 = __ldg(rec + 2LL * (s1 - 1) + 1);
+    for (long long k = a1.z + threadIdx.x; k < (long long)b1.z + b1.w; k += blockDim.x) mx = max(mx, __ldg(colp + k));
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int2 c0 = subc[s0];
+        const int split = (c0.x < 0x7fffffff && s0 > 0 && c0.y > row_start[c0.x]) ? 1 : 0;
+        out[c] = make_int4(s0, c0.x, split, red[0]);
+    }
+}
+
+cudaError_t launch_pipeline_plan(const int32_t* row_start, const MliPlan& P, int K, int* out, cudaStream_t st) {
+    if (K <= 0 || P.nsub <= 0) return cudaSuccess;
+    k_pipeline_plan<<<K, 256, 0, st>>>(row_start, P.subc, P.rec, P.colp, P.nsub, K, reinterpret_cast<int4*>(out));
+    return cudaGetLastError();
+}
+
+// SpMV over sub-tiles [t0, t1) (FP64) and the fix-up of the runs starting in
+// [f0, f1).
+cudaError_t launch_merge_spmv_range(const DevMatrix& M, const MliPlan& P, int t0, int t1, int grid, const double* x,
+                                    double* y, double* carries, int* status, cudaStream_t st, int l1) {
+    if (t1 <= t0) return cudaSuccess;
+    CfgF64::geom(l1);
+    MergeArgs<double, double, double> a{M.row_start, P.colp, P.valp, P.rec, P.masks, M.nor, t1 - t0,
+                                        x, y, carries, nullptr, status, t0};
+    if (l1) k_merge_spmv<MODE_SPMV, double, double, double, 128, kMliIpt, 1><<<grid, 128, CfgF64::SMEM, st>>>(a);
+    else k_merge_spmv<MODE_SPMV, double, double, double, 128, kMliIpt, 0><<<grid, 128, CfgF64::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge_fixup_range(const DevMatrix& M, const int2* tiles, int num_tiles, int f0, int f1, double* y,
+                                     const double* carries, cudaStream_t st, int sm_count) {
+    if (f1 <= f0) return cudaSuccess;
+    FixArgs<double, double> a{M.row_start, tiles, M.nor, num_tiles, y, carries, nullptr, f0, f1};
+    k_merge_fixup<MODE_SPMV, double, double><<<fixup_grid(f1 - f0, sm_count), 256, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, double* partials, unsigned int* counter,

@@ -539,6 +539,102 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
     return PWMGPU_OK;
 }
 
+// ---- pipelined host-array SpMV -------------------------------------------
+// x goes up in kPipeX pieces on one stream, y comes down per chunk on
+// another; chunk c's SpMV waits only for the x pieces holding the columns
+// chunks 0..c read, and chunk c's rows go down once the fix-up of the runs
+// starting in chunk c has run (after chunk c+1's SpMV: such a run ends in
+// chunk c+1 at the latest, checked at plan time).  Upload, compute and
+// download overlap; the result is the same as the one-shot path (the same
+// sub-tiles and fix-ups, in the same arithmetic).
+constexpr int kPipeChunks = 16;
+constexpr int kPipeX = 16;
+
+int plan_pipeline(pwmgpu_matrix* m) {
+    auto& p = m->pipe;
+    if (p.K != 0) return PWMGPU_OK;
+    p.K = -1;
+    const int K = kPipeChunks;
+    if (m->num_tiles < 64 * K) return PWMGPU_OK;  // too small to gain from it
+    int* d = nullptr;
+    TRY(dalloc(&d, 4 * (size_t)K));
+    p.rec.assign(4 * (size_t)K, 0);
+    cudaError_t e = launch_pipeline_plan(m->M.row_start, m->P, K, d, m->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(p.rec.data(), d, sizeof(int) * 4 * K, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    dfree(d);
+    if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "pipeline plan: %s", cudaGetErrorString(e));
+    // a run of sub-tiles may cross at most one chunk boundary: chunk first
+    // rows must increase strictly
+    for (int c = 1; c < K; ++c)
+        if (p.rec[4 * c + 1] <= p.rec[4 * (c - 1) + 1]) return PWMGPU_OK;
+    for (int c = 1; c < K; ++c) p.rec[4 * c + 3] = std::max(p.rec[4 * c + 3], p.rec[4 * (c - 1) + 3]);
+    CU(cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&p.ev_start, cudaEventDisableTiming));
+    p.ev_x.assign(kPipeX, nullptr);
+    p.ev_y.assign(K, nullptr);
+    for (auto& ev : p.ev_x) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    for (auto& ev : p.ev_y) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    p.K = K;
+    return PWMGPU_OK;
+}
+
+int mv_pipelined(pwmgpu_matrix* m, const double* x, double* y) {
+    auto& p = m->pipe;
+    const int K = p.K, noc = m->M.noc, nor = m->M.nor, nsub = m->num_tiles;
+    // the streams start after earlier work on the handle's stream
+    CU(cudaEventRecord(p.ev_start, m->stream));
+    CU(cudaStreamWaitEvent(p.in, p.ev_start, 0));
+    CU(cudaStreamWaitEvent(p.out, p.ev_start, 0));
+    for (int q = 0; q < kPipeX; ++q) {
+        const long long a = (long long)noc * q / kPipeX, b = (long long)noc * (q + 1) / kPipeX;
+        if (b > a)
+            CU(cudaMemcpyAsync(m->dx + a, x + a, sizeof(double) * (size_t)(b - a), cudaMemcpyHostToDevice, p.in));
+        CU(cudaEventRecord(p.ev_x[(size_t)q], p.in));
+    }
+    auto piece_of = [&](int col) {  // the x piece holding column col
+        int q = 0;
+        while (q + 1 < kPipeX && (long long)noc * (q + 1) / kPipeX <= col) ++q;
+        return q;
+    };
+    auto chunk_tiles = [&](int c, int* t0, int* t1) {
+        *t0 = p.rec[4 * c];
+        *t1 = c + 1 < K ? p.rec[4 * (c + 1)] : nsub;
+    };
+    // rows chunk c downloads: [lo_c, lo_{c+1})
+    auto row_lo = [&](int c) { return c == 0 ? 0 : (c >= K ? nor : p.rec[4 * c + 1] + p.rec[4 * c + 2]); };
+    int waited = -1;
+    for (int c = 0; c <= K; ++c) {
+        if (c < K) {
+            const int need = piece_of(p.rec[4 * c + 3]);
+            for (int q = waited + 1; q <= need; ++q) CU(cudaStreamWaitEvent(m->stream, p.ev_x[(size_t)q], 0));
+            waited = std::max(waited, need);
+            int t0, t1;
+            chunk_tiles(c, &t0, &t1);
+            const int grid = merge_grid(kCfgF64, t1 - t0, m->sm_count, m->l1);
+            CU(launch_merge_spmv_range(m->M, m->P, t0, t1, grid, m->dx, m->dy, m->carries, m->status, m->stream,
+                                       m->l1));
+        }
+        if (c >= 1) {
+            // chunk c-1: fix-up of its runs (they end by chunk c), then its rows go down
+            int t0, t1;
+            chunk_tiles(c - 1, &t0, &t1);
+            CU(launch_merge_fixup_range(m->M, m->P.subc, nsub, t0, t1, m->dy, m->carries, m->stream, m->sm_count));
+            CU(cudaEventRecord(p.ev_y[(size_t)c - 1], m->stream));
+            CU(cudaStreamWaitEvent(p.out, p.ev_y[(size_t)c - 1], 0));
+            const int r0 = row_lo(c - 1), r1 = row_lo(c);
+            if (r1 > r0)
+                CU(cudaMemcpyAsync(y + r0, m->dy + r0, sizeof(double) * (size_t)(r1 - r0), cudaMemcpyDeviceToHost,
+                                   p.out));
+        }
+    }
+    CU(cudaStreamSynchronize(p.out));
+    CU(cudaStreamSynchronize(p.in));
+    return check_status(m);
+}
+
 }  // namespace
 
 namespace pwmgpu {
@@ -831,6 +927,11 @@ int pwmgpu_mv(pwmgpu_matrix* m, const double* x, double* y) {
     if (m->M.nor == 0) return PWMGPU_OK;
     if (!y || (m->M.noc > 0 && !x)) return fail(PWMGPU_ERR_INVALID, "null vector");
     TRY(ensure_vectors(m));
+    if (m->format == PWMGPU_FMT_MERGE) {
+        int rc = plan_pipeline(m);
+        if (rc != PWMGPU_OK) return rc;
+        if (m->pipe.K > 0) return mv_pipelined(m, x, y);
+    }
     if (m->M.noc > 0)
         CU(cudaMemcpyAsync(m->dx, x, sizeof(double) * (size_t)m->M.noc, cudaMemcpyHostToDevice, m->stream));
     TRY(spmv_f64(m, m->dx, m->dy));
