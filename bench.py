@@ -128,14 +128,21 @@ def dist_setup(n_gpus):
     return world, rank, local
 
 
-def max_over_ranks(v, world):
+def max_over_ranks(v, world, device="cuda"):
+    """The slowest rank's time (replicas: the job ends with its last rank)."""
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_gbs(bytes_per_rank, ms_max, world):
+    """Whole-job throughput of N independent replicas: every rank's bytes over
+    the slowest rank's time (weak scaling: each rank does a full SpMV)."""
+    return bytes_per_rank * world / (ms_max * 1e-3) / 1e9
 
 
 def barrier(world):
@@ -491,7 +498,7 @@ def run_ours(args, world, rank, local):
     barrier(world)
     ms_total = max_over_ranks(ms_total, world)
     ms = ms_total / args.steps
-    value = B * world / (ms * 1e-3) / 1e9
+    value = replica_gbs(B, ms, world)
 
     # ---- the same Poisson matrix in the CSB and CO-H formats ----
     formats = {}
