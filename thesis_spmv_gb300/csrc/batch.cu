@@ -84,7 +84,7 @@ __device__ __forceinline__ int4 prefetch_rec(const BatchTable& T, int g, int& j)
 }
 
 template <typename VT, typename XT, typename AT, int NT, int IPT>
-__global__ void __launch_bounds__(NT, 4) k_batch_spmv(const BatchTable* __restrict__ Tp) {
+__global__ void __launch_bounds__(NT, 5) k_batch_spmv(const BatchTable* __restrict__ Tp) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
     constexpr int NS = kBatchStages;
