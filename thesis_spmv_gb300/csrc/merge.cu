@@ -843,18 +843,22 @@ cudaError_t launch_merge_fixup_f32(int mode, const DevMatrix& M, const int2* til
 // Chunk records of the pipelined host-array SpMV: chunk c covers sub-tiles
 // [c*nsub/K, (c+1)*nsub/K); out[c] = {first sub-tile, its first row, 1 if
 // that row began in the previous chunk, largest column the chunk reads}.
-// One CTA per chunk.
+// kPlanCtas CTAs per chunk share the column scan (atomicMax into out[c].w,
+// which starts at -1).
+constexpr int kPlanCtas = 32;
 __global__ void __launch_bounds__(256) k_pipeline_plan(const int32_t* __restrict__ row_start,
                                                        const int2* __restrict__ subc, const int4* __restrict__ rec,
                                                        const int32_t* __restrict__ colp, int nsub, int K,
                                                        int4* __restrict__ out) {
     __shared__ int red[256];
-    const int c = blockIdx.x;
+    const int c = blockIdx.x / kPlanCtas, part = blockIdx.x % kPlanCtas;
     const int s0 = (int)((long long)nsub * c / K), s1 = (int)((long long)nsub * (c + 1) / K);
     // the chunk's storage is contiguous (gaps between sub-tiles hold 0)
-    int mx = -1;
     const int4 a1 = __ldg(rec + 2LL * s0 + 1), b1 = __ldg(rec + 2LL * (s1 - 1) + 1);
-    for (long long k = a1.z + threadIdx.x; k < (long long)b1.z + b1.w; k += blockDim.x) mx = max(mx, __ldg(colp + k));
+    const long long lo = a1.z, hi = (long long)b1.z + b1.w, len = hi - lo;
+    const long long p0 = lo + len * part / kPlanCtas, p1 = lo + len * (part + 1) / kPlanCtas;
+    int mx = -1;
+    for (long long k = p0 + threadIdx.x; k < p1; k += blockDim.x) mx = max(mx, __ldg(colp + k));
     red[threadIdx.x] = mx;
     __syncthreads();
     for (int o = 128; o > 0; o >>= 1) {
@@ -862,15 +866,23 @@ __global__ void __launch_bounds__(256) k_pipeline_plan(const int32_t* __restrict
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        const int2 c0 = subc[s0];
-        const int split = (c0.x < 0x7fffffff && s0 > 0 && c0.y > row_start[c0.x]) ? 1 : 0;
-        out[c] = make_int4(s0, c0.x, split, red[0]);
+        atomicMax(&out[c].w, red[0]);
+        if (part == 0) {
+            const int2 c0 = subc[s0];
+            const int split = (s0 > 0 && c0.y > row_start[c0.x]) ? 1 : 0;
+            out[c].x = s0;
+            out[c].y = c0.x;
+            out[c].z = split;
+        }
     }
 }
 
 cudaError_t launch_pipeline_plan(const int32_t* row_start, const MliPlan& P, int K, int* out, cudaStream_t st) {
     if (K <= 0 || P.nsub <= 0) return cudaSuccess;
-    k_pipeline_plan<<<K, 256, 0, st>>>(row_start, P.subc, P.rec, P.colp, P.nsub, K, reinterpret_cast<int4*>(out));
+    cudaError_t e = cudaMemsetAsync(out, 0xFF, sizeof(int4) * (size_t)K, st);  // -1 everywhere
+    if (e != cudaSuccess) return e;
+    k_pipeline_plan<<<K * kPlanCtas, 256, 0, st>>>(row_start, P.subc, P.rec, P.colp, P.nsub, K,
+                                                   reinterpret_cast<int4*>(out));
     return cudaGetLastError();
 }
 
