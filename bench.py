@@ -456,6 +456,50 @@ def serving(pwm, args):
     return out
 
 
+def triplet_load(pwm, torch, dev, M, N, cpu=True):
+    """Triplet -> CRS on the device (pwmgpu_load_triplets_device) for the
+    entries of the matrix M holds in a seeded shuffled order; the result must
+    be M's CRS bit for bit.  CPU leg: the oracle's TripletToCRS restatement
+    (one thread) on a shuffled 1024 x 1024 Poisson triplet."""
+    rs, ci, v = M.getCSR()
+    nnz = ci.size
+    counts = torch.from_numpy(np.diff(rs).astype(np.int64)).to(dev)
+    rows = torch.repeat_interleave(torch.arange(N, dtype=torch.int32, device=dev), counts)
+    g = torch.Generator(device=dev).manual_seed(11)
+    perm = torch.randperm(nnz, device=dev, generator=g)
+    dr = rows[perm].contiguous()
+    dc = torch.from_numpy(ci).to(dev)[perm].contiguous()
+    dv = torch.from_numpy(v).to(dev)[perm].contiguous()
+    del rows, perm, counts
+    T = pwm.CRSCuda(1)
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        T.loadFromDeviceTriplets(N, N, nnz, dr.data_ptr(), dc.data_ptr(), dv.data_ptr())
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    trs, tci, tv = T.getCSR()
+    same = bool(np.array_equal(trs, rs) and np.array_equal(tci, ci) and np.array_equal(tv, v))
+    ms = 1e3 * sorted(times)[1]
+    out = {"workload": "%d shuffled triplets of the Poisson matrix above" % nnz,
+           "api": "pwmgpu_load_triplets_device (includes the merge-path plan build)",
+           "ms": round(ms, 3), "entries_per_s": round(nnz / (ms * 1e-3), 1), "same_crs_as_generated": same}
+    del dr, dc, dv, T
+    if cpu:
+        from oracle import pyoracle as O
+        r0, c0, v0 = O.triplet_poisson(1024, 1024)
+        p = np.random.default_rng(11).permutation(r0.size)
+        r0, c0, v0 = r0[p].copy(), c0[p].copy(), v0[p].copy()
+        t0 = time.perf_counter()
+        O.triplet_to_crs(1024 * 1024, 1024 * 1024, r0, c0, v0)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"entries_per_s": round(r0.size / cs, 1), "cores": 1, "kind": "port",
+                               "sample": "%d shuffled triplets of the 1024x1024 Poisson matrix "
+                                         "(TripletToCRS restated in oracle/oracle.c)" % r0.size}
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import thesis_spmv_gb300 as pwm
@@ -519,6 +563,7 @@ def run_ours(args, world, rank, local):
             fms = f0.elapsed_time(f1) / 50
             formats[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
             del F
+        formats_load = triplet_load(pwm, torch, dev, M, N, cpu=rank == 0 and world == 1 and not args.no_cpu)
 
     # ---- power method: 500 iterations (reference powerIteration semantics),
     #      fused persistent kernel and two kernels per iteration ----
@@ -588,6 +633,7 @@ def run_ours(args, world, rank, local):
     }
     if formats:
         result["formats_poisson"] = formats
+        result["triplet_to_crs"] = formats_load
     if extra:
         result.update(extra)
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -94,9 +94,14 @@ int pwmgpu_load_csr(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, con
                     const int32_t* col_ind, const double* vals);
 /* Replaces loadFromTriplets(input, partitions) (SparseMatrix.hpp:48).  Like
  * the reference (Util/TripletToCRS.hpp:139-142) it sorts the caller's
- * triplet arrays in place (by row, then column). */
+ * triplet arrays in place (by row, then column; entries with equal
+ * coordinates keep their input order).  The sort runs on the device. */
 int pwmgpu_load_triplets(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, int32_t* rows, int32_t* cols,
                          double* vals);
+/* The same CRS from triplet arrays already on the device (d_rows[nnz],
+ * d_cols[nnz], d_vals[nnz]), which are left unchanged; synchronous. */
+int pwmgpu_load_triplets_device(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* d_rows,
+                                const int32_t* d_cols, const double* d_vals);
 int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz);
 /* Copy the device CRS arrays back (row_start[nor+1], col_ind[nnz], vals[nnz]);
  * the reference's protected row_start / col_ind / data_arr (CRS.hpp:30-37). */

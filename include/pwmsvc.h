@@ -44,6 +44,8 @@ typedef struct {
 #define PWMSVC_SRC_CSR 0     /* host CRS arrays, copied at submit */
 #define PWMSVC_SRC_POISSON 1 /* grid_m x grid_n 5-point Poisson (Util/Poisson.hpp:32-83), built on the device */
 #define PWMSVC_SRC_RANDOM 2  /* pwmgpu_generate_random's matrix, built on the device */
+#define PWMSVC_SRC_TRIPLETS 3 /* host triplets (row_ind, col_ind, vals; square nor), copied at submit,
+                                 * turned into CRS on the device at admission (pwmgpu_load_triplets) */
 
 typedef struct {
     int32_t source;
@@ -70,6 +72,9 @@ typedef struct {
     double tol;
     int32_t precision;   /* PWMGPU_PREC_* */
     int32_t keep_vector; /* 1: keep the eigenvector on the host for pwmsvc_result */
+    /* PWMSVC_SRC_TRIPLETS: the row of each of the nnz entries (col_ind and
+     * vals as for PWMSVC_SRC_CSR, in the same entry order) */
+    const int32_t* row_ind;
 } pwmsvc_request;
 
 #define PWMSVC_QUEUED 0

@@ -174,3 +174,28 @@ def test_service_mixed_and_f32_against_oracle(svc_mod):
         assert res_r <= 2 * tol and abs(lam_r - r64.lambda_) <= 1e-10 * abs(lam_r)
     lam_r, res_r = O.rayleigh(A, u32)
     assert res_r <= 1e-4 and abs(lam_r - r64.lambda_) <= 1e-5 * abs(lam_r)
+
+
+def test_service_triplet_source_equals_csr(svc_mod):
+    """PWMSVC_SRC_TRIPLETS: shuffled triplets of a matrix, sorted into CRS on
+    the device at admission, give the same bits as the CSR request of it."""
+    t, S = svc_mod
+    A = _positive_random(3000, 6.0, 21)
+    rows = np.repeat(np.arange(A.nor, dtype=np.int32), np.diff(A.row_start))
+    p = np.random.default_rng(22).permutation(rows.size)
+    svc = S.Service(round_iterations=8)
+    a = svc.submit_csr(A, max_it=400, tol=1e-12, x0_seed=4, keep_vector=True)
+    b = svc.submit_triplets(A.nor, rows[p], A.col_ind[p], A.data[p], max_it=400, tol=1e-12, x0_seed=4,
+                            keep_vector=True)
+    svc.run_until_idle()
+    ra, ua = svc.result(a, want_vector=True)
+    rb, ub = svc.result(b, want_vector=True)
+    assert ra.state == rb.state == S.DONE and ra.iterations == rb.iterations
+    assert ra.lambda_ == rb.lambda_ and ra.residual == rb.residual
+    assert np.array_equal(ua, ub)
+    with pytest.raises(ValueError):
+        svc.submit_triplets(10, np.zeros(3), np.zeros(2), np.zeros(3))
+    # an entry out of range fails at admission, as a failed request
+    bad = svc.submit_triplets(4, np.array([0, 1, 9]), np.array([0, 1, 2]), np.ones(3), max_it=10)
+    svc.run_until_idle()
+    assert svc.result(bad).state == S.FAILED

@@ -49,6 +49,7 @@ SIGNATURES = {
     "pwmgpu_generate_random": (C.c_int, [vp, i32, C.c_uint64, C.c_int, C.c_double, C.c_double, i32, i32, i32]),
     "pwmgpu_load_csr": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_load_triplets": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
+    "pwmgpu_load_triplets_device": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_dims": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64)]),
     "pwmgpu_get_csr": (C.c_int, [vp, vp, vp, vp]),
     "pwmgpu_mv": (C.c_int, [vp, vp, vp]),

@@ -113,6 +113,25 @@ cudaError_t launch_random_fill(const uint64_t* thr, int max_len, int n, uint64_t
 long long scan_scratch_elems(long long n);
 cudaError_t launch_inclusive_scan(int32_t* a, long long n, int32_t* scratch, cudaStream_t st);
 
+// triplet.cu: triplet -> CRS on the device (stable LSD radix sort by (row, col))
+struct TripletScan {
+    unsigned long long bad;   // first entry with a row or column out of range (~0 when none)
+    unsigned int unsorted_rc; // input not sorted by (row, col)
+    unsigned int unsorted_c;  // input not sorted by column
+};
+cudaError_t launch_triplet_scan(const int32_t* rows, const int32_t* cols, long long nnz, int32_t nor, int32_t noc,
+                                int32_t* cnt, TripletScan* flags, int sm_count, cudaStream_t st);
+long long triplet_sort_table_elems(long long nnz);
+int triplet_sort_passes(int32_t nor, int32_t noc, bool col_passes);
+cudaError_t launch_triplet_sort(const int32_t* rows, const int32_t* cols, long long nnz, int32_t nor, int32_t noc,
+                                bool col_passes, unsigned long long* keys_a, int32_t* src_a,
+                                unsigned long long* keys_b, int32_t* src_b, int32_t* tab, int32_t* scan_scratch,
+                                unsigned long long** keys_sorted, int32_t** src_sorted, int sm_count,
+                                cudaStream_t st);
+cudaError_t launch_triplet_gather(const unsigned long long* keys, const int32_t* src, const double* vals,
+                                  long long nnz, int32_t* col, double* val, int32_t* rows_out, int sm_count,
+                                  cudaStream_t st);
+
 // batch.cu: one round (`steps` power steps + the residual pass) of every slot
 // of a class table; seeded uniform start vectors
 struct BatchTable;

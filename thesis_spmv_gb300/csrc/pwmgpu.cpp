@@ -797,6 +797,116 @@ int pwmgpu_generate_random(pwmgpu_matrix* m, int32_t n, uint64_t seed, int lengt
     return build_plan(m);
 }
 
+}  // extern "C"
+namespace {
+
+struct TripletIn {
+    int32_t* rows = nullptr;
+    int32_t* cols = nullptr;
+    double* vals = nullptr;
+    void release() {
+        dfree(rows);
+        dfree(cols);
+        dfree(vals);
+    }
+};
+
+// Util/TripletToCRS.hpp:135-172 on the device: CRS with rows ascending and
+// columns ascending within a row (duplicates in input order) from device
+// triplet arrays, which are not modified.  With host arrays h_* the sorted
+// triplet is also written back there, as the reference sorts its caller's
+// triplet in place (TripletToCRS.hpp:139-142).  Entries are range-checked
+// before anything of the previous matrix is released.
+int load_triplets_dev(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* rows,
+                      const int32_t* cols, const double* vals, int32_t* h_rows, int32_t* h_cols, double* h_vals) {
+    int32_t* cnt = nullptr;
+    int32_t* scan_scratch = nullptr;
+    TripletScan* dflags = nullptr;
+    unsigned long long *keys_a = nullptr, *keys_b = nullptr;
+    int32_t *src_a = nullptr, *src_b = nullptr, *tab = nullptr;
+    bool matrix_touched = false;
+    int rc = PWMGPU_OK;
+    do {
+        const long long tab_elems = triplet_sort_table_elems(nnz);
+        const long long scan_n = std::max<long long>(nor, tab_elems);
+        if ((rc = dalloc(&cnt, (size_t)nor + 1)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&scan_scratch, (size_t)scan_scratch_elems(scan_n))) != PWMGPU_OK) break;
+        if ((rc = dalloc(&dflags, 1)) != PWMGPU_OK) break;
+        TripletScan flags{~0ull, 0u, 0u};
+        cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ((size_t)nor + 1), m->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dflags, &flags, sizeof flags, cudaMemcpyHostToDevice, m->stream);
+        if (e == cudaSuccess) e = launch_triplet_scan(rows, cols, nnz, nor, noc, cnt, dflags, m->sm_count, m->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, dflags, sizeof flags, cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "triplet scan: %s", cudaGetErrorString(e)); break; }
+        if (flags.bad != ~0ull) {
+            const long long k = (long long)flags.bad;
+            int32_t r = 0, c = 0;
+            e = cudaMemcpy(&r, rows + k, sizeof r, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess) e = cudaMemcpy(&c, cols + k, sizeof c, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "triplet check: %s", cudaGetErrorString(e)); break; }
+            if (r < 0 || r >= nor)
+                rc = fail(PWMGPU_ERR_INVALID, "row %d at entry %lld out of range", r, k);
+            else
+                rc = fail(PWMGPU_ERR_INVALID, "column %d at entry %lld out of range", c, k);
+            break;
+        }
+        e = launch_inclusive_scan(cnt + 1, nor, scan_scratch, m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "row scan: %s", cudaGetErrorString(e)); break; }
+        matrix_touched = true;
+        if ((rc = alloc_matrix(m, nor, noc, nnz)) != PWMGPU_OK) break;
+        e = cudaMemcpyAsync(m->M.row_start, cnt, sizeof(int32_t) * ((size_t)nor + 1), cudaMemcpyDeviceToDevice,
+                            m->stream);
+        if (e == cudaSuccess && nnz > 0 && !flags.unsorted_rc) {
+            // already in CRS order: the columns and values are the input
+            e = cudaMemcpyAsync(m->M.col, cols, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToDevice, m->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(m->M.val, vals, sizeof(double) * (size_t)nnz, cudaMemcpyDeviceToDevice,
+                                    m->stream);
+        } else if (e == cudaSuccess && nnz > 0) {
+            if ((rc = dalloc(&keys_a, (size_t)nnz)) != PWMGPU_OK) break;
+            if ((rc = dalloc(&keys_b, (size_t)nnz)) != PWMGPU_OK) break;
+            if ((rc = dalloc(&src_a, (size_t)nnz)) != PWMGPU_OK) break;
+            if ((rc = dalloc(&src_b, (size_t)nnz)) != PWMGPU_OK) break;
+            if ((rc = dalloc(&tab, (size_t)tab_elems)) != PWMGPU_OK) break;
+            unsigned long long* keys = nullptr;
+            int32_t* src = nullptr;
+            e = launch_triplet_sort(rows, cols, nnz, nor, noc, flags.unsorted_c != 0, keys_a, src_a, keys_b, src_b,
+                                    tab, scan_scratch, &keys, &src, m->sm_count, m->stream);
+            // the sorted rows (for the caller's triplet) overwrite the source indices
+            if (e == cudaSuccess)
+                e = launch_triplet_gather(keys, src, vals, nnz, m->M.col, m->M.val, h_rows ? src : nullptr,
+                                          m->sm_count, m->stream);
+            if (e == cudaSuccess && h_rows)
+                e = cudaMemcpyAsync(h_rows, src, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToHost, m->stream);
+            if (e == cudaSuccess && h_cols)
+                e = cudaMemcpyAsync(h_cols, m->M.col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyDeviceToHost,
+                                    m->stream);
+            if (e == cudaSuccess && h_vals)
+                e = cudaMemcpyAsync(h_vals, m->M.val, sizeof(double) * (size_t)nnz, cudaMemcpyDeviceToHost,
+                                    m->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "triplet to CRS: %s", cudaGetErrorString(e)); break; }
+    } while (0);
+    dfree(cnt);
+    dfree(scan_scratch);
+    dfree(dflags);
+    dfree(keys_a);
+    dfree(keys_b);
+    dfree(src_a);
+    dfree(src_b);
+    dfree(tab);
+    if (rc != PWMGPU_OK) {
+        if (matrix_touched) m->release_matrix();
+        return rc;
+    }
+    return build_plan(m);
+}
+
+}  // namespace
+extern "C" {
+
 int pwmgpu_load_csr(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
                     const int32_t* col_ind, const double* vals) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
@@ -825,53 +935,34 @@ int pwmgpu_load_triplets(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
     TRY(check_sizes(nor, noc, nnz));
     if (nnz > 0 && (!rows || !cols || !vals)) return fail(PWMGPU_ERR_INVALID, "null triplet array");
-    for (int32_t k = 0; k < nnz; ++k) {
-        if (rows[k] < 0 || rows[k] >= nor) return fail(PWMGPU_ERR_INVALID, "row %d at entry %d out of range", rows[k], k);
-        if (cols[k] < 0 || cols[k] >= noc) return fail(PWMGPU_ERR_INVALID, "column %d at entry %d out of range", cols[k], k);
-    }
-    // Util/TripletToCRS.hpp:135-172: rows ascending, columns ascending within
-    // a row (for unique coordinates the reference's randomised quicksort
-    // yields exactly this order).  Counting sort by row, then each row by
-    // column; the caller's arrays are left sorted, as in the reference.
-    std::vector<int32_t> row_start((size_t)nor + 1, 0);
-    for (int32_t k = 0; k < nnz; ++k) row_start[(size_t)rows[k] + 1]++;
-    for (int32_t i = 0; i < nor; ++i) row_start[(size_t)i + 1] += row_start[i];
-    std::vector<int32_t> pos(row_start.begin(), row_start.end() - 1);
-    std::vector<int32_t> c2((size_t)nnz);
-    std::vector<double> v2((size_t)nnz);
-    for (int32_t k = 0; k < nnz; ++k) {
-        int32_t p = pos[rows[k]]++;
-        c2[p] = cols[k];
-        v2[p] = vals[k];
-    }
-    std::vector<std::pair<int32_t, int32_t>> tmp;
-    for (int32_t i = 0; i < nor; ++i) {
-        int32_t a = row_start[i], b = row_start[(size_t)i + 1];
-        if (b - a < 2) continue;
-        bool sorted = true;
-        for (int32_t k = a + 1; k < b; ++k)
-            if (c2[k] < c2[k - 1]) { sorted = false; break; }
-        if (sorted) continue;
-        tmp.resize(b - a);
-        for (int32_t k = a; k < b; ++k) tmp[k - a] = {c2[k], k};
-        std::stable_sort(tmp.begin(), tmp.end(),
-                         [](const std::pair<int32_t, int32_t>& p, const std::pair<int32_t, int32_t>& q) {
-                             return p.first < q.first;
-                         });
-        std::vector<double> vv(b - a);
-        for (int32_t k = 0; k < b - a; ++k) vv[k] = v2[tmp[k].second];
-        for (int32_t k = 0; k < b - a; ++k) {
-            c2[a + k] = tmp[k].first;
-            v2[a + k] = vv[k];
+    // the triplet goes up, is sorted on the device and comes back sorted
+    TripletIn in;
+    int rc = PWMGPU_OK;
+    do {
+        if ((rc = dalloc(&in.rows, (size_t)nnz)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&in.cols, (size_t)nnz)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&in.vals, (size_t)nnz)) != PWMGPU_OK) break;
+        cudaError_t e = cudaSuccess;
+        if (nnz > 0) {
+            e = cudaMemcpyAsync(in.rows, rows, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, m->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(in.cols, cols, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, m->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(in.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, m->stream);
         }
-    }
-    for (int32_t i = 0; i < nor; ++i)
-        for (int32_t k = row_start[i]; k < row_start[(size_t)i + 1]; ++k) rows[k] = i;
-    if (nnz > 0) {
-        std::memcpy(cols, c2.data(), sizeof(int32_t) * (size_t)nnz);
-        std::memcpy(vals, v2.data(), sizeof(double) * (size_t)nnz);
-    }
-    return pwmgpu_load_csr(m, nor, noc, nnz, row_start.data(), c2.data(), v2.data());
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "triplet upload: %s", cudaGetErrorString(e)); break; }
+        rc = load_triplets_dev(m, nor, noc, nnz, in.rows, in.cols, in.vals, rows, cols, vals);
+    } while (0);
+    in.release();
+    return rc;
+}
+
+int pwmgpu_load_triplets_device(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* d_rows,
+                                const int32_t* d_cols, const double* d_vals) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    TRY(check_sizes(nor, noc, nnz));
+    if (nnz > 0 && (!d_rows || !d_cols || !d_vals)) return fail(PWMGPU_ERR_INVALID, "null triplet array");
+    return load_triplets_dev(m, nor, noc, nnz, d_rows, d_cols, d_vals, nullptr, nullptr, nullptr);
 }
 
 int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz) {

@@ -38,7 +38,7 @@ constexpr double kSvcSwitchRel = 2e-6;
 struct Req {
     int64_t id = 0;
     pwmsvc_request spec{};
-    std::vector<int32_t> rs, ci;
+    std::vector<int32_t> rs, ci, ri;
     std::vector<double> vals, x0;
     int state = PWMSVC_QUEUED;
     int error = PWMGPU_OK;
@@ -150,6 +150,14 @@ int admit(pwmsvc* S, Req* r) {
     } else if (q.source == PWMSVC_SRC_RANDOM) {
         TRY(pwmgpu_generate_random(m, q.n, q.seed, q.length_dist, q.mean_len, q.sigma, q.max_len, q.band_permille,
                                    q.band_half));
+    } else if (q.source == PWMSVC_SRC_TRIPLETS) {
+        TRY(pwmgpu_load_triplets(m, q.nor, q.nor, q.nnz, r->ri.data(), r->ci.data(), r->vals.data()));
+        r->ri.clear();
+        r->ri.shrink_to_fit();
+        r->ci.clear();
+        r->ci.shrink_to_fit();
+        r->vals.clear();
+        r->vals.shrink_to_fit();
     } else {
         TRY(pwmgpu_load_csr(m, q.nor, q.nor, q.nnz, r->rs.data(), r->ci.data(), r->vals.data()));
         r->rs.clear();
@@ -469,6 +477,15 @@ int pwmsvc_submit(pwmsvc* s, const pwmsvc_request* q, int64_t* id) {
             r->ci.assign(q->col_ind, q->col_ind + nnz);
             r->vals.assign(q->vals, q->vals + nnz);
             break;
+        case PWMSVC_SRC_TRIPLETS:
+            if (q->nor < 1 || q->nnz < 0 || (q->nnz > 0 && (!q->row_ind || !q->col_ind || !q->vals)))
+                return fail(PWMGPU_ERR_INVALID, "bad triplet request");
+            nor = q->nor;
+            nnz = q->nnz;
+            r->ri.assign(q->row_ind, q->row_ind + nnz);
+            r->ci.assign(q->col_ind, q->col_ind + nnz);
+            r->vals.assign(q->vals, q->vals + nnz);
+            break;
         case PWMSVC_SRC_POISSON:
             if (q->grid_m < 1 || q->grid_n < 1) return fail(PWMGPU_ERR_INVALID, "bad Poisson grid");
             nor = (long long)q->grid_m * q->grid_n;
@@ -483,6 +500,7 @@ int pwmsvc_submit(pwmsvc* s, const pwmsvc_request* q, int64_t* id) {
             return fail(PWMGPU_ERR_INVALID, "unknown source %d", q->source);
     }
     r->spec.row_start = nullptr;
+    r->spec.row_ind = nullptr;
     r->spec.col_ind = nullptr;
     r->spec.vals = nullptr;
     if (q->x0) r->x0.assign(q->x0, q->x0 + nor);

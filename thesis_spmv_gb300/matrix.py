@@ -162,6 +162,12 @@ class CudaSparseMatrix:
                                               _ptr(triplet.row_coord), _ptr(triplet.col_coord),
                                               _ptr(triplet.data)), "loadFromTriplets")
 
+    def loadFromDeviceTriplets(self, nor, noc, nnz, rows_ptr, cols_ptr, vals_ptr):
+        """CRS from triplet arrays already on the device (int32 rows / cols,
+        float64 values, e.g. torch tensors' data_ptr()); they stay unchanged."""
+        check(_lib.lib().pwmgpu_load_triplets_device(self._h, int(nor), int(noc), int(nnz), rows_ptr, cols_ptr,
+                                                     vals_ptr), "loadFromDeviceTriplets")
+
     def loadCSR(self, nor, noc, row_start, col_ind, data):
         rs = np.ascontiguousarray(row_start, _I32)
         ci = np.ascontiguousarray(col_ind, _I32)

@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib
 from ._lib import PREC_F64, check
 
-SRC_CSR, SRC_POISSON, SRC_RANDOM = 0, 1, 2
+SRC_CSR, SRC_POISSON, SRC_RANDOM, SRC_TRIPLETS = 0, 1, 2, 3
 QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
 
 
@@ -27,7 +27,8 @@ class Request(C.Structure):
                 ("n", C.c_int32), ("seed", C.c_uint64), ("length_dist", C.c_int32), ("mean_len", C.c_double),
                 ("sigma", C.c_double), ("max_len", C.c_int32), ("band_permille", C.c_int32),
                 ("band_half", C.c_int32), ("x0", C.c_void_p), ("x0_seed", C.c_uint64), ("max_it", C.c_int32),
-                ("tol", C.c_double), ("precision", C.c_int32), ("keep_vector", C.c_int32)]
+                ("tol", C.c_double), ("precision", C.c_int32), ("keep_vector", C.c_int32),
+                ("row_ind", C.c_void_p)]
 
 
 class Result(C.Structure):
@@ -133,6 +134,21 @@ class Service:
         req.source = SRC_CSR
         req.nor, req.nnz = int(A.nor), int(ci.size)
         req.row_start, req.col_ind, req.vals = rs.ctypes.data, ci.ctypes.data, d.ctypes.data
+        self._common(req, max_it, tol, precision, x0_seed, keep_vector)
+        return self._submit(req, x0, keep_vector)
+
+    def submit_triplets(self, n, rows, cols, vals, max_it=2000, tol=1e-10, precision=PREC_F64, x0=None, x0_seed=0,
+                        keep_vector=False):
+        """An n x n matrix as triplets (any entry order), sorted into CRS on the device at admission."""
+        ri = np.ascontiguousarray(rows, np.int32)
+        ci = np.ascontiguousarray(cols, np.int32)
+        d = np.ascontiguousarray(vals, np.float64)
+        if not (ri.size == ci.size == d.size):
+            raise ValueError("rows, cols and vals differ in length")
+        req = Request()
+        req.source = SRC_TRIPLETS
+        req.nor, req.nnz = int(n), int(ci.size)
+        req.row_ind, req.col_ind, req.vals = ri.ctypes.data, ci.ctypes.data, d.ctypes.data
         self._common(req, max_it, tol, precision, x0_seed, keep_vector)
         return self._submit(req, x0, keep_vector)
 
