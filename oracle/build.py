@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpwmref.so")
+REF_STATS = os.path.join(HERE, "_ref", "calc_stats")
 REF_DIR = os.environ.get("PWM_REFERENCE_DIR", "/root/reference")
 
 
@@ -34,8 +35,11 @@ def build_ref(force=False):
     if not os.path.isdir(os.path.join(REF_DIR, "Matrix")):
         return None
     if not force and os.path.exists(REF_LIB):
-        srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "build_ref.sh")]
-        if os.path.getmtime(REF_LIB) >= max(os.path.getmtime(p) for p in srcs):
+        srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "ref_stats_main.cpp"),
+                os.path.join(HERE, "build_ref.sh")]
+        outs = [REF_LIB, REF_STATS]
+        if all(os.path.exists(o) for o in outs) and \
+                min(os.path.getmtime(o) for o in outs) >= max(os.path.getmtime(p) for p in srcs):
             return REF_LIB
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
     return REF_LIB

@@ -778,3 +778,76 @@ void orc_uniform_vector(int32_t n, uint64_t seed, double* x) {
     for (int32_t i = 0; i < n; ++i)
         x[i] = (double)(rg_mix(seed + 0x9e3779b97f4a7c15ull * (uint64_t)(i + 1)) >> 11) * (1.0 / 9007199254740992.0);
 }
+
+/* ------------------------------------------------------------------ */
+/* Matrix statistics                                                    */
+/* ------------------------------------------------------------------ */
+
+int orc_calc_stats(int64_t nnz, int32_t nor, const int32_t* rows, const int32_t* cols, double* out) {
+    /* Util_Scripts/calc_stats.cpp:45-98 with index_t = uint32_t
+     * (Util/Constants.hpp:38): counters are uint32, each variance term is
+     * pow(count - avg, 2) / n (x * x here: both correctly rounded), summed in
+     * the script's loop order. */
+    const uint32_t n = (uint32_t)nor;
+    const double rows_avg = (double)nnz / (double)n;
+    const uint32_t lg = (uint32_t)ceil(log2(sqrt((double)n)));
+    const uint32_t bits = 3 + lg < 16 ? 3 + lg : 16;
+    const uint32_t bs = (uint32_t)1 << bits;
+    uint32_t nb = n / bs + (n % bs != 0);
+    uint32_t* rows_nnz = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
+    uint32_t* block_nnz = (uint32_t*)calloc((size_t)nb * nb ? (size_t)nb * nb : 1, sizeof(uint32_t));
+    if (!rows_nnz || !block_nnz) {
+        free(rows_nnz);
+        free(block_nnz);
+        return -1;
+    }
+    for (int64_t k = 0; k < nnz; ++k) {
+        const uint32_t r = (uint32_t)rows[k], c = (uint32_t)cols[k];
+        if (r / bs >= nb || c / bs >= nb) {
+            free(rows_nnz);
+            free(block_nnz);
+            return -1;
+        }
+        rows_nnz[r]++;
+        block_nnz[(size_t)(r / bs) * nb + c / bs]++;
+    }
+    double rows_var = 0.;
+    for (uint32_t i = 0; i < n; ++i) {
+        const double d = (double)rows_nnz[i] - rows_avg;
+        rows_var += d * d / (double)n;
+    }
+    const uint32_t stride = nb;
+    if (n % bs != 0) nb--;
+    const double nb2 = (double)nb * (double)nb;
+    double block_avg = 0., block_row_avg = 0.;
+    uint32_t* block_row_nnz = (uint32_t*)calloc(nb ? nb : 1, sizeof(uint32_t));
+    for (uint32_t i = 0; i < nb; ++i) {
+        for (uint32_t j = 0; j < nb; ++j) {
+            block_row_nnz[i] += block_nnz[(size_t)i * stride + j];
+            block_avg += (double)block_nnz[(size_t)i * stride + j] / nb2;
+        }
+        block_row_avg += (double)block_row_nnz[i] / (double)nb;
+    }
+    double block_var = 0.;
+    int balanced = 1;
+    for (uint32_t i = 0; i < nb; ++i) {
+        if ((double)block_row_nnz[i] > 2 * block_row_avg) balanced = 0;
+        for (uint32_t j = 0; j < nb; ++j) {
+            const double d = (double)block_nnz[(size_t)i * stride + j] - block_avg;
+            block_var += d * d / nb2;
+        }
+    }
+    out[0] = (double)n;
+    out[1] = (double)nnz;
+    out[2] = rows_avg;
+    out[3] = rows_var;
+    out[4] = block_avg;
+    out[5] = block_var;
+    out[6] = balanced;
+    out[7] = bits;
+    out[8] = nb;
+    free(rows_nnz);
+    free(block_nnz);
+    free(block_row_nnz);
+    return 0;
+}

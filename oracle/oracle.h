@@ -119,6 +119,14 @@ int64_t orc_random_crs(int32_t n, uint64_t seed, int kind, double mean, double s
 /* The batched service's seeded start vector (uniform in [0, 1)). */
 void orc_uniform_vector(int32_t n, uint64_t seed, double* x);
 
+/* Matrix statistics (Util_Scripts/calc_stats.cpp:45-98), in the script's
+ * order of operations.  out: size, nnz, rows_avg, rows_var, block_avg,
+ * block_var, balanced (1/0), block_bits, whole blocks per side (the script's
+ * nb_blocks after its "whole blocks only" decrement).  Square matrices (the
+ * script indexes column blocks by the row count); returns -1 if a column block
+ * falls outside, or the block table cannot be allocated. */
+int orc_calc_stats(int64_t nnz, int32_t nor, const int32_t* rows, const int32_t* cols, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,8 @@ def lib():
                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.orc_load_bin.restype = C.c_int64
         L.orc_load_bin.argtypes = [C.c_char_p, C.c_int32, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        L.orc_calc_stats.restype = C.c_int
+        L.orc_calc_stats.argtypes = [C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, F64P]
         _lib = L
     return _lib
 
@@ -305,3 +307,22 @@ def row_error_bound(A, x, u=2.0 ** -53):
     rows = np.repeat(np.arange(A.nor), np.diff(A.row_start))
     np.add.at(s, rows, prod)
     return 2.0 * rl * u * s
+
+
+STAT_KEYS = ("size", "nnz", "rows_avg", "rows_var", "block_avg", "block_var", "balanced", "block_bits",
+             "nb_blocks")
+
+
+def calc_stats(nor, rows, cols):
+    """Util_Scripts/calc_stats.cpp:45-98 on a square triplet: dict of STAT_KEYS."""
+    r = np.ascontiguousarray(rows, np.int32)
+    c = np.ascontiguousarray(cols, np.int32)
+    out = np.zeros(9)
+    rc = lib().orc_calc_stats(r.size, nor, r.ctypes.data if r.size else None, c.ctypes.data if c.size else None,
+                              out)
+    if rc != 0:
+        raise ValueError("calc_stats: column block out of range or allocation failed")
+    d = dict(zip(STAT_KEYS, out.tolist()))
+    for k in ("size", "nnz", "balanced", "block_bits", "nb_blocks"):
+        d[k] = int(d[k])
+    return d

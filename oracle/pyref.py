@@ -201,3 +201,41 @@ class Matrix:
 
 def hilbert(size, row, col):
     return int(lib().ref_hilbert(size, row, col))
+
+
+def calc_stats(nor, noc, rows, cols, vals):
+    """Run the reference's calc_stats (oracle/_ref/calc_stats) on a triplet;
+    returns the printed figures (17 significant digits) as a dict with the
+    keys of pyoracle.STAT_KEYS (without block_bits / nb_blocks)."""
+    import subprocess
+    import tempfile
+    from .build import REF_STATS
+    if lib() is None or not os.path.exists(REF_STATS):
+        raise RuntimeError("reference calc_stats not built")
+    r = np.ascontiguousarray(rows, np.int32)
+    c = np.ascontiguousarray(cols, np.int32)
+    v = np.ascontiguousarray(vals, np.float64)
+    tmpdir = os.path.join(os.path.dirname(REF_STATS), "tmp")
+    os.makedirs(tmpdir, exist_ok=True)
+    with tempfile.NamedTemporaryFile(dir=tmpdir, suffix=".trip", delete=False) as f:
+        np.array([nor, noc, r.size], np.int32).tofile(f)
+        r.tofile(f)
+        c.tofile(f)
+        v.tofile(f)
+        path = f.name
+    try:
+        out = subprocess.run([REF_STATS, path], capture_output=True, text=True, check=True).stdout
+    finally:
+        os.remove(path)
+    keys = {"Size:": "size", "Nonzeros:": "nnz", "Average nnz per row:": "rows_avg",
+            "Variance of nnz per row:": "rows_var", "Average nnz per block:": "block_avg",
+            "Variance of nnz per block:": "block_var"}
+    d = {}
+    for line in out.splitlines():
+        for label, key in keys.items():
+            if line.startswith(label):
+                d[key] = float(line[len(label):])
+        if "balanced for CSB" in line:
+            d["balanced"] = 0 if "unbalanced" in line else 1
+    d["size"], d["nnz"] = int(d["size"]), int(d["nnz"])
+    return d

@@ -9,6 +9,9 @@ Writes
                            input, operation, tolerance and the golden vector
                            ("precomputed using matlab"), read as text.
   matrices/             -- the six input fixtures of Test_input/, as files.
+  ref_stats.json        -- what the reference's Util_Scripts/calc_stats.cpp
+                           prints for the matrices of
+                           tests/golden_cases.stats_cases() (--stats: only these).
   ref_outputs.npz       -- outputs of the UNMODIFIED reference classes
                            (oracle/_ref) on small seeded inputs: CRS arrays,
                            merge-path coordinates, CSB and CO-H arrays, mv and
@@ -148,5 +151,24 @@ def main(ref_dir):
     print("ref_outputs keys:", len(out), "bytes:", os.path.getsize(os.path.join(HERE, "ref_outputs.npz")))
 
 
+def make_stats():
+    """ref_stats.json: the figures the reference's Util_Scripts/calc_stats.cpp
+    prints (built unmodified into oracle/_ref/calc_stats, 17 significant
+    digits) for tests/golden_cases.stats_cases()."""
+    from oracle import pyref as R
+    sys.path.insert(0, os.path.dirname(HERE))
+    from golden_cases import stats_cases
+    res = {}
+    for name, n, r, c, v in stats_cases():
+        res[name] = R.calc_stats(n, n, r, c, v)
+    with open(os.path.join(HERE, "ref_stats.json"), "w") as f:
+        json.dump(dict(generated_by="tests/golden/make_golden.py --stats", cases=res), f, indent=1)
+    print("stats cases:", len(res))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PWM_REFERENCE_DIR", "/root/reference"))
+    if "--stats" in sys.argv:
+        make_stats()
+    else:
+        main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PWM_REFERENCE_DIR", "/root/reference"))
+        make_stats()

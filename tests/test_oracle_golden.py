@@ -112,3 +112,19 @@ def test_oracle_plants_a_mistake_is_caught():
     y = O.crs_mv(A, np.ones(A.noc))
     y[3] += 1e-9
     assert not boost_close(y, np.array(case["golden"]), case["tolerance"]).all()
+
+
+def test_calc_stats_against_reference_outputs():
+    """The oracle's Util_Scripts/calc_stats.cpp restatement prints the same
+    doubles as the reference's own script (tests/golden/ref_stats.json)."""
+    from golden_cases import ref_stats, stats_cases
+    ref = ref_stats()
+    names = set()
+    for name, n, r, c, v in stats_cases():
+        got = O.calc_stats(n, r, c)
+        want = ref[name]
+        for k in ("size", "nnz", "rows_avg", "rows_var", "block_avg", "block_var", "balanced"):
+            assert got[k] == want[k], (name, k, got[k], want[k])
+        names.add(name)
+    assert names == set(ref)
+    assert any(w["balanced"] == 0 for w in ref.values()) and any(w["balanced"] == 1 for w in ref.values())

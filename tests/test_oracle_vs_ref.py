@@ -63,3 +63,18 @@ def test_power_matches_reference_bitwise():
         xo, yo = O.power(A, x, it)
         xr, yr = M.power(x, it)
         assert np.array_equal(xo, xr) and np.array_equal(yo, yr)
+
+
+@pytest.mark.parametrize("n,seed", [(777, 1), (3000, 2), (70000, 3)])
+def test_calc_stats_matches_reference(n, seed):
+    """Random square triplets (duplicates included) through the reference's
+    calc_stats and the oracle: the same doubles."""
+    rng = np.random.default_rng(seed)
+    nnz = n * 7
+    r = rng.integers(0, n, nnz).astype(np.int32)
+    c = np.where(rng.random(nnz) < 0.5, r, rng.integers(0, n, nnz)).astype(np.int32)
+    v = rng.random(nnz)
+    got = O.calc_stats(n, r, c)
+    want = R.calc_stats(n, n, r, c, v)
+    for k, w in want.items():
+        assert got[k] == w, (k, got[k], w)
