@@ -254,6 +254,7 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
         fm[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
         del F
     out["irregular"]["formats"] = fm
+    out["irregular"]["stats"] = M.stats()
     x0 = np.random.default_rng(20261203).random(N)
     solves = {}
     lam = {}
@@ -634,6 +635,7 @@ def run_ours(args, world, rank, local):
     if formats:
         result["formats_poisson"] = formats
         result["triplet_to_crs"] = formats_load
+        result["poisson_stats"] = M.stats()
     if extra:
         result.update(extra)
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -107,6 +107,28 @@ int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz
  * the reference's protected row_start / col_ind / data_arr (CRS.hpp:30-37). */
 int pwmgpu_get_csr(pwmgpu_matrix* m, int32_t* row_start, int32_t* col_ind, double* vals);
 
+/* Matrix statistics of Util_Scripts/calc_stats.cpp:45-98, computed on the
+ * device from the loaded matrix (any format).  Blocks are squares of side
+ * 2^block_bits, block_bits = min(16, 3 + ceil(log2 sqrt(nor))); the block
+ * figures cover the nb_blocks x nb_blocks whole blocks (columns beyond them
+ * are not counted).  Counts are exact; rows_var, block_avg and block_var are
+ * summed in a fixed parallel order (deterministic; the script sums
+ * sequentially), balanced uses the script's own order for the average block
+ * row. */
+typedef struct {
+    int64_t size;        /* nor */
+    int64_t nnz;
+    double rows_avg;     /* nonzeros per row: mean */
+    double rows_var;     /* nonzeros per row: population variance */
+    double block_avg;    /* nonzeros per whole block: mean */
+    double block_var;    /* nonzeros per whole block: population variance */
+    int32_t balanced;    /* 1: no block row holds more than twice the average block row */
+    int32_t block_bits;
+    int32_t nb_blocks;   /* whole blocks per side */
+    int32_t max_row_nnz; /* longest row */
+} pwmgpu_matrix_stats;
+int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out);
+
 /* Replaces mv(x, y) (SparseMatrix.hpp:57, CRS.hpp:99-109): y = A x with
  * caller-owned host arrays x[noc], y[nor]; synchronous. */
 int pwmgpu_mv(pwmgpu_matrix* m, const double* x, double* y);

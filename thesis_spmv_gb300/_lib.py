@@ -29,6 +29,12 @@ class PwmGpuError(RuntimeError):
         super().__init__(msg)
 
 
+class MatrixStats(C.Structure):
+    _fields_ = [("size", C.c_int64), ("nnz", C.c_int64), ("rows_avg", C.c_double), ("rows_var", C.c_double),
+                ("block_avg", C.c_double), ("block_var", C.c_double), ("balanced", C.c_int32),
+                ("block_bits", C.c_int32), ("nb_blocks", C.c_int32), ("max_row_nnz", C.c_int32)]
+
+
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("iterations_low", C.c_int32), ("converged", C.c_int32),
                 ("precision", C.c_int32), ("lambda_", C.c_double), ("residual", C.c_double)]
@@ -51,6 +57,7 @@ SIGNATURES = {
     "pwmgpu_load_triplets": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_load_triplets_device": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_dims": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64)]),
+    "pwmgpu_stats": (C.c_int, [vp, C.POINTER(MatrixStats)]),
     "pwmgpu_get_csr": (C.c_int, [vp, vp, vp, vp]),
     "pwmgpu_mv": (C.c_int, [vp, vp, vp]),
     "pwmgpu_mv_device": (C.c_int, [vp, vp, vp]),

@@ -132,6 +132,16 @@ cudaError_t launch_triplet_gather(const unsigned long long* keys, const int32_t*
                                   long long nnz, int32_t* col, double* val, int32_t* rows_out, int sm_count,
                                   cudaStream_t st);
 
+// stats.cu: Util_Scripts/calc_stats.cpp figures on the device
+struct StatsDev {
+    double rows_var, block_avg, block_var;
+    int max_row_nnz, balanced;
+};
+int stats_row_ctas(int n);
+cudaError_t launch_matrix_stats(const int32_t* row_start, const int32_t* col, int n, double avg, int bits, int nbw,
+                                unsigned int* blocks, long long* brow, double* row_partials, double* blk_partials,
+                                StatsDev* out, cudaStream_t st);
+
 // batch.cu: one round (`steps` power steps + the residual pass) of every slot
 // of a class table; seeded uniform start vectors
 struct BatchTable;

@@ -965,6 +965,70 @@ int pwmgpu_load_triplets_device(pwmgpu_matrix* m, int32_t nor, int32_t noc, int3
     return load_triplets_dev(m, nor, noc, nnz, d_rows, d_cols, d_vals, nullptr, nullptr, nullptr);
 }
 
+int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out) {
+    if (!m || !out) return fail(PWMGPU_ERR_INVALID, "null handle or output");
+    const long long n = m->M.nor, nnz = m->M.nnz;
+    if (!m->loaded || n <= 0 || !m->M.row_start)
+        return fail(PWMGPU_ERR_INVALID, "statistics need a loaded, non-empty matrix");
+    // Util_Scripts/calc_stats.cpp:45-58
+    const double avg = (double)nnz / (double)n;
+    const int lg = (int)std::ceil(std::log2(std::sqrt((double)n)));
+    const int bits = std::min(16, 3 + lg);
+    const long long nbw = n >> bits;  // whole blocks (the script's nb_blocks after :70-73)
+    unsigned int* blocks = nullptr;
+    long long* brow = nullptr;
+    double *rp = nullptr, *bp = nullptr;
+    StatsDev* dst = nullptr;
+    int32_t* tcol = nullptr;
+    double* tval = nullptr;
+    const int32_t* col = m->M.col;
+    int rc = PWMGPU_OK;
+    StatsDev h{};
+    do {
+        if (nbw > 0 && nnz > 0 && !col) {
+            // the merge format keeps only its lane-interleaved copy of the
+            // columns: bring them back to CRS order for the block pass
+            if ((rc = dalloc(&tcol, (size_t)nnz)) != PWMGPU_OK) break;
+            if ((rc = dalloc(&tval, (size_t)nnz)) != PWMGPU_OK) break;
+            cudaError_t e = launch_mli_unpermute(m->P, tcol, tval, m->sm_count, m->stream);
+            if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "matrix statistics: %s", cudaGetErrorString(e)); break; }
+            col = tcol;
+        }
+        if ((rc = dalloc(&blocks, (size_t)(nbw * nbw))) != PWMGPU_OK) break;
+        if ((rc = dalloc(&brow, (size_t)nbw)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&rp, (size_t)stats_row_ctas((int)n))) != PWMGPU_OK) break;
+        if ((rc = dalloc(&bp, (size_t)nbw)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&dst, 1)) != PWMGPU_OK) break;
+        cudaError_t e = cudaMemsetAsync(blocks, 0, sizeof(unsigned int) * (size_t)(nbw * nbw), m->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(dst, 0, sizeof(StatsDev), m->stream);
+        if (e == cudaSuccess)
+            e = launch_matrix_stats(m->M.row_start, col, (int)n, avg, bits, (int)nbw, blocks, brow, rp, bp, dst,
+                                    m->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dst, sizeof h, cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        if (e != cudaSuccess) rc = fail(PWMGPU_ERR_CUDA, "matrix statistics: %s", cudaGetErrorString(e));
+    } while (0);
+    dfree(blocks);
+    dfree(brow);
+    dfree(rp);
+    dfree(bp);
+    dfree(dst);
+    dfree(tcol);
+    dfree(tval);
+    if (rc != PWMGPU_OK) return rc;
+    out->size = n;
+    out->nnz = nnz;
+    out->rows_avg = avg;
+    out->rows_var = h.rows_var;
+    out->block_avg = h.block_avg;
+    out->block_var = h.block_var;
+    out->balanced = h.balanced;
+    out->block_bits = bits;
+    out->nb_blocks = (int32_t)nbw;
+    out->max_row_nnz = h.max_row_nnz;
+    return PWMGPU_OK;
+}
+
 int pwmgpu_dims(const pwmgpu_matrix* m, int32_t* nor, int32_t* noc, int64_t* nnz) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
     if (nor) *nor = m->M.nor;

@@ -180,6 +180,14 @@ class CudaSparseMatrix:
         check(_lib.lib().pwmgpu_dims(self._h, C.byref(nor), C.byref(noc), C.byref(nnz)), "pwmgpu_dims")
         return nor.value, noc.value, nnz.value
 
+    def stats(self):
+        """Util_Scripts/calc_stats.cpp figures of the loaded matrix, computed on
+        the device: dict with size, nnz, rows_avg, rows_var, block_avg,
+        block_var, balanced, block_bits, nb_blocks, max_row_nnz."""
+        st = _lib.MatrixStats()
+        check(_lib.lib().pwmgpu_stats(self._h, C.byref(st)), "pwmgpu_stats")
+        return {name: getattr(st, name) for name, _ in st._fields_}
+
     def getCSR(self):
         """The device CRS arrays (row_start, col_ind, data) copied to the host."""
         nor, noc, nnz = self.dims()
