@@ -570,13 +570,18 @@ int plan_pipeline(pwmgpu_matrix* m) {
     for (int c = 1; c < K; ++c)
         if (p.rec[4 * c + 1] <= p.rec[4 * (c - 1) + 1]) return PWMGPU_OK;
     for (int c = 1; c < K; ++c) p.rec[4 * c + 3] = std::max(p.rec[4 * c + 3], p.rec[4 * (c - 1) + 3]);
-    CU(cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking));
-    CU(cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking));
-    CU(cudaEventCreateWithFlags(&p.ev_start, cudaEventDisableTiming));
-    p.ev_x.assign(kPipeX, nullptr);
-    p.ev_y.assign(K, nullptr);
-    for (auto& ev : p.ev_x) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    for (auto& ev : p.ev_y) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    // streams and events outlive a reload of the matrix: create them once
+    if (!p.in) CU(cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking));
+    if (!p.out) CU(cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking));
+    if (!p.ev_start) CU(cudaEventCreateWithFlags(&p.ev_start, cudaEventDisableTiming));
+    for (auto* v : {&p.ev_x, &p.ev_y}) {
+        const size_t want = v == &p.ev_x ? (size_t)kPipeX : (size_t)K;
+        while (v->size() < want) {
+            cudaEvent_t ev = nullptr;
+            CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            v->push_back(ev);
+        }
+    }
     p.K = K;
     return PWMGPU_OK;
 }
