@@ -600,6 +600,15 @@ def run_ours(args, world, rank, local):
         for _ in range(e2e_steps):
             M.mv(xn, yn_)  # H2D x, SpMV, D2H y, synchronous
         e2e_s = (time.perf_counter() - t0) / e2e_steps
+        # the same call on pageable arrays (what the reference's drivers pass:
+        # new[] buffers)
+        xq = x_host.numpy().copy()
+        yq = np.zeros(N)
+        M.mv(xq, yq)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            M.mv(xq, yq)
+        e2e_pageable_s = (time.perf_counter() - t0) / e2e_steps
     e2e_gbs = B * world / e2e_s / 1e9 if e2e_steps else None
 
     extra = None if args.no_extra else irregular_and_solves(pwm, torch, dev, stream, args)
@@ -621,7 +630,9 @@ def run_ours(args, world, rank, local):
                      "algorithmic_bytes_per_launch": B, "timed": "k_merge_spmv + k_merge_fixup (one SpMV)"},
         "e2e": ({"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 8 * N,
                  "d2h_bytes_per_step": 8 * N, "ms_per_step": round(e2e_s * 1e3, 4),
-                 "api": "pwmgpu_mv (host arrays, pinned)"} if e2e_steps else None),
+                 "api": "pwmgpu_mv (host arrays, pinned)",
+                 "pageable": {"ms_per_step": round(e2e_pageable_s * 1e3, 4),
+                              "gb_s": round(B * world / e2e_pageable_s / 1e9, 3)}} if e2e_steps else None),
         "gpu_launches": 2 * args.steps,
         "power": {"iterations": p_it,
                   "fused": {"ms_per_iteration": round(power_ms["fused"] / p_it, 5),

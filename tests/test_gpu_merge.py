@@ -276,6 +276,37 @@ def test_launch_tuner_variants_same_bits(pwm, kind):
     assert np.all(np.abs(ys[0] - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
 
 
+@pytest.mark.parametrize("offset", [0, 1])
+def test_pipelined_host_mv_pageable_and_pinned(pwm, offset):
+    """Host arrays that are pinned go through the copy engines; pageable ones
+    (where the GPU reaches pageable memory) through SM copy kernels -- both at
+    any 8-byte offset, with the same bits as the device-resident path."""
+    torch = pytest.importorskip("torch")
+    M = pwm.CRSCuda(1)
+    M.generatePoissonMatrix(701, 899, 1)
+    n = M.dims()[0]
+    x = np.random.default_rng(8).uniform(-1, 1, n)
+    dx = torch.tensor(x, device="cuda")
+    dy = torch.zeros(n, dtype=torch.float64, device="cuda")
+    M.mv_device(dx.data_ptr(), dy.data_ptr())
+    torch.cuda.synchronize()
+    want = dy.cpu().numpy()
+    # pageable, shifted by `offset` doubles (8-byte phase of a 16-byte boundary)
+    xb = np.empty(n + 1)
+    yb = np.full(n + 1, np.nan)
+    xa, ya = xb[offset:offset + n], yb[1 - offset:1 - offset + n]
+    xa[:] = x
+    for _ in range(2):
+        ya[:] = np.nan
+        M.mv(xa, ya)
+        assert np.array_equal(ya, want)
+    # pinned
+    xp = torch.tensor(x).pin_memory()
+    yp = torch.full((n,), float("nan"), dtype=torch.float64).pin_memory()
+    M.mv(xp.numpy(), yp.numpy())
+    assert np.array_equal(yp.numpy(), want)
+
+
 @pytest.mark.parametrize("kind", ["poisson", "random", "long_rows"])
 def test_pipelined_host_mv_same_bits(pwm, kind):
     """pwmgpu_mv on host arrays runs pipelined (x up in pieces, the SpMV in

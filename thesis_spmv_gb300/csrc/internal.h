@@ -142,6 +142,10 @@ cudaError_t launch_matrix_stats(const int32_t* row_start, const int32_t* col, in
                                 unsigned int* blocks, long long* brow, double* row_partials, double* blk_partials,
                                 StatsDev* out, cudaStream_t st);
 
+// hostcopy.cu: SM-driven copy between pageable host memory and the device
+// (only where the device reaches pageable memory)
+cudaError_t launch_host_copy(const double* src, double* dst, long long n, cudaStream_t st);
+
 // batch.cu: one round (`steps` power steps + the residual pass) of every slot
 // of a class table; seeded uniform start vectors
 struct BatchTable;

@@ -59,6 +59,7 @@ struct pwmgpu_matrix {
     int partitions = 1;
     int device = 0;
     int sm_count = 1;
+    int pageable_access = -1;  // the device reads / writes pageable host memory (-1: not asked yet)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool loaded = false;

@@ -571,8 +571,11 @@ int plan_pipeline(pwmgpu_matrix* m) {
         if (p.rec[4 * c + 1] <= p.rec[4 * (c - 1) + 1]) return PWMGPU_OK;
     for (int c = 1; c < K; ++c) p.rec[4 * c + 3] = std::max(p.rec[4 * c + 3], p.rec[4 * (c - 1) + 3]);
     // streams and events outlive a reload of the matrix: create them once
-    if (!p.in) CU(cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking));
-    if (!p.out) CU(cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking));
+    // highest priority: their copy kernels (pageable arrays) go ahead of SpMV CTAs
+    int lo_prio = 0, hi_prio = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    if (!p.in) CU(cudaStreamCreateWithPriority(&p.in, cudaStreamNonBlocking, hi_prio));
+    if (!p.out) CU(cudaStreamCreateWithPriority(&p.out, cudaStreamNonBlocking, hi_prio));
     if (!p.ev_start) CU(cudaEventCreateWithFlags(&p.ev_start, cudaEventDisableTiming));
     for (auto* v : {&p.ev_x, &p.ev_y}) {
         const size_t want = v == &p.ev_x ? (size_t)kPipeX : (size_t)K;
@@ -586,16 +589,38 @@ int plan_pipeline(pwmgpu_matrix* m) {
     return PWMGPU_OK;
 }
 
+// A caller array the copy engines would have to stage (pageable memory) but
+// the SMs can reach directly: copied by launch_host_copy instead.
+bool sm_reachable_pageable(pwmgpu_matrix* m, const void* h) {
+    if (m->pageable_access < 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
+            v = 0;
+        m->pageable_access = v ? 1 : 0;
+    }
+    if (!m->pageable_access) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
 int mv_pipelined(pwmgpu_matrix* m, const double* x, double* y) {
     auto& p = m->pipe;
     const int K = p.K, noc = m->M.noc, nor = m->M.nor, nsub = m->num_tiles;
+    const bool x_sm = sm_reachable_pageable(m, x), y_sm = sm_reachable_pageable(m, y);
     // the streams start after earlier work on the handle's stream
     CU(cudaEventRecord(p.ev_start, m->stream));
     CU(cudaStreamWaitEvent(p.in, p.ev_start, 0));
     CU(cudaStreamWaitEvent(p.out, p.ev_start, 0));
     for (int q = 0; q < kPipeX; ++q) {
         const long long a = (long long)noc * q / kPipeX, b = (long long)noc * (q + 1) / kPipeX;
-        if (b > a)
+        if (b > a && x_sm)
+            CU(launch_host_copy(x + a, m->dx + a, b - a, p.in));
+        else if (b > a)
             CU(cudaMemcpyAsync(m->dx + a, x + a, sizeof(double) * (size_t)(b - a), cudaMemcpyHostToDevice, p.in));
         CU(cudaEventRecord(p.ev_x[(size_t)q], p.in));
     }
@@ -630,7 +655,9 @@ int mv_pipelined(pwmgpu_matrix* m, const double* x, double* y) {
             CU(cudaEventRecord(p.ev_y[(size_t)c - 1], m->stream));
             CU(cudaStreamWaitEvent(p.out, p.ev_y[(size_t)c - 1], 0));
             const int r0 = row_lo(c - 1), r1 = row_lo(c);
-            if (r1 > r0)
+            if (r1 > r0 && y_sm)
+                CU(launch_host_copy(m->dy + r0, y + r0, r1 - r0, p.out));
+            else if (r1 > r0)
                 CU(cudaMemcpyAsync(y + r0, m->dy + r0, sizeof(double) * (size_t)(r1 - r0), cudaMemcpyDeviceToHost,
                                    p.out));
         }
