@@ -333,3 +333,40 @@ def test_pipelined_host_mv_same_bits(pwm, kind):
     rs, ci, d = M.getCSR()
     A = O.CRSArrays(n, n, rs, ci, d)
     assert np.all(np.abs(y - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
+
+
+def test_sixteen_bit_columns_where_spans_fit(pwm):
+    """Stencil / banded matrices stream 16-bit column offsets (2 bytes per
+    nonzero less); a matrix with columns spread over 4M does not; both give
+    the oracle's SpMV, and the merge, CSB and CO-H formats agree on Poisson."""
+    M = pwm.CRSCuda(1)
+    M.generatePoissonMatrix(1500, 1300, 1)
+    assert M.column_bytes() == 2
+    n = M.dims()[0]
+    x = np.random.default_rng(3).uniform(-1, 1, n)
+    y = np.zeros(n)
+    M.mv(x, y)
+    rs, ci, d = M.getCSR()
+    A = O.CRSArrays(n, n, rs, ci, d)
+    assert np.all(np.abs(y - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
+    xs, ys = x.copy(), np.zeros(n)
+    M.powerIteration(xs, ys, 5)
+    xr, yr = O.power(A, x.copy(), 5)
+    assert np.allclose(ys, yr, rtol=1e-12, atol=1e-14)
+    R = pwm.CRSCuda(1)
+    R.generateRandom(300_000, 4, mean_len=10.0)
+    assert R.column_bytes() == 4
+    # a span of exactly 65535 fits, 65536 does not
+    for span, want in ((65535, 2), (65536, 4)):
+        nn = 70_000
+        rows = np.arange(nn, dtype=np.int32)  # the identity plus (0, span)
+        B = pwm.CRSCuda(1)
+        B.loadFromTriplets(pwm.Triplet(nn, nn, np.concatenate([rows, [0]]).astype(np.int32),
+                                       np.concatenate([rows, [span]]).astype(np.int32), np.ones(nn + 1)), 1)
+        assert B.column_bytes() == want
+        xb = np.random.default_rng(5).random(nn)
+        yb = np.zeros(nn)
+        B.mv(xb, yb)
+        want_y = xb.copy()
+        want_y[0] += xb[span]
+        assert np.allclose(yb, want_y, rtol=1e-15, atol=0)

@@ -72,7 +72,7 @@ template <typename VT, int IPT>
 __device__ __forceinline__ void issue_global(unsigned char* st, uint64_t* bar, const BatchSlot* slots, int j, int g,
                                              int4 r1, uint64_t pol) {
     const BatchSlot* d = slots + j;
-    issue_subtile<VT, IPT>(st, bar, g - d->tile0, r1, d->rec, d->masks, d->colp, static_cast<const VT*>(d->valp),
+    issue_subtile<VT, IPT>(st, bar, g - d->tile0, r1, d->rec, d->masks, d->colp, nullptr, static_cast<const VT*>(d->valp),
                            pol);
 }
 

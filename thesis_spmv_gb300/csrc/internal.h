@@ -46,11 +46,13 @@ struct MliPlan {
     uint16_t* masks = nullptr;  // nsub x 32 row-end masks
     int32_t* colp = nullptr;    // lane-interleaved column indices
     double* valp = nullptr;     // lane-interleaved FP64 values
+    uint16_t* colp16 = nullptr; // or null: the same columns as offsets from the sub-tile's base (rec0.w)
 };
 long long mli_storage_elems(long long nnz, long long nsub);
 
-// l1: launch variant of the merge kernels (0: most resident CTAs; 1: a
-// smaller shared-memory carveout, more L1 for irregular gathers).
+// l1: launch variant of the merge kernels.  Bit 0: 0 = most resident CTAs,
+// 1 = a smaller shared-memory carveout, more L1 for irregular gathers; bit 1:
+// stream the plan's 16-bit column offsets (set only when the plan has them).
 MergeGeom merge_geometry(int cfg, int l1 = 0);
 int merge_grid(int cfg, int nsub, int sm_count, int l1 = 0);
 int fixup_grid(int num_tiles, int sm_count);
@@ -71,6 +73,8 @@ cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long 
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
                             int sm_count, cudaStream_t st);
 cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st);
+cudaError_t launch_mli_colspan(const MliPlan& P, int* cbase, int* flag, int sm_count, cudaStream_t st);
+cudaError_t launch_mli_col16(const MliPlan& P, const int* cbase, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,

@@ -150,6 +150,7 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(P.rec);
         pwmgpu::dfree(P.masks);
         pwmgpu::dfree(P.colp);
+        pwmgpu::dfree(P.colp16);
         pwmgpu::dfree(P.valp);
         P = MliPlan();
         pwmgpu::dfree(val32);

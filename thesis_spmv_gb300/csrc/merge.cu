@@ -96,6 +96,51 @@ __global__ void k_mli_convert(const double* __restrict__ valp, const int2* __res
     }
 }
 
+// 16-bit columns.  Sub-tile s holds elements [base, base + nkw) of the
+// lane-interleaved storage; when every sub-tile's columns span less than 2^16
+// (banded and stencil matrices: the rows of a sub-tile are consecutive), the
+// plan also keeps col - cbase(s) as uint16 with cbase(s) = the sub-tile's
+// smallest column in rec0.w (rec0.w otherwise holds kw1, which no kernel
+// reads).  Pass 1: cbase per sub-tile, flag[0] = 1 if some span is too wide.
+__global__ void k_mli_colspan(const int32_t* __restrict__ colp, const int4* __restrict__ rec, int nsub,
+                              int* __restrict__ cbase, int* __restrict__ flag) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
+        const int4 r1 = rec[2LL * s + 1];
+        const long long base = r1.z;
+        const int nkw = r1.w;
+        int lo = INT_MAX, hi = INT_MIN;
+        for (int k = lane; k < nkw; k += 32) {
+            const int c = colp[base + k];
+            lo = min(lo, c);
+            hi = max(hi, c);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            cbase[s] = nkw > 0 ? lo : 0;
+            if (nkw > 0 && (long long)hi - (long long)lo > 65535) atomicOr(flag, 1);
+        }
+    }
+}
+
+// Pass 2: the uint16 offsets and rec0.w = cbase.
+__global__ void k_mli_col16(const int32_t* __restrict__ colp, int4* __restrict__ rec, int nsub,
+                            const int* __restrict__ cbase, uint16_t* __restrict__ colp16) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < nsub; s += gridDim.x * wpb) {
+        const int4 r1 = rec[2LL * s + 1];
+        const long long base = r1.z;
+        const int nkw = r1.w, cb = cbase[s];
+        for (int k = lane; k < nkw; k += 32) colp16[base + k] = (uint16_t)(colp[base + k] - cb);
+        if (lane == 0) rec[2LL * s].w = cb;
+    }
+}
+
 // Back to CRS order (for reading the matrix out).
 __global__ void k_mli_unpermute(const int32_t* __restrict__ colp, const double* __restrict__ valp,
                                 const int2* __restrict__ subc, const int4* __restrict__ rec, int nsub,
@@ -134,6 +179,7 @@ struct MergeArgs {
     const double* nsq_in;  // MODE_POWER: ||x||^2 (source of the 2^e rescale), or null for e = 0
     int* status;
     int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
+    const uint16_t* colp16 = nullptr;  // C16 kernels: 16-bit column offsets (base in rec0.w)
 };
 
 constexpr int kMliStages = 2;
@@ -143,11 +189,11 @@ constexpr int kMliStages = 2;
 // warp's stage uses so far, so mbarrier phases carry across passes of a
 // persistent kernel.  Returns false (warp-uniformly) after a timeout, once
 // this warp's copies in flight have landed or a short bound ran out.
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH>
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH, bool C16>
 __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
                                           XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
                                           AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol) {
-    using S = WarpStage<VT, IPT>;
+    using S = WarpStage<VT, IPT, C16>;
     constexpr int NS = kMliStages;
     constexpr int W = NT / 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -158,8 +204,8 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         for (int k = 0; k < NS && k < n; ++k) {
             const uint32_t u = ticket + k;
             const int s = a.tile0 + gw + k * tw;
-            issue_subtile<VT, IPT>(stages + (u % NS) * S::BYTES, &bars[u % NS], s, __ldg(a.rec + 2LL * s + 1),
-                                   a.rec, a.masks, a.colp, a.valp, pol);
+            issue_subtile<VT, IPT, C16>(stages + (u % NS) * S::BYTES, &bars[u % NS], s, __ldg(a.rec + 2LL * s + 1),
+                                        a.rec, a.masks, a.colp, a.colp16, a.valp, pol);
         }
         if (n > NS) pref = __ldg(a.rec + 2LL * (a.tile0 + gw + NS * tw) + 1);
     }
@@ -173,18 +219,19 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         const bool ok = mbar_wait_bounded(&bars[k], (u / NS) & 1u, a.status);
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
         AT xv[IPT];
-        gather_subtile<VT, XT, AT, IPT, XCOH>(st, x, xv);
+        gather_subtile<VT, XT, AT, IPT, XCOH, C16>(st, x, xv);
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
-            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow, cval,
-                                                        hval);
+            finish_subtile<MODE, true, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
+                                                             cval, hval);
         else
-            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow, cval,
-                                                         hval);
+            finish_subtile<MODE, false, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
+                                                              cval, hval);
         // every lane is done with this stage (finish_subtile ends with a warp
         // barrier): refill it with the warp's sub-tile i + NS
         if (lane == 0 && i + NS < n) {
             fence_proxy_async();
-            issue_subtile<VT, IPT>(st, &bars[k], s + NS * tw, pref, a.rec, a.masks, a.colp, a.valp, pol);
+            issue_subtile<VT, IPT, C16>(st, &bars[k], s + NS * tw, pref, a.rec, a.masks, a.colp, a.colp16, a.valp,
+                                        pol);
             pref = (i + NS + 1 < n) ? __ldg(a.rec + 2LL * (s + (NS + 1) * tw) + 1) : make_int4(0, 0, 0, 0);
         }
     }
@@ -206,9 +253,10 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
 // L1: launch variant (0: shared-memory-heavy carveout, most resident CTAs;
 // 1: a smaller carveout that leaves more L1 for the x gathers); the code is
 // the same, the two instances carry different function attributes.
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0>
+// C16: the plan's 16-bit column offsets are streamed instead of 32-bit columns.
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0, bool C16 = false>
 __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
-    using S = WarpStage<VT, IPT>;
+    using S = WarpStage<VT, IPT, C16>;
     constexpr int W = NT / 32;
     constexpr int NS = kMliStages;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -225,8 +273,8 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     __syncwarp();
     uint32_t ticket = 0;
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
-    warp_pass<MODE, VT, XT, AT, NT, IPT, false>(a, a.x, a.y, stages, bars[w], crow + 32 * w, cval + 32 * w,
-                                                hval + 32 * w, ticket, e, policy_evict_first());
+    warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16>(a, a.x, a.y, stages, bars[w], crow + 32 * w, cval + 32 * w,
+                                                     hval + 32 * w, ticket, e, policy_evict_first());
 }
 
 template <typename XT, typename AT>
@@ -404,9 +452,9 @@ __device__ __forceinline__ void grid_total2(const double* partials, double* tota
     __syncthreads();
 }
 
-template <typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0>
+template <typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0, bool C16 = false>
 __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p) {
-    using S = WarpStage<VT, IPT>;
+    using S = WarpStage<VT, IPT, C16>;
     constexpr int W = NT / 32;
     constexpr int NS = kMliStages;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -436,8 +484,8 @@ __global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p
         e = k > 0 ? pow2_rescale_exponent(nsq_cur, rescale_window<XT>()) : 0;
         nsq_last = nsq_cur;
         const bool want_dot = p.result && k == p.k0 + p.nk - 1;
-        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true>(a, in, out, stages, bars[w], crow + 32 * w, cval + 32 * w,
-                                                         hval + 32 * w, ticket, e, pol);
+        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
+                                                              cval + 32 * w, hval + 32 * w, ticket, e, pol);
         if (!grid_sync(p.barrier, a.status)) return;
         fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub, nthr);
         if (!grid_sync(p.barrier, a.status)) return;
@@ -639,77 +687,110 @@ long long mli_storage_elems(long long nnz, long long nsub) { return mli_size(nnz
 // variant: room for 4 CTAs' stages, the rest of the 256 KB as L1.
 constexpr int kL1Carveout = 72;
 
+// Launch variant v of the merge kernels: bit 0 = L1 (the smaller shared-memory
+// carveout), bit 1 = C16 (16-bit column offsets; only for plans that have them).
 template <typename VT, typename XT, typename AT, int NT, int IPT>
 struct MergeKernels {
-    static constexpr int SMEM = (NT / 32) * kMliStages * WarpStage<VT, IPT>::BYTES;
+    static constexpr int smem(bool c16) {
+        return (NT / 32) * kMliStages * (c16 ? WarpStage<VT, IPT, true>::BYTES : WarpStage<VT, IPT, false>::BYTES);
+    }
 
     template <typename K>
-    static int setup(K k, int l1) {
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    static int setup(K k, int l1, int bytes) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (l1) cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, kL1Carveout);
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, SMEM) != cudaSuccess) o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, bytes) != cudaSuccess) o = 0;
         return o;
     }
 
-    static MergeGeom geom(int l1 = 0) {
-        static int occ[2] = {-1, -1};
-        if (occ[l1] < 0) {
+    template <int L1, bool C16>
+    static int setup_spmv() {
+        setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
+        return setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
+    }
+
+    static MergeGeom geom(int v = 0) {
+        v &= 3;
+        static int occ[4] = {-1, -1, -1, -1};
+        if (occ[v] < 0) {
             int o;
-            if (l1) {
-                setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 1>, 1);
-                o = setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 1>, 1);
-            } else {
-                setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 0>, 0);
-                o = setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 0>, 0);
+            switch (v) {
+                case 1: o = setup_spmv<1, false>(); break;
+                case 2: o = setup_spmv<0, true>(); break;
+                case 3: o = setup_spmv<1, true>(); break;
+                default: o = setup_spmv<0, false>(); break;
             }
-            occ[l1] = o > 0 ? o : 1;
+            occ[v] = o > 0 ? o : 1;
         }
-        return MergeGeom{32 * IPT, NT / 32, SMEM, occ[l1], NT};
+        return MergeGeom{32 * IPT, NT / 32, smem(v & 2), occ[v], NT};
+    }
+
+    template <int L1, bool C16>
+    static const void* power_kernel() {
+        return (const void*)k_power_persistent<VT, XT, AT, NT, IPT, L1, C16>;
+    }
+    static const void* power_kernel(int v) {
+        switch (v & 3) {
+            case 1: return power_kernel<1, false>();
+            case 2: return power_kernel<0, true>();
+            case 3: return power_kernel<1, true>();
+            default: return power_kernel<0, false>();
+        }
     }
 
     // resident CTAs per SM of the persistent power kernel (0: cannot launch)
-    static int power_occ(int l1 = 0) {
-        static int occ[2] = {-1, -1};
-        if (occ[l1] < 0)
-            occ[l1] = l1 ? setup(k_power_persistent<VT, XT, AT, NT, IPT, 1>, 1)
-                         : setup(k_power_persistent<VT, XT, AT, NT, IPT, 0>, 0);
-        return occ[l1];
+    static int power_occ(int v = 0) {
+        v &= 3;
+        static int occ[4] = {-1, -1, -1, -1};
+        if (occ[v] < 0) {
+            const void* k = power_kernel(v);
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem(v & 2));
+            if (v & 1) cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, kL1Carveout);
+            int o = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, NT, smem(v & 2)) != cudaSuccess) o = 0;
+            occ[v] = o;
+        }
+        return occ[v];
     }
 
     static cudaError_t power(const DevMatrix& M, const void* valp, const MliPlan& P, int grid, void* X, void* Y,
                              void* carries, int k0, int nk, double* nsq, double* result, double* partials,
-                             unsigned int* barrier, int* status, cudaStream_t st, int l1) {
-        power_occ(l1);
+                             unsigned int* barrier, int* status, cudaStream_t st, int v) {
+        if (!P.colp16) v &= 1;
+        power_occ(v);
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
-                                 nullptr, (AT*)carries, nullptr, status},
+                                 nullptr, (AT*)carries, nullptr, status, 0, P.colp16},
                                 P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier};
         cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned int), st);
         if (e != cudaSuccess) return e;
         void* args[] = {&p};
         // cooperative launch: fails instead of running if the grid cannot be
         // co-resident, so the grid barriers cannot wait on unscheduled CTAs
-        const void* k = l1 ? (const void*)k_power_persistent<VT, XT, AT, NT, IPT, 1>
-                           : (const void*)k_power_persistent<VT, XT, AT, NT, IPT, 0>;
-        return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(NT), args, SMEM, st);
+        return cudaLaunchCooperativeKernel(power_kernel(v), dim3(grid), dim3(NT), args, smem(v & 2), st);
+    }
+
+    template <int L1, bool C16>
+    static void launch_spmv(int mode, const MergeArgs<VT, XT, AT>& a, int grid, cudaStream_t st) {
+        if (mode == MODE_POWER)
+            k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16><<<grid, NT, smem(C16), st>>>(a);
+        else
+            k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16><<<grid, NT, smem(C16), st>>>(a);
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                            cudaStream_t st, int l1) {
-        geom(l1);
-        MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub,
-                                (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status};
-        if (l1) {
-            if (mode == MODE_POWER)
-                k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 1><<<grid, NT, SMEM, st>>>(a);
-            else
-                k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 1><<<grid, NT, SMEM, st>>>(a);
-        } else {
-            if (mode == MODE_POWER)
-                k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, 0><<<grid, NT, SMEM, st>>>(a);
-            else
-                k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, 0><<<grid, NT, SMEM, st>>>(a);
+                            cudaStream_t st, int v, int tile0 = 0, int nsub = -1) {
+        if (!P.colp16) v &= 1;
+        geom(v);
+        MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
+                                nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
+                                tile0, P.colp16};
+        switch (v & 3) {
+            case 1: launch_spmv<1, false>(mode, a, grid, st); break;
+            case 2: launch_spmv<0, true>(mode, a, grid, st); break;
+            case 3: launch_spmv<1, true>(mode, a, grid, st); break;
+            default: launch_spmv<0, false>(mode, a, grid, st); break;
         }
         return cudaGetLastError();
     }
@@ -790,6 +871,18 @@ cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const 
     if (P.nsub == 0) return cudaSuccess;
     k_mli_plan<<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(row_start, col, val, P.subc, P.nsub, P.colp, P.valp,
                                                              P.masks, P.rec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mli_colspan(const MliPlan& P, int* cbase, int* flag, int sm_count, cudaStream_t st) {
+    if (P.nsub == 0) return cudaSuccess;
+    k_mli_colspan<<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(P.colp, P.rec, P.nsub, cbase, flag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mli_col16(const MliPlan& P, const int* cbase, int sm_count, cudaStream_t st) {
+    if (P.nsub == 0 || !P.colp16) return cudaSuccess;
+    k_mli_col16<<<warp_grid(P.nsub, sm_count), 256, 0, st>>>(P.colp, P.rec, P.nsub, cbase, P.colp16);
     return cudaGetLastError();
 }
 
@@ -891,12 +984,7 @@ cudaError_t launch_pipeline_plan(const int32_t* row_start, const MliPlan& P, int
 cudaError_t launch_merge_spmv_range(const DevMatrix& M, const MliPlan& P, int t0, int t1, int grid, const double* x,
                                     double* y, double* carries, int* status, cudaStream_t st, int l1) {
     if (t1 <= t0) return cudaSuccess;
-    CfgF64::geom(l1);
-    MergeArgs<double, double, double> a{M.row_start, P.colp, P.valp, P.rec, P.masks, M.nor, t1 - t0,
-                                        x, y, carries, nullptr, status, t0};
-    if (l1) k_merge_spmv<MODE_SPMV, double, double, double, 128, kMliIpt, 1><<<grid, 128, CfgF64::SMEM, st>>>(a);
-    else k_merge_spmv<MODE_SPMV, double, double, double, 128, kMliIpt, 0><<<grid, 128, CfgF64::SMEM, st>>>(a);
-    return cudaGetLastError();
+    return CfgF64::spmv(MODE_SPMV, M, P.valp, P, grid, x, y, carries, nullptr, status, st, l1, t0, t1 - t0);
 }
 
 cudaError_t launch_merge_fixup_range(const DevMatrix& M, const int2* tiles, int num_tiles, int f0, int f1, double* y,

@@ -176,13 +176,14 @@ __device__ __forceinline__ void load_lane(const T* p, int qm, int cnt, int lane,
 enum MergeMode { MODE_SPMV = 0, MODE_POWER = 1 };
 
 // One warp's shared-memory stage: the staged sub-tile's record, row-end
-// masks, lane-interleaved columns and values.
-template <typename VT, int IPT>
+// masks, lane-interleaved columns and values.  C16: the columns are stored as
+// 16-bit offsets from a per-sub-tile base (rec0.w).
+template <typename VT, int IPT, bool C16 = false>
 struct WarpStage {
     static constexpr int WM = 32 * IPT;
     static constexpr int REC_B = 32;                // int4 rec0, rec1
     static constexpr int MASK_B = 64;               // 32 x uint16
-    static constexpr int COL_B = WM * 4;            // multiple of 16
+    static constexpr int COL_B = WM * (C16 ? 2 : 4);  // multiple of 16
     static constexpr int VAL_B = WM * (int)sizeof(VT);
     static constexpr int BYTES = REC_B + MASK_B + COL_B + VAL_B;
     static_assert(BYTES % 16 == 0, "stage must keep 16-byte alignment");
@@ -192,19 +193,22 @@ struct WarpStage {
 // sub-tile ({fr, flags, base, nkw}), loaded one iteration earlier so the
 // issue does not wait on it.  Sizes are rounded up to 16 bytes; the arrays
 // carry slack past the last sub-tile, so the rounded copies stay inside.
-template <typename VT, int IPT>
+template <typename VT, int IPT, bool C16 = false>
 __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, int s, int4 r1,
                                               const int4* __restrict__ rec, const uint16_t* __restrict__ masks,
-                                              const int32_t* __restrict__ colp, const VT* __restrict__ valp,
-                                              uint64_t pol) {
-    using S = WarpStage<VT, IPT>;
+                                              const int32_t* __restrict__ colp, const uint16_t* __restrict__ colp16,
+                                              const VT* __restrict__ valp, uint64_t pol) {
+    using S = WarpStage<VT, IPT, C16>;
     const int base = r1.z, nkw = r1.w;
-    const uint32_t cb = (uint32_t)((nkw * 4 + 15) & ~15);
+    const uint32_t cb = (uint32_t)((nkw * (C16 ? 2 : 4) + 15) & ~15);
     const uint32_t vb = (uint32_t)((nkw * (int)sizeof(VT) + 15) & ~15);
     mbar_arrive_expect_tx(bar, S::REC_B + S::MASK_B + cb + vb);
     bulk_g2s(st, rec + 2LL * s, S::REC_B, bar, pol);
     bulk_g2s(st + S::REC_B, masks + 32LL * s, S::MASK_B, bar, pol);
-    if (cb) bulk_g2s(st + S::REC_B + S::MASK_B, colp + base, cb, bar, pol);
+    if (cb) {
+        if (C16) bulk_g2s(st + S::REC_B + S::MASK_B, colp16 + base, cb, bar, pol);
+        else bulk_g2s(st + S::REC_B + S::MASK_B, colp + base, cb, bar, pol);
+    }
     if (vb) bulk_g2s(st + S::REC_B + S::MASK_B + S::COL_B, valp + base, vb, bar, pol);
 }
 
@@ -214,15 +218,23 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 // it is read with ordinary coherent loads (ld.global.ca: L1-cached, and
 // ordered after the grid barrier's acquire) instead of the read-only
 // non-coherent path.
-template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false>
+template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false, bool C16 = false>
 __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT]) {
-    using S = WarpStage<VT, IPT>;
+    using S = WarpStage<VT, IPT, C16>;
     const int lane = threadIdx.x & 31;
     const int nkw = reinterpret_cast<const int4*>(st)[1].w;
     const int qm = nkw >> 5, rem = nkw & 31;
     const int cnt = qm + (lane < rem ? 1 : 0);
     int32_t cv[IPT];
-    load_lane<int32_t, IPT>(reinterpret_cast<const int32_t*>(st + S::REC_B + S::MASK_B), qm, cnt, lane, cv);
+    if (C16) {
+        uint16_t c16[IPT];
+        load_lane<uint16_t, IPT>(reinterpret_cast<const uint16_t*>(st + S::REC_B + S::MASK_B), qm, cnt, lane, c16);
+        const int cbase = reinterpret_cast<const int4*>(st)[0].w;
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) cv[j] = cbase + (int)c16[j];
+    } else {
+        load_lane<int32_t, IPT>(reinterpret_cast<const int32_t*>(st + S::REC_B + S::MASK_B), qm, cnt, lane, cv);
+    }
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
         if (XCOH) xv[j] = (j < cnt) ? (AT)__ldca(x + cv[j]) : AT(0);
@@ -236,12 +248,12 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 //   e         MODE_POWER: rows are stored times 2^e (exact rescale of the
 //             power method's iterate; a warp-uniform skip when e == 0)
 //   crow, cval, hval   this warp's 32-entry shared scratch
-template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT>
+template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT, bool C16 = false>
 __device__ __forceinline__ void finish_subtile(int s, const unsigned char* st, const AT (&xv)[IPT],
                                                const int32_t* __restrict__ row_start, XT* __restrict__ y,
                                                AT* __restrict__ carries, int nor, int e, int* crow, AT* cval,
                                                AT* hval) {
-    using S = WarpStage<VT, IPT>;
+    using S = WarpStage<VT, IPT, C16>;
     const int lane = threadIdx.x & 31;
     const int4 r0 = reinterpret_cast<const int4*>(st)[0];
     const int4 r1 = reinterpret_cast<const int4*>(st)[1];

@@ -157,14 +157,15 @@ int tune(pwmgpu_matrix* m) {
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     int rc = PWMGPU_OK;
+    const int c16 = m->P.colp16 ? 2 : 0;
     for (int v = 0; v < 2 && rc == PWMGPU_OK; ++v) {
-        const int grid = merge_grid(kCfgF64, m->num_tiles, m->sm_count, v);
+        const int grid = merge_grid(kCfgF64, m->num_tiles, m->sm_count, v | c16);
         cudaError_t e = cudaSuccess;
         for (int r = 0; r < 5 && e == cudaSuccess; ++r) {  // one warm-up, four timed
             if (r == 1) e = cudaEventRecord(e0, m->stream);
             if (e == cudaSuccess)
                 e = launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, grid, m->dx, m->dy, m->carries,
-                                      nullptr, m->status, m->stream, v);
+                                      nullptr, m->status, m->stream, v | c16);
         }
         if (e == cudaSuccess) e = cudaEventRecord(e1, m->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -176,12 +177,49 @@ int tune(pwmgpu_matrix* m) {
     cudaEventDestroy(e1);
     TRY(rc);
     TRY(check_status(m));
-    const int v = m->tune_ms[1] < 0.97f * m->tune_ms[0] ? 1 : 0;
+    const int v = (m->tune_ms[1] < 0.97f * m->tune_ms[0] ? 1 : 0) | c16;
     m->l1 = v;
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, v);
     m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, v);
     m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, v);
     m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, v);
+    return PWMGPU_OK;
+}
+
+// 16-bit columns for the merge kernels when every sub-tile's columns span
+// less than 2^16 (then the SpMV streams 10 bytes per FP64 nonzero instead of
+// 12).  Skipped, not an error, when the span is wider or the extra array does
+// not fit.
+int build_col16(pwmgpu_matrix* m) {
+    MliPlan& P = m->P;
+    if (P.nsub == 0 || m->M.nnz == 0) return PWMGPU_OK;
+    int* cbase = nullptr;
+    int* flag = nullptr;
+    TRY(dalloc(&cbase, (size_t)P.nsub));
+    int rc = dalloc(&flag, 1);
+    int wide = 1;
+    cudaError_t e = cudaSuccess;
+    if (rc == PWMGPU_OK) {
+        e = cudaMemsetAsync(flag, 0, sizeof(int), m->stream);
+        if (e == cudaSuccess) e = launch_mli_colspan(P, cbase, flag, m->sm_count, m->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&wide, flag, sizeof(int), cudaMemcpyDeviceToHost, m->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    }
+    if (rc == PWMGPU_OK && e == cudaSuccess && !wide) {
+        const size_t elems = (size_t)mli_storage_elems(m->M.nnz, P.nsub);
+        if (cudaMalloc((void**)&P.colp16, elems * sizeof(uint16_t)) != cudaSuccess) {
+            (void)cudaGetLastError();
+            P.colp16 = nullptr;
+        } else {
+            e = cudaMemsetAsync(P.colp16, 0, elems * sizeof(uint16_t), m->stream);
+            if (e == cudaSuccess) e = launch_mli_col16(P, cbase, m->sm_count, m->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+        }
+    }
+    dfree(cbase);
+    dfree(flag);
+    if (rc != PWMGPU_OK) return rc;
+    if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "16-bit column plan: %s", cudaGetErrorString(e));
     return PWMGPU_OK;
 }
 
@@ -207,14 +245,15 @@ int build_plan(pwmgpu_matrix* m) {
         CU(launch_mli_plan(m->M.row_start, m->M.col, m->M.val, P, m->sm_count, m->stream));
     }
     CU(cudaStreamSynchronize(m->stream));
+    TRY(build_col16(m));
     dfree(m->M.col);
     dfree(m->M.val);
-    m->l1 = 0;
-    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count);
+    m->l1 = m->P.colp16 ? 2 : 0;
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, m->l1);
     m->fix_grid = fixup_grid(m->num_tiles, m->sm_count);
-    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count);
-    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count);
-    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, m->l1);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, m->l1);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, m->l1);
     const int pmax = std::max(m->pgrid, std::max(m->pgrid32, m->pgridbf));
     TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
     TRY(ensure_cap(&m->partials, &m->partials_cap,
@@ -1348,7 +1387,7 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
 int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* grid, int32_t* power_grid,
                          float* tuned_ms) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
-    if (prefer_l1) *prefer_l1 = m->l1;
+    if (prefer_l1) *prefer_l1 = m->l1 & 1;
     if (grid) *grid = m->grid;
     if (power_grid) *power_grid = m->pgrid;
     if (tuned_ms) {
@@ -1363,11 +1402,18 @@ int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1) {
     if (prefer_l1 != 0 && prefer_l1 != 1) return fail(PWMGPU_ERR_INVALID, "prefer_l1 must be 0 or 1");
     if (!m->loaded || m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_STATE, "no merge-format matrix loaded");
     CU(cudaStreamSynchronize(m->stream));
-    m->l1 = prefer_l1;
-    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, prefer_l1);
-    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, prefer_l1);
-    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, prefer_l1);
-    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, prefer_l1);
+    m->l1 = prefer_l1 | (m->P.colp16 ? 2 : 0);
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, m->l1);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, m->l1);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, m->l1);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, m->l1);
+    return PWMGPU_OK;
+}
+
+int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (column_bytes) *column_bytes = m->format != PWMGPU_FMT_MERGE ? 4 : (m->P.colp16 ? 2 : 4);
     return PWMGPU_OK;
 }
 

@@ -254,6 +254,12 @@ class CudaSparseMatrix:
         check(_lib.lib().pwmgpu_launch_config(self._h, C.byref(a), C.byref(b), C.byref(c), ms), "launch_config")
         return a.value, b.value, c.value, (ms[0], ms[1])
 
+    def column_bytes(self):
+        """2 when the merge kernels stream 16-bit column offsets, else 4."""
+        b = C.c_int32()
+        check(_lib.lib().pwmgpu_plan_info(self._h, C.byref(b)), "pwmgpu_plan_info")
+        return b.value
+
     def set_launch_variant(self, prefer_l1):
         check(_lib.lib().pwmgpu_set_launch_variant(self._h, int(prefer_l1)), "set_launch_variant")
 
