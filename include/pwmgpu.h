@@ -149,11 +149,13 @@ int pwmgpu_power(pwmgpu_matrix* m, double* x, double* y, int32_t it);
 int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
 
 /* How pwmgpu_power / pwmgpu_power_device run the iterations:
- * AUTO (default) and FUSED use one persistent cooperative kernel for all
- * iterations (SpMV, norm and rescale fused; two grid barriers per iteration;
- * FUSED fails with PWMGPU_ERR_UNSUPPORTED where it cannot be co-resident);
- * MULTI launches an SpMV kernel and a fix-up / reduction kernel per
- * iteration.  Results are equal within the power method's tolerance. */
+ * FUSED uses one persistent cooperative kernel for all iterations (SpMV,
+ * fix-up, norm and rescale; three grid barriers per iteration; fails with
+ * PWMGPU_ERR_UNSUPPORTED where it cannot be co-resident); MULTI launches the
+ * SpMV, fix-up and norm kernels per iteration; AUTO (default) takes FUSED
+ * for matrices with fewer than two merge sub-tiles per resident warp (where
+ * launches would dominate), MULTI otherwise.  Results are equal within the
+ * power method's tolerance. */
 #define PWMGPU_POWER_AUTO 0
 #define PWMGPU_POWER_FUSED 1
 #define PWMGPU_POWER_MULTI 2

@@ -452,8 +452,9 @@ __device__ __forceinline__ void grid_total2(const double* partials, double* tota
     __syncthreads();
 }
 
+// (at most 80 registers: 6 CTAs per SM fit beside the 16-bit-column stages)
 template <typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0, bool C16 = false>
-__global__ void __launch_bounds__(NT) k_power_persistent(PowerArgs<VT, XT, AT> p) {
+__global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT> p) {
     using S = WarpStage<VT, IPT, C16>;
     constexpr int W = NT / 32;
     constexpr int NS = kMliStages;

@@ -348,9 +348,17 @@ int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double
     return PWMGPU_OK;
 }
 
+// POWER_AUTO: the persistent kernel saves three launches per iteration,
+// which pays while a pass is short; once every resident warp has a few
+// sub-tiles per pass, the two-kernel step is as fast or faster (its SpMV runs
+// the most resident CTAs and its kernel boundaries are cheaper than grid
+// barriers: 4096^2 Poisson 0.277 vs 0.29 ms per iteration, 1024^2 0.038 vs
+// 0.043, the irregular 4M matrix 0.418 vs 0.424).
 bool use_fused(const pwmgpu_matrix* m, int pgrid) {
-    if (m->power_mode == PWMGPU_POWER_MULTI) return false;
-    return pgrid > 0;
+    if (m->power_mode == PWMGPU_POWER_MULTI || pgrid <= 0) return false;
+    if (m->power_mode == PWMGPU_POWER_FUSED) return true;
+    const MergeGeom g = merge_geometry(kCfgF64, m->l1);
+    return m->num_tiles < 2LL * g.occ * g.w * m->sm_count;
 }
 
 int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
