@@ -47,6 +47,11 @@ struct MliPlan {
     int32_t* colp = nullptr;    // lane-interleaved column indices
     double* valp = nullptr;     // lane-interleaved FP64 values
     uint16_t* colp16 = nullptr; // or null: the same columns as offsets from the sub-tile's base (rec0.w)
+    // fix-up runs with a carry to add: {first sub-tile t, completing sub-tile n, row r, 0},
+    // ordered by t; run_pre[t] = runs whose first sub-tile is < t (nsub + 1 entries)
+    int4* runs = nullptr;
+    int* run_pre = nullptr;
+    int nruns = 0;
 };
 long long mli_storage_elems(long long nnz, long long nsub);
 
@@ -73,6 +78,13 @@ cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long 
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
                             int sm_count, cudaStream_t st);
 cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st);
+// fix-up run descriptors of a plan (P.runs, P.run_pre, P.nruns; scratch: 2 *
+// (nsub + 1) ints and nsub int4) and the fix-up over descriptors [k0, k1)
+int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, cudaStream_t st);
+cudaError_t launch_fix_runs_f64(int mode, const MliPlan& P, int k0, int k1, double* y, const double* carries,
+                                const double* nsq_in, cudaStream_t st);
+cudaError_t launch_fix_runs_f32(int mode, const MliPlan& P, int k0, int k1, float* y, const float* carries,
+                                const double* nsq_in, cudaStream_t st);
 cudaError_t launch_mli_colspan(const MliPlan& P, int* cbase, int* flag, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_col16(const MliPlan& P, const int* cbase, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);

@@ -129,6 +129,7 @@ struct pwmgpu_matrix {
     struct {
         int K = 0;          // chunks (0: not planned yet, -1: not pipelined)
         std::vector<int> rec;  // 4 per chunk: first sub-tile, first row, split flag, prefix max column
+        std::vector<int> fpre; // K + 1: fix-up descriptors of the runs starting before each chunk
         cudaStream_t in = nullptr, out = nullptr;
         std::vector<cudaEvent_t> ev_x, ev_y;
         cudaEvent_t ev_start = nullptr;
@@ -151,6 +152,8 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(P.masks);
         pwmgpu::dfree(P.colp);
         pwmgpu::dfree(P.colp16);
+        pwmgpu::dfree(P.runs);
+        pwmgpu::dfree(P.run_pre);
         pwmgpu::dfree(P.valp);
         P = MliPlan();
         pwmgpu::dfree(val32);

@@ -297,6 +297,47 @@ __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
     fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, t_end, stride);
 }
 
+// Fix-up runs, found once per matrix: sub-tile t starts a run when it leaves
+// row r = subc[t+1].x unfinished and sub-tile t-1 did not; the run's
+// sub-tiles t..n-1 all end in row r and sub-tile n completes it; the carries
+// are real only if n started inside row r (as in fixup_pass).
+__global__ void k_run_flags(const int32_t* __restrict__ row_start, const int2* __restrict__ subc, int nsub, int nor,
+                            int* __restrict__ flag, int4* __restrict__ desc) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nsub; t += gridDim.x * blockDim.x) {
+        const int r = subc[t + 1].x;
+        int ok = r < nor && (t == 0 || subc[t].x != r);
+        int n = t + 1;
+        if (ok) {
+            while (n < nsub && subc[n + 1].x == r) ++n;
+            ok = subc[n].y > row_start[r];
+        }
+        flag[t] = ok;
+        desc[t] = make_int4(t, n, r, 0);
+    }
+}
+
+// pre[t] = runs whose first sub-tile is before t
+__global__ void k_run_compact(const int* __restrict__ pre, const int4* __restrict__ desc, int nsub,
+                              int4* __restrict__ runs) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nsub; t += gridDim.x * blockDim.x)
+        if (pre[t + 1] != pre[t]) runs[pre[t]] = desc[t];
+}
+
+// One thread per run: y[r] += (carries[t] + ... + carries[n-1]) -- the sums of
+// fixup_pass in the same order, without its search (one descriptor load, then
+// the carries and y[r] together).
+template <int MODE, typename XT, typename AT>
+__global__ void __launch_bounds__(256) k_fix_runs(const int4* __restrict__ runs, int k0, int k1, XT* __restrict__ y,
+                                                  const AT* __restrict__ carries, const double* nsq_in) {
+    const int e = (MODE == MODE_POWER && nsq_in) ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
+    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+        const int4 d = runs[k];
+        AT sum = __ldcg(carries + d.x);
+        for (int j = d.x + 1; j < d.y; ++j) sum += __ldcg(carries + j);
+        y[d.z] = (XT)((AT)__ldcg(y + d.z) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+    }
+}
+
 // ||y||^2 (and x . y with DOT) with one deterministic reduction: per-CTA
 // partials, then the last CTA sums them in order.  out[0] = sum y^2,
 // out[1] = sum x y.
@@ -1003,10 +1044,78 @@ cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, doubl
     return cudaGetLastError();
 }
 
+// One thread per sub-tile: a fix-up is a short chain of dependent L2 loads,
+// so its time is latency, not bandwidth -- every sub-tile in flight at once
+// (a grid capped at one CTA per SM left ~7 sub-tiles per thread and cost
+// ~24 us per SpMV on the 4096^2 Poisson matrix).
+int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, cudaStream_t st) {
+    (void)sm_count;
+    P.nruns = 0;
+    if (P.nsub <= 0) return 0;
+    int* scan_scratch = nullptr;
+    int4* desc = nullptr;
+    int rc = 0;
+    const int nb = (P.nsub + 255) / 256;
+    do {
+        if (cudaMalloc((void**)&desc, sizeof(int4) * (size_t)P.nsub) != cudaSuccess ||
+            cudaMalloc((void**)&scan_scratch, sizeof(int) * (size_t)scan_scratch_elems(P.nsub + 1)) != cudaSuccess ||
+            cudaMalloc((void**)&P.run_pre, sizeof(int) * ((size_t)P.nsub + 1)) != cudaSuccess) {
+            rc = 1;
+            break;
+        }
+        // run_pre[0] = 0, run_pre[t + 1] = flag[t]; the inclusive scan of
+        // run_pre + 1 makes run_pre[t] the runs that start before t
+        if (cudaMemsetAsync(P.run_pre, 0, sizeof(int), st) != cudaSuccess) { rc = 1; break; }
+        k_run_flags<<<nb, 256, 0, st>>>(row_start, P.subc, P.nsub, nor, P.run_pre + 1, desc);
+        if (launch_inclusive_scan(P.run_pre + 1, P.nsub, scan_scratch, st) != cudaSuccess) { rc = 1; break; }
+        int total = 0;
+        if (cudaMemcpyAsync(&total, P.run_pre + P.nsub, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = 1;
+            break;
+        }
+        P.nruns = total;
+        if (cudaMalloc((void**)&P.runs, sizeof(int4) * (size_t)(total > 0 ? total : 1)) != cudaSuccess) { rc = 1; break; }
+        if (total > 0) k_run_compact<<<nb, 256, 0, st>>>(P.run_pre, desc, P.nsub, P.runs);
+        if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = 1;
+    } while (0);
+    if (desc) cudaFree(desc);
+    if (scan_scratch) cudaFree(scan_scratch);
+    if (rc) {
+        (void)cudaGetLastError();
+        if (P.runs) cudaFree(P.runs);
+        if (P.run_pre) cudaFree(P.run_pre);
+        P.runs = nullptr;
+        P.run_pre = nullptr;
+        P.nruns = 0;
+    }
+    return rc;
+}
+
+template <typename XT, typename AT>
+static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT* y, const AT* carries,
+                                 const double* nsq_in, cudaStream_t st) {
+    if (k1 <= k0) return cudaSuccess;
+    const int grid = (k1 - k0 + 255) / 256;
+    if (mode == MODE_POWER) k_fix_runs<MODE_POWER, XT, AT><<<grid, 256, 0, st>>>(P.runs, k0, k1, y, carries, nsq_in);
+    else k_fix_runs<MODE_SPMV, XT, AT><<<grid, 256, 0, st>>>(P.runs, k0, k1, y, carries, nsq_in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fix_runs_f64(int mode, const MliPlan& P, int k0, int k1, double* y, const double* carries,
+                                const double* nsq_in, cudaStream_t st) {
+    return fix_runs_impl<double, double>(mode, P, k0, k1, y, carries, nsq_in, st);
+}
+
+cudaError_t launch_fix_runs_f32(int mode, const MliPlan& P, int k0, int k1, float* y, const float* carries,
+                                const double* nsq_in, cudaStream_t st) {
+    return fix_runs_impl<float, float>(mode, P, k0, k1, y, carries, nsq_in, st);
+}
+
 int fixup_grid(int num_tiles, int sm_count) {
-    long long g = (num_tiles + 255) / 256;
-    if (g > sm_count) g = sm_count;
-    return g > 0 ? (int)g : 1;
+    (void)sm_count;
+    const long long g = (num_tiles + 255) / 256;
+    return g > 0 ? (int)(g < (1LL << 30) ? g : (1LL << 30)) : 1;
 }
 
 cudaError_t launch_power_finalize_f64(double* last, const double* nsq_last, double* prev, const double* nsq_prev,

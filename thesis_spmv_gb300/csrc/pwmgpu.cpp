@@ -246,6 +246,8 @@ int build_plan(pwmgpu_matrix* m) {
     }
     CU(cudaStreamSynchronize(m->stream));
     TRY(build_col16(m));
+    // fix-up descriptors; without them (no memory) the search-based fix-up runs
+    (void)build_fix_runs(m->P, m->M.row_start, m->M.nor, m->sm_count, m->stream);
     dfree(m->M.col);
     dfree(m->M.val);
     m->l1 = m->P.colp16 ? 2 : 0;
@@ -331,8 +333,11 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     if (m->num_tiles == 0) return PWMGPU_OK;
     CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, m->status,
                          m->stream, m->l1));
-    CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, m->fix_grid,
-                              m->stream));
+    if (m->P.runs)
+        CU(launch_fix_runs_f64(kModeSpmv, m->P, 0, m->P.nruns, dy, m->carries, nullptr, m->stream));
+    else
+        CU(launch_merge_fixup_f64(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, m->carries, nullptr, m->fix_grid,
+                                  m->stream));
     return PWMGPU_OK;
 }
 
@@ -341,8 +346,11 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
     CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
                          m->status, m->stream, m->l1));
-    CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in, m->fix_grid,
-                              m->stream));
+    if (m->P.runs)
+        CU(launch_fix_runs_f64(kModePower, m->P, 0, m->P.nruns, out, m->carries, nsq_in, m->stream));
+    else
+        CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, out, m->carries, nsq_in,
+                                  m->fix_grid, m->stream));
     CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, nsq_out,
                              dot_grid(m->M.nor, m->sm_count), m->stream));
     return PWMGPU_OK;
@@ -617,6 +625,12 @@ int plan_pipeline(pwmgpu_matrix* m) {
     for (int c = 1; c < K; ++c)
         if (p.rec[4 * c + 1] <= p.rec[4 * (c - 1) + 1]) return PWMGPU_OK;
     for (int c = 1; c < K; ++c) p.rec[4 * c + 3] = std::max(p.rec[4 * c + 3], p.rec[4 * (c - 1) + 3]);
+    p.fpre.assign(K + 1, 0);
+    if (m->P.runs) {
+        for (int c = 0; c < K; ++c)
+            CU(cudaMemcpy(&p.fpre[(size_t)c], m->P.run_pre + p.rec[4 * c], sizeof(int), cudaMemcpyDeviceToHost));
+        p.fpre[(size_t)K] = m->P.nruns;
+    }
     // streams and events outlive a reload of the matrix: create them once
     // highest priority: their copy kernels (pageable arrays) go ahead of SpMV CTAs
     int lo_prio = 0, hi_prio = 0;
@@ -698,7 +712,12 @@ int mv_pipelined(pwmgpu_matrix* m, const double* x, double* y) {
             // chunk c-1: fix-up of its runs (they end by chunk c), then its rows go down
             int t0, t1;
             chunk_tiles(c - 1, &t0, &t1);
-            CU(launch_merge_fixup_range(m->M, m->P.subc, nsub, t0, t1, m->dy, m->carries, m->stream, m->sm_count));
+            if (m->P.runs)
+                CU(launch_fix_runs_f64(kModeSpmv, m->P, p.fpre[(size_t)c - 1], p.fpre[(size_t)c], m->dy, m->carries,
+                                       nullptr, m->stream));
+            else
+                CU(launch_merge_fixup_range(m->M, m->P.subc, nsub, t0, t1, m->dy, m->carries, m->stream,
+                                            m->sm_count));
             CU(cudaEventRecord(p.ev_y[(size_t)c - 1], m->stream));
             CU(cudaStreamWaitEvent(p.out, p.ev_y[(size_t)c - 1], 0));
             const int r0 = row_lo(c - 1), r1 = row_lo(c);
@@ -1234,8 +1253,12 @@ int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     TRY(ensure_low_values(m, false, &cfg, &valp, &pg));
     CU(launch_merge_spmv(kCfgF32, kModeSpmv, m->M, valp, m->P, merge_grid(kCfgF32, m->num_tiles, m->sm_count, m->l1),
                          dx, dy, m->carries, nullptr, m->status, m->stream, m->l1));
-    CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
-                              nullptr, m->fix_grid, m->stream));
+    if (m->P.runs)
+        CU(launch_fix_runs_f32(kModeSpmv, m->P, 0, m->P.nruns, dy, reinterpret_cast<float*>(m->carries), nullptr,
+                               m->stream));
+    else
+        CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
+                                  nullptr, m->fix_grid, m->stream));
     return PWMGPU_OK;
 }
 
