@@ -33,6 +33,14 @@ __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor on the stream finishes;
+// pdl_wait() blocks until the predecessor has completed and its writes are
+// visible (a no-op without such a predecessor); pdl_trigger() lets this
+// kernel's own dependent launch start early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }

@@ -265,12 +265,14 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     __shared__ AT cval[NT];
     __shared__ AT hval[NT];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     if (lane == 0) {
         for (int k = 0; k < NS; ++k) mbar_init(&bars[w][k], 1);
         fence_mbar_init();
     }
     __syncwarp();
+    // x, y, carries and ||x||^2 may belong to the kernel before on the stream
+    pdl_wait();
+    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     uint32_t ticket = 0;
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
     warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16>(a, a.x, a.y, stages, bars[w], crow + 32 * w, cval + 32 * w,
@@ -329,9 +331,12 @@ __global__ void k_run_compact(const int* __restrict__ pre, const int4* __restric
 template <int MODE, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_fix_runs(const int4* __restrict__ runs, int k0, int k1, XT* __restrict__ y,
                                                   const AT* __restrict__ carries, const double* nsq_in) {
+    const int kk = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int4 d0 = kk < k1 ? runs[kk] : make_int4(0, 0, 0, 0);  // plan data: before the wait
+    pdl_wait();  // carries and y come from the SpMV before on the stream
     const int e = (MODE == MODE_POWER && nsq_in) ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
-    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
-        const int4 d = runs[k];
+    for (int k = kk; k < k1; k += gridDim.x * blockDim.x) {
+        const int4 d = k == kk ? d0 : runs[k];
         AT sum = __ldcg(carries + d.x);
         for (int j = d.x + 1; j < d.y; ++j) sum += __ldcg(carries + j);
         y[d.z] = (XT)((AT)__ldcg(y + d.z) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
@@ -813,26 +818,36 @@ struct MergeKernels {
     }
 
     template <int L1, bool C16>
-    static void launch_spmv(int mode, const MergeArgs<VT, XT, AT>& a, int grid, cudaStream_t st) {
+    static void launch_spmv(int mode, const MergeArgs<VT, XT, AT>& a, int grid, cudaStream_t st, bool pdl) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = smem(C16);
+        cfg.stream = st;
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr.val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = pdl ? 1 : 0;
         if (mode == MODE_POWER)
-            k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16><<<grid, NT, smem(C16), st>>>(a);
+            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16>, a);
         else
-            k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16><<<grid, NT, smem(C16), st>>>(a);
+            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16>, a);
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                            cudaStream_t st, int v, int tile0 = 0, int nsub = -1) {
+                            cudaStream_t st, int v, int tile0 = 0, int nsub = -1, bool pdl = true) {
         if (!P.colp16) v &= 1;
         geom(v);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
                                 nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
                                 tile0, P.colp16};
         switch (v & 3) {
-            case 1: launch_spmv<1, false>(mode, a, grid, st); break;
-            case 2: launch_spmv<0, true>(mode, a, grid, st); break;
-            case 3: launch_spmv<1, true>(mode, a, grid, st); break;
-            default: launch_spmv<0, false>(mode, a, grid, st); break;
+            case 1: launch_spmv<1, false>(mode, a, grid, st, pdl); break;
+            case 2: launch_spmv<0, true>(mode, a, grid, st, pdl); break;
+            case 3: launch_spmv<1, true>(mode, a, grid, st, pdl); break;
+            default: launch_spmv<0, false>(mode, a, grid, st, pdl); break;
         }
         return cudaGetLastError();
     }
@@ -1026,7 +1041,9 @@ cudaError_t launch_pipeline_plan(const int32_t* row_start, const MliPlan& P, int
 cudaError_t launch_merge_spmv_range(const DevMatrix& M, const MliPlan& P, int t0, int t1, int grid, const double* x,
                                     double* y, double* carries, int* status, cudaStream_t st, int l1) {
     if (t1 <= t0) return cudaSuccess;
-    return CfgF64::spmv(MODE_SPMV, M, P.valp, P, grid, x, y, carries, nullptr, status, st, l1, t0, t1 - t0);
+    // without programmatic overlap: CTAs waiting on the previous chunk would hold
+    // the SMs the pageable-array copy kernels of the other streams need
+    return CfgF64::spmv(MODE_SPMV, M, P.valp, P, grid, x, y, carries, nullptr, status, st, l1, t0, t1 - t0, false);
 }
 
 cudaError_t launch_merge_fixup_range(const DevMatrix& M, const int2* tiles, int num_tiles, int f0, int f1, double* y,
@@ -1096,9 +1113,18 @@ template <typename XT, typename AT>
 static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT* y, const AT* carries,
                                  const double* nsq_in, cudaStream_t st) {
     if (k1 <= k0) return cudaSuccess;
-    const int grid = (k1 - k0 + 255) / 256;
-    if (mode == MODE_POWER) k_fix_runs<MODE_POWER, XT, AT><<<grid, 256, 0, st>>>(P.runs, k0, k1, y, carries, nsq_in);
-    else k_fix_runs<MODE_SPMV, XT, AT><<<grid, 256, 0, st>>>(P.runs, k0, k1, y, carries, nsq_in);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((k1 - k0 + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    const int4* runs = P.runs;
+    if (mode == MODE_POWER) cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_POWER, XT, AT>, runs, k0, k1, y, carries, nsq_in);
+    else cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_SPMV, XT, AT>, runs, k0, k1, y, carries, nsq_in);
     return cudaGetLastError();
 }
 
