@@ -315,7 +315,7 @@ struct BatchKernels {
     }
     static cudaError_t step(const BatchTable* T, int want_dot, int sm_count, cudaStream_t st) {
         k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid(sm_count), kBatchNT, SMEM, st>>>(T);
-        k_batch_fixup<XT, AT><<<2 * sm_count, 256, 0, st>>>(T);
+        k_batch_fixup<XT, AT><<<8 * sm_count, 256, 0, st>>>(T);
         k_batch_norm<XT><<<4 * sm_count, 256, 0, st>>>(T, want_dot);
         return cudaGetLastError();
     }

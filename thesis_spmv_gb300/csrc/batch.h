@@ -15,7 +15,7 @@
 
 namespace pwmgpu {
 
-constexpr int kFixTiles = 2048;   // sub-tiles per fix-up chunk
+constexpr int kFixTiles = 256;    // sub-tiles per fix-up chunk (one per thread: a fix-up is latency-bound)
 constexpr int kRowChunk = 32768;  // rows per norm / residual chunk
 
 struct BatchSlot {
