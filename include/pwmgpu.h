@@ -169,7 +169,8 @@ int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
  * PWMGPU_PREC_*.  lambda is the Rayleigh quotient u^T A u of the returned u
  * (||u|| = 1), the normalised iterate after iterations - 1 SpMVs (the last
  * SpMV computes A u for lambda and the residual).  The residual test runs
- * every chunk of iterations inside the persistent kernel (FP64 reductions);
+ * after every chunk of iterations (FP64 reductions), the chunk executed as
+ * pwmgpu_set_power_mode selects (the persistent kernel, or separate kernels);
  * MIXED runs FP32 (BF16 values where exact) until the residual reaches 2e-6,
  * stops falling below 1e-4 (the FP32 rounding floor), or only the FP64
  * reserve of min(64, max_it/4) iterations is left; then FP64 to tol. */

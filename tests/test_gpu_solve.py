@@ -51,13 +51,24 @@ def _load(pwm, A):
     return M
 
 
+POWER_MODES = ["fused", "multi"]
+
+
+def _set_mode(pwm, M, mode):
+    """fused: the persistent kernel runs each chunk; multi: SpMV, fix-up and
+    norm kernels per iteration plus the result pass."""
+    M.set_power_mode(pwm.POWER_FUSED if mode == "fused" else pwm.POWER_MULTI)
+
+
+@pytest.mark.parametrize("mode", POWER_MODES)
 @pytest.mark.parametrize("kind,it", [("poisson", 2), ("poisson", 37), ("random", 2), ("random", 24),
                                      ("poisson", 301)])
-def test_solve_equal_counts_matches_oracle(pwm, kind, it):
+def test_solve_equal_counts_matches_oracle(pwm, kind, it, mode):
     """tol = 0: exactly `it` SpMVs; lambda and u are those of the oracle's
     iterate after it - 1 steps of powerIteration."""
     A = O.fill_poisson(37, 23) if kind == "poisson" else _positive_random(3000, 7, 5)
     M = _load(pwm, A)
+    _set_mode(pwm, M, mode)
     x0 = np.random.default_rng(8).random(A.nor)
     u = x0.copy()
     info = M.solve(u, it, 0.0, pwm.PREC_F64)
@@ -84,13 +95,15 @@ def test_solve_poisson_analytic_lambda_max(pwm, m):
     assert abs(np.linalg.norm(u) - 1.0) <= 1e-12
 
 
+@pytest.mark.parametrize("mode", POWER_MODES)
 @pytest.mark.parametrize("kind", ["poisson", "random"])
-def test_solve_mixed_reaches_tolerance(pwm, kind):
+def test_solve_mixed_reaches_tolerance(pwm, kind, mode):
     """FP32 (BF16 values for the exactly representable Poisson stencil) bulk
     phase, FP64 refinement: the oracle confirms the residual, and lambda
     matches the FP64 solve."""
     A = O.fill_poisson(14, 14) if kind == "poisson" else _positive_random(20000, 8, 9)
     M = _load(pwm, A)
+    _set_mode(pwm, M, mode)
     x0 = np.random.default_rng(3).random(A.nor)
     tol = 1e-10
     u64 = x0.copy()
@@ -158,3 +171,24 @@ def test_mv_device_f32_row_bound(pwm, kind):
     s = O.crs_mv(O.CRSArrays(A.nor, A.noc, A.row_start, A.col_ind, np.abs(A.data)), np.abs(x))
     bound = (2 * nnz_row + 3) * 2.0 ** -24 * s
     assert np.all(np.abs(y - ref) <= bound)
+
+
+def test_solve_modes_agree_on_a_large_poisson_grid(pwm):
+    """Large enough that AUTO takes the separate kernels: 60 steps in both
+    forms give the same iterates (the SpMV bits do not depend on how the
+    norms were summed), so lambda agrees to rounding; FP64 and mixed each."""
+    g = 600
+    M = pwm.CRSCuda(1)
+    M.generatePoissonMatrix(g, g, 1)
+    x0 = np.random.default_rng(4).random(g * g)
+    lam = {}
+    for mode in POWER_MODES:
+        _set_mode(pwm, M, mode)
+        for prec in (pwm.PREC_F64, pwm.PREC_MIXED):
+            u = x0.copy()
+            info = M.solve(u, 60, 0.0, prec)
+            assert info.iterations == 60
+            lam[(mode, prec)] = info.lambda_
+    for prec, tol in ((pwm.PREC_F64, 1e-12), (pwm.PREC_MIXED, 1e-9)):
+        a, b = lam[("fused", prec)], lam[("multi", prec)]
+        assert abs(a - b) <= tol * abs(a)

@@ -78,6 +78,12 @@ cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long 
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
                             int sm_count, cudaStream_t st);
 cudaError_t launch_mli_convert(const MliPlan& P, int cfg, void* out, int sm_count, cudaStream_t st);
+// the separate-kernel form of a solve chunk: FP32 norm pass and the result pass
+cudaError_t launch_power_norm_f32(const float* y, const float* x, int n, double* partials, unsigned int* counter,
+                                  double* out, int grid, cudaStream_t st);
+cudaError_t launch_solve_result(bool f32, const void* in, const void* out, int n, const double* nsq_k,
+                                const double* nd, double* nsq_next, double* result, double* partials,
+                                unsigned int* counter, int grid, cudaStream_t st);
 // fix-up run descriptors of a plan (P.runs, P.run_pre, P.nruns; scratch: 2 *
 // (nsub + 1) ints and nsub int4) and the fix-up over descriptors [k0, k1)
 int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, cudaStream_t st);

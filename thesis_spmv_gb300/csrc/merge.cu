@@ -669,6 +669,51 @@ __global__ void __launch_bounds__(256) k_dot2(const XT* __restrict__ va, const X
     }
 }
 
+// The result pass of a solve chunk run with separate kernels (the persistent
+// kernel's `want_dot` pass): from ||v_k||^2 (nsq_k, k >= 1) and nd = {||v_{k+1}||^2,
+// v_k . v_{k+1}} of the last norm pass, lambda_k = 2^{-e} dot / ||v_k||^2 and
+// the eigen-residual ||2^{-e} v_{k+1} - lambda_k v_k||^2 (deterministic:
+// per-CTA partials summed in order by the last CTA); result = {lambda,
+// residual^2, ||v_k||^2, dot, e}, and nsq_next = ||v_{k+1}||^2.
+template <typename XT>
+__global__ void __launch_bounds__(256) k_solve_result(const XT* __restrict__ in, const XT* __restrict__ out, int n,
+                                                      const double* nsq_k, const double* nd, double* nsq_next,
+                                                      double* result, double* partials, unsigned int* counter) {
+    __shared__ double red[32];
+    __shared__ bool am_last;
+    const double nsq_last = *nsq_k, dot = nd[1];
+    const int e = pow2_rescale_exponent(nsq_last, rescale_window<XT>());
+    const double lam = scale_pow2(dot, -e) / nsq_last;
+    double rr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double d = scale_pow2((double)__ldcg(out + i), -e) - lam * (double)__ldcg(in + i);
+        rr = fma(d, d, rr);
+    }
+    const double t = block_sum<256>(rr, red);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = t;
+        __threadfence();
+        am_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (am_last && threadIdx.x < 32) {
+        __threadfence();
+        const int l = threadIdx.x;
+        double a0 = 0.0;
+        for (int i = l; i < (int)gridDim.x; i += 32) a0 += __ldcg(partials + i);
+        for (int o = 16; o > 0; o >>= 1) a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        if (l == 0) {
+            result[0] = lam;
+            result[1] = a0;
+            result[2] = nsq_last;
+            result[3] = dot;
+            result[4] = (double)e;
+            *nsq_next = nd[0];
+            *counter = 0u;
+        }
+    }
+}
+
 template <typename XT>
 __global__ void __launch_bounds__(256) k_resid(const XT* __restrict__ va, double sa, const XT* __restrict__ vb,
                                                double sb, int n, double* partials, unsigned int* counter,
@@ -1065,6 +1110,25 @@ cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, doubl
 // so its time is latency, not bandwidth -- every sub-tile in flight at once
 // (a grid capped at one CTA per SM left ~7 sub-tiles per thread and cost
 // ~24 us per SpMV on the 4096^2 Poisson matrix).
+cudaError_t launch_power_norm_f32(const float* y, const float* x, int n, double* partials, unsigned int* counter,
+                                  double* out, int grid, cudaStream_t st) {
+    if (x) k_power_norm<float, true><<<grid, 256, 0, st>>>(y, x, n, partials, counter, out);
+    else k_power_norm<float, false><<<grid, 256, 0, st>>>(y, x, n, partials, counter, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_result(bool f32, const void* in, const void* out, int n, const double* nsq_k,
+                                const double* nd, double* nsq_next, double* result, double* partials,
+                                unsigned int* counter, int grid, cudaStream_t st) {
+    if (f32)
+        k_solve_result<float><<<grid, 256, 0, st>>>((const float*)in, (const float*)out, n, nsq_k, nd, nsq_next,
+                                                     result, partials, counter);
+    else
+        k_solve_result<double><<<grid, 256, 0, st>>>((const double*)in, (const double*)out, n, nsq_k, nd, nsq_next,
+                                                      result, partials, counter);
+    return cudaGetLastError();
+}
+
 int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, cudaStream_t st) {
     (void)sm_count;
     P.nruns = 0;

@@ -470,10 +470,52 @@ namespace {
 struct ChunkOut {
     double lambda, rel;
 };
+// Iterations k0 .. k0+nk-1 of a solve and the Rayleigh quotient / residual of
+// the last: in the persistent kernel, or (where the two-kernel step is the
+// faster, see use_fused) as SpMV, fix-up and norm kernels per iteration plus
+// a result pass -- the same steps; only the order of the reductions' sums
+// differs.
 int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X, void* Y, int k0, int nk,
                 ChunkOut* o) {
-    CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
-                               m->partials, m->barrier, m->status, m->stream, m->l1));
+    if (use_fused(m, pgrid)) {
+        CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
+                                   m->partials, m->barrier, m->status, m->stream, m->l1));
+    } else {
+        const bool f32 = cfg != kCfgF64;
+        const int grid = merge_grid(cfg, m->num_tiles, m->sm_count, m->l1);
+        const int dg = dot_grid(m->M.nor, m->sm_count);
+        for (int k = k0; k < k0 + nk; ++k) {
+            void* in = (k & 1) ? Y : X;
+            void* out = (k & 1) ? X : Y;
+            const double* nsq_in = k > 0 ? m->nsq + k : nullptr;
+            const bool last = k == k0 + nk - 1;
+            CU(launch_merge_spmv(cfg, kModePower, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
+                                 m->stream, m->l1));
+            if (f32) {
+                if (m->P.runs)
+                    CU(launch_fix_runs_f32(kModePower, m->P, 0, m->P.nruns, (float*)out, (const float*)m->carries,
+                                           nsq_in, m->stream));
+                else
+                    CU(launch_merge_fixup_f32(kModePower, m->M, m->P.subc, m->num_tiles, (float*)out,
+                                              (const float*)m->carries, nsq_in, m->fix_grid, m->stream));
+                CU(launch_power_norm_f32((const float*)out, last ? (const float*)in : nullptr, m->M.nor, m->partials,
+                                         m->counter, last ? m->small + 6 : m->nsq + k + 1, dg, m->stream));
+            } else {
+                if (m->P.runs)
+                    CU(launch_fix_runs_f64(kModePower, m->P, 0, m->P.nruns, (double*)out, m->carries, nsq_in,
+                                           m->stream));
+                else
+                    CU(launch_merge_fixup_f64(kModePower, m->M, m->P.subc, m->num_tiles, (double*)out, m->carries,
+                                              nsq_in, m->fix_grid, m->stream));
+                CU(launch_power_norm_f64((const double*)out, last ? (const double*)in : nullptr, m->M.nor,
+                                         m->partials, m->counter, last ? m->small + 6 : m->nsq + k + 1, dg,
+                                         m->stream));
+            }
+            if (last)
+                CU(launch_solve_result(f32, in, out, m->M.nor, m->nsq + k, m->small + 6, m->nsq + k + 1, m->small,
+                                       m->partials, m->counter, dg, m->stream));
+        }
+    }
     CU(cudaMemcpyAsync(m->hres, m->small, 5 * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
     TRY(check_status(m));
     const double lam = m->hres[0], r2 = m->hres[1], nsq = m->hres[2];
@@ -526,7 +568,8 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
         int cfg = kCfgF32, pg = 0;
         const void* valp = nullptr;
         TRY(ensure_low_values(m, precision == PWMGPU_PREC_MIXED, &cfg, &valp, &pg));
-        if (pg == 0) return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
+        if (pg == 0 && m->power_mode == PWMGPU_POWER_FUSED)
+            return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
         TRY(ensure_fvectors(m));
         CU(launch_convert_f64_f32(m->dx, m->fx, N, m->sm_count, m->stream));
         int kl = 0, chunk = 16, nchunks = 0;
@@ -562,7 +605,8 @@ int solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision
         }
     }
     if (precision != PWMGPU_PREC_F32) {
-        if (m->pgrid == 0) return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
+        if (m->pgrid == 0 && m->power_mode == PWMGPU_POWER_FUSED)
+            return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident");
         int kl = 0, chunk = precision == PWMGPU_PREC_MIXED ? 8 : 16;
         double prev = precision == PWMGPU_PREC_MIXED ? o.rel : 1.0;
         while (true) {
@@ -1280,8 +1324,6 @@ int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int pr
     if (!(tol >= 0.0)) return fail(PWMGPU_ERR_INVALID, "tol must be >= 0");
     if (precision != PWMGPU_PREC_F64 && precision != PWMGPU_PREC_F32 && precision != PWMGPU_PREC_MIXED)
         return fail(PWMGPU_ERR_INVALID, "unknown precision %d", precision);
-    if (m->power_mode == PWMGPU_POWER_MULTI)
-        return fail(PWMGPU_ERR_UNSUPPORTED, "the solve runs on the fused power kernel only");
     if (m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_UNSUPPORTED, "the solve runs on the merge format");
     std::memset(info, 0, sizeof *info);
     return solve(m, x, max_it, tol, precision, info);
