@@ -180,6 +180,7 @@ struct MergeArgs {
     int* status;
     int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
     const uint16_t* colp16 = nullptr;  // C16 kernels: 16-bit column offsets (base in rec0.w)
+    int cg = 0;                        // gathers bypass L1
 };
 
 constexpr int kMliStages = 2;
@@ -219,7 +220,7 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         const bool ok = mbar_wait_bounded(&bars[k], (u / NS) & 1u, a.status);
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
         AT xv[IPT];
-        gather_subtile<VT, XT, AT, IPT, XCOH, C16>(st, x, xv);
+        gather_subtile<VT, XT, AT, IPT, XCOH, C16>(st, x, xv, a.cg != 0);
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
             finish_subtile<MODE, true, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
                                                              cval, hval);
@@ -849,7 +850,8 @@ struct MergeKernels {
     static cudaError_t power(const DevMatrix& M, const void* valp, const MliPlan& P, int grid, void* X, void* Y,
                              void* carries, int k0, int nk, double* nsq, double* result, double* partials,
                              unsigned int* barrier, int* status, cudaStream_t st, int v) {
-        if (!P.colp16) v &= 1;
+        if (!P.colp16) v &= ~2;
+        v &= 3;
         power_occ(v);
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
                                  nullptr, (AT*)carries, nullptr, status, 0, P.colp16},
@@ -883,11 +885,11 @@ struct MergeKernels {
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
                             cudaStream_t st, int v, int tile0 = 0, int nsub = -1, bool pdl = true) {
-        if (!P.colp16) v &= 1;
+        if (!P.colp16) v &= ~2;
         geom(v);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
                                 nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
-                                tile0, P.colp16};
+                                tile0, P.colp16, (v >> 2) & 1};
         switch (v & 3) {
             case 1: launch_spmv<1, false>(mode, a, grid, st, pdl); break;
             case 2: launch_spmv<0, true>(mode, a, grid, st, pdl); break;
