@@ -679,7 +679,7 @@ def main():
     ap.add_argument("--batch-only", action="store_true",
                     help="only the 256-matrix batch through the FP64 service (a profiling case)")
     ap.add_argument("--stream-requests", type=int, default=48)
-    ap.add_argument("--stream-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0])
+    ap.add_argument("--stream-rates", type=float, nargs="+", default=[50.0, 100.0, 200.0, 500.0, 1000.0, 2000.0])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
