@@ -623,7 +623,11 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "poisson2d_%dx%d_fp64_spmv" % (grid_side, grid_side), "N": N, "nnz": nnz,
                    "l2": "inputs larger than L2 (1.34 GB per pass)", "items_per_tile": tm, "tiles": ntiles,
-                   "grid": grid, "parallelism": "replicas" if world > 1 else "single"},
+                   "grid": grid, "launch_variant": dict(zip(("prefer_l1", "grid", "power_grid", "tuned_ms"),
+                                                            M.launch_config()),
+                                                        column_bytes=M.plan_info()[0],
+                                                        gathers_bypass_l1=M.plan_info()[1]),
+                   "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": round(B / (ms * 1e-3) / 1e9, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(B / (ms * 1e-3) / 1e9 / peak, 4), "traffic": traffic,
                      "peak_source": peak_kind, "frac_of_nominal_8TBs": round(B / (ms * 1e-3) / 1e9 / NOMINAL_HBM_GBS, 4),

@@ -251,8 +251,10 @@ int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* gr
 int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1);
 /* Bytes per column index the merge kernels stream: 2 when every merge
  * sub-tile's columns span less than 2^16 (banded and stencil matrices: the
- * plan then keeps 16-bit offsets from a per-sub-tile base), else 4. */
-int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes);
+ * plan then keeps 16-bit offsets from a per-sub-tile base), else 4; and
+ * whether the load-time tuner chose x gathers that bypass L1 (1) or not (0).
+ * Either pointer may be null. */
+int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes, int32_t* gathers_bypass_l1);
 
 /* Tile size (merge items per tile) and tile count used by the SpMV kernel. */
 int pwmgpu_tile_info(const pwmgpu_matrix* m, int32_t* items_per_tile, int32_t* num_tiles, int32_t* grid);

@@ -58,7 +58,8 @@ long long mli_storage_elems(long long nnz, long long nsub);
 // l1: launch variant of the merge kernels.  Bit 0: 0 = most resident CTAs,
 // 1 = a smaller shared-memory carveout, more L1 for irregular gathers; bit 1:
 // stream the plan's 16-bit column offsets (set only when the plan has them);
-// bit 2: the SpMV's x gathers bypass L1 (the persistent kernel ignores it).
+// bit 2: the FP64 SpMV's x gathers bypass L1 (the persistent and the
+// low-precision kernels ignore it).
 MergeGeom merge_geometry(int cfg, int l1 = 0);
 int merge_grid(int cfg, int nsub, int sm_count, int l1 = 0);
 int fixup_grid(int num_tiles, int sm_count);

@@ -11,6 +11,7 @@
 //   k_dot2 / k_resid   Rayleigh quotient and eigen-residual passes (not in the
 //                       reference; used by the solve with a stopping test)
 #include <cstdio>
+#include <type_traits>
 
 #include "internal.h"
 #include "merge.cuh"
@@ -180,7 +181,6 @@ struct MergeArgs {
     int* status;
     int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
     const uint16_t* colp16 = nullptr;  // C16 kernels: 16-bit column offsets (base in rec0.w)
-    int cg = 0;                        // gathers bypass L1
 };
 
 constexpr int kMliStages = 2;
@@ -190,7 +190,7 @@ constexpr int kMliStages = 2;
 // warp's stage uses so far, so mbarrier phases carry across passes of a
 // persistent kernel.  Returns false (warp-uniformly) after a timeout, once
 // this warp's copies in flight have landed or a short bound ran out.
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH, bool C16>
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH, bool C16, bool CG = false>
 __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
                                           XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
                                           AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol) {
@@ -220,7 +220,7 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         const bool ok = mbar_wait_bounded(&bars[k], (u / NS) & 1u, a.status);
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
         AT xv[IPT];
-        gather_subtile<VT, XT, AT, IPT, XCOH, C16>(st, x, xv, a.cg != 0);
+        gather_subtile<VT, XT, AT, IPT, XCOH, C16, CG>(st, x, xv);
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
             finish_subtile<MODE, true, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
                                                              cval, hval);
@@ -255,7 +255,9 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
 // 1: a smaller carveout that leaves more L1 for the x gathers); the code is
 // the same, the two instances carry different function attributes.
 // C16: the plan's 16-bit column offsets are streamed instead of 32-bit columns.
-template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0, bool C16 = false>
+// CG: the x gathers bypass L1 (FP64 instances only).
+template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, int L1 = 0, bool C16 = false,
+          bool CG = false>
 __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     using S = WarpStage<VT, IPT, C16>;
     constexpr int W = NT / 32;
@@ -276,8 +278,9 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     uint32_t ticket = 0;
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
-    warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16>(a, a.x, a.y, stages, bars[w], crow + 32 * w, cval + 32 * w,
-                                                     hval + 32 * w, ticket, e, policy_evict_first());
+    warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16, CG>(a, a.x, a.y, stages, bars[w], crow + 32 * w,
+                                                         cval + 32 * w, hval + 32 * w, ticket, e,
+                                                         policy_evict_first());
 }
 
 template <typename XT, typename AT>
@@ -797,9 +800,15 @@ struct MergeKernels {
         return o;
     }
 
+    static constexpr bool kHasCG = std::is_same<VT, double>::value;
+
     template <int L1, bool C16>
     static int setup_spmv() {
         setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
+        if constexpr (kHasCG) {
+            setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16, true>, L1, smem(C16));
+            setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16, true>, L1, smem(C16));
+        }
         return setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
     }
 
@@ -864,7 +873,7 @@ struct MergeKernels {
         return cudaLaunchCooperativeKernel(power_kernel(v), dim3(grid), dim3(NT), args, smem(v & 2), st);
     }
 
-    template <int L1, bool C16>
+    template <int L1, bool C16, bool CG = false>
     static void launch_spmv(int mode, const MergeArgs<VT, XT, AT>& a, int grid, cudaStream_t st, bool pdl) {
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3(grid);
@@ -877,9 +886,21 @@ struct MergeKernels {
         cfg.attrs = &attr;
         cfg.numAttrs = pdl ? 1 : 0;
         if (mode == MODE_POWER)
-            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16>, a);
+            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16, CG>, a);
         else
-            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16>, a);
+            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16, CG>, a);
+    }
+
+    template <int L1, bool C16>
+    static void launch_spmv_cg(bool cg, int mode, const MergeArgs<VT, XT, AT>& a, int grid, cudaStream_t st,
+                               bool pdl) {
+        if constexpr (kHasCG) {
+            if (cg) {
+                launch_spmv<L1, C16, true>(mode, a, grid, st, pdl);
+                return;
+            }
+        }
+        launch_spmv<L1, C16, false>(mode, a, grid, st, pdl);
     }
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
@@ -889,12 +910,13 @@ struct MergeKernels {
         geom(v);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
                                 nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
-                                tile0, P.colp16, (v >> 2) & 1};
+                                tile0, P.colp16};
+        const bool cg = (v >> 2) & 1;
         switch (v & 3) {
-            case 1: launch_spmv<1, false>(mode, a, grid, st, pdl); break;
-            case 2: launch_spmv<0, true>(mode, a, grid, st, pdl); break;
-            case 3: launch_spmv<1, true>(mode, a, grid, st, pdl); break;
-            default: launch_spmv<0, false>(mode, a, grid, st, pdl); break;
+            case 1: launch_spmv_cg<1, false>(cg, mode, a, grid, st, pdl); break;
+            case 2: launch_spmv_cg<0, true>(cg, mode, a, grid, st, pdl); break;
+            case 3: launch_spmv_cg<1, true>(cg, mode, a, grid, st, pdl); break;
+            default: launch_spmv_cg<0, false>(cg, mode, a, grid, st, pdl); break;
         }
         return cudaGetLastError();
     }

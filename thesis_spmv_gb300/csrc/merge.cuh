@@ -218,11 +218,10 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 // it is read with ordinary coherent loads (ld.global.ca: L1-cached, and
 // ordered after the grid barrier's acquire) instead of the read-only
 // non-coherent path.
-// cg: gathers that bypass L1 (ld.global.cg) -- faster where x is spread too
+// CG: gathers that bypass L1 (ld.global.cg) -- faster where x is spread too
 // widely for L1 to hit (the launch tuner decides per matrix).
-template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false, bool C16 = false>
-__device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT],
-                                               bool cg = false) {
+template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false, bool C16 = false, bool CG = false>
+__device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT]) {
     using S = WarpStage<VT, IPT, C16>;
     const int lane = threadIdx.x & 31;
     const int nkw = reinterpret_cast<const int4*>(st)[1].w;
@@ -241,7 +240,7 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
     if (XCOH) {
 #pragma unroll
         for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldca(x + cv[j]) : AT(0);
-    } else if (cg) {
+    } else if (CG) {
 #pragma unroll
         for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldcg(x + cv[j]) : AT(0);
     } else {

@@ -165,7 +165,7 @@ int tune(pwmgpu_matrix* m) {
         const int v = cand[c] | c16;
         const int grid = merge_grid(kCfgF64, m->num_tiles, m->sm_count, v);
         cudaError_t e = cudaSuccess;
-        for (int r = 0; r < 5 && e == cudaSuccess; ++r) {  // one warm-up, four timed
+        for (int r = 0; r < 9 && e == cudaSuccess; ++r) {  // one warm-up, eight timed
             if (r == 1) e = cudaEventRecord(e0, m->stream);
             if (e == cudaSuccess)
                 e = launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, grid, m->dx, m->dy, m->carries,
@@ -175,7 +175,7 @@ int tune(pwmgpu_matrix* m) {
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[c], e0, e1);
         if (e != cudaSuccess) rc = fail(PWMGPU_ERR_CUDA, "launch tuning: %s", cudaGetErrorString(e));
-        ms[c] /= 4.f;
+        ms[c] /= 8.f;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1492,10 +1492,12 @@ int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1) {
     return PWMGPU_OK;
 }
 
-int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes) {
+int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes, int32_t* gathers_bypass_l1) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
     if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
-    if (column_bytes) *column_bytes = m->format != PWMGPU_FMT_MERGE ? 4 : (m->P.colp16 ? 2 : 4);
+    const bool merge = m->format == PWMGPU_FMT_MERGE;
+    if (column_bytes) *column_bytes = merge && m->P.colp16 ? 2 : 4;
+    if (gathers_bypass_l1) *gathers_bypass_l1 = merge && (m->l1 & 4) ? 1 : 0;
     return PWMGPU_OK;
 }
 

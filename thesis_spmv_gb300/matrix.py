@@ -256,9 +256,13 @@ class CudaSparseMatrix:
 
     def column_bytes(self):
         """2 when the merge kernels stream 16-bit column offsets, else 4."""
-        b = C.c_int32()
-        check(_lib.lib().pwmgpu_plan_info(self._h, C.byref(b)), "pwmgpu_plan_info")
-        return b.value
+        return self.plan_info()[0]
+
+    def plan_info(self):
+        """(bytes per streamed column index, 1 if the x gathers bypass L1)."""
+        b, g = C.c_int32(), C.c_int32()
+        check(_lib.lib().pwmgpu_plan_info(self._h, C.byref(b), C.byref(g)), "pwmgpu_plan_info")
+        return b.value, g.value
 
     def set_launch_variant(self, prefer_l1):
         check(_lib.lib().pwmgpu_set_launch_variant(self._h, int(prefer_l1)), "set_launch_variant")
