@@ -83,8 +83,15 @@ __device__ __forceinline__ int4 prefetch_rec(const BatchTable& T, int g, int& j)
     return __ldg(d->rec + 2LL * (g - d->tile0) + 1);
 }
 
+// Resident CTAs per SM the kernel is compiled for: the low-precision classes
+// are latency-bound (no FP64 pipe limit), so they trade registers for warps.
+template <typename VT>
+constexpr int batch_min_ctas() {
+    return sizeof(VT) == 8 ? 5 : 8;
+}
+
 template <typename VT, typename XT, typename AT, int NT, int IPT>
-__global__ void __launch_bounds__(NT, 5) k_batch_spmv(const BatchTable* __restrict__ Tp) {
+__global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const BatchTable* __restrict__ Tp) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
     constexpr int NS = kBatchStages;
