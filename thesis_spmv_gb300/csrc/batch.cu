@@ -148,12 +148,13 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
         AT xv[IPT];
         gather_subtile<VT, XT, AT, IPT>(st, in, xv);
         const bool general = reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral;
+        double no_ss = 0.0;
         if (general)
             finish_subtile<MODE_POWER, true, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
-                                                              cval, hval);
+                                                              cval, hval, no_ss);
         else
             finish_subtile<MODE_POWER, false, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
-                                                               cval, hval);
+                                                               cval, hval, no_ss);
         if (lane == 0) {
             if (i + NS < n) {
                 fence_proxy_async();
@@ -194,8 +195,9 @@ __global__ void __launch_bounds__(256) k_batch_fixup(const BatchTable* __restric
         const int lo = (c - d.fix0) * kFixTiles;
         const int hi = min(d.nsub, lo + kFixTiles);
         const AT* car = static_cast<const AT*>(d.carries);
+        double no_ss = 0.0;
         fixup_pass<MODE_POWER, XT, AT>(d.row_start, d.subc, d.nor, d.nsub, out, car, e, lo + threadIdx.x, hi,
-                                       blockDim.x);
+                                       blockDim.x, no_ss);
     }
 }
 

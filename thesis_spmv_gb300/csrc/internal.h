@@ -93,12 +93,21 @@ cudaError_t launch_fix_runs_f64(int mode, const MliPlan& P, int k0, int k1, doub
                                 const double* nsq_in, cudaStream_t st);
 cudaError_t launch_fix_runs_f32(int mode, const MliPlan& P, int k0, int k1, float* y, const float* carries,
                                 const double* nsq_in, cudaStream_t st);
+// ||y||^2 of a power step inside its kernels: the MODE_POWER SpMV launched
+// with `npart` writes one share per CTA (spmv_grid of them), this fix-up over
+// all runs adds one per CTA after them and its last CTA writes the ordered
+// total to *nsq_out.  npart holds power_norm_parts(P, spmv_grid) doubles;
+// counter is zero between launches.
+int power_norm_parts(const MliPlan& P, int spmv_grid);
+cudaError_t launch_fix_runs_norm(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
+                                 double* npart, int spmv_grid, unsigned int* counter, double* nsq_out,
+                                 cudaStream_t st);
 cudaError_t launch_mli_colspan(const MliPlan& P, int* cbase, int* flag, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_col16(const MliPlan& P, const int* cbase, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st, int l1 = 0);
+                              cudaStream_t st, int l1 = 0, double* npart = nullptr);
 // Carries of the merge SpMV into y (MODE_POWER: times the rescale factor of
 // nsq_in).
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,

@@ -88,8 +88,8 @@ struct pwmgpu_matrix {
     size_t carries_cap = 0;
     double* partials = nullptr;  // spmv partials
     size_t partials_cap = 0;
-    double* fix_partials = nullptr;
-    size_t fix_cap = 0;
+    double* npart = nullptr;  // per-CTA shares of a power step's ||y||^2 (SpMV CTAs, then fix-up CTAs)
+    size_t npart_cap = 0;
     unsigned int* counter = nullptr;
     double* nsq = nullptr;
     size_t nsq_cap = 0;
@@ -191,7 +191,7 @@ struct pwmgpu_matrix {
         pipe.in = pipe.out = nullptr;
         pwmgpu::dfree(carries);
         pwmgpu::dfree(partials);
-        pwmgpu::dfree(fix_partials);
+        pwmgpu::dfree(npart);
         pwmgpu::dfree(counter);
         pwmgpu::dfree(nsq);
         pwmgpu::dfree(small);
@@ -203,7 +203,7 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(dy);
         pwmgpu::dfree(fx);
         pwmgpu::dfree(fy);
-        carries_cap = partials_cap = fix_cap = nsq_cap = vec_cap = fvec_cap = 0;
+        carries_cap = partials_cap = npart_cap = nsq_cap = vec_cap = fvec_cap = 0;
     }
 };
 

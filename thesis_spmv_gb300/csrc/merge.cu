@@ -181,6 +181,7 @@ struct MergeArgs {
     int* status;
     int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
     const uint16_t* colp16 = nullptr;  // C16 kernels: 16-bit column offsets (base in rec0.w)
+    double* npart = nullptr;  // MODE_POWER: per-CTA sums of the squares of the rows the CTA completes, or null
 };
 
 constexpr int kMliStages = 2;
@@ -191,9 +192,11 @@ constexpr int kMliStages = 2;
 // persistent kernel.  Returns false (warp-uniformly) after a timeout, once
 // this warp's copies in flight have landed or a short bound ran out.
 template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH, bool C16, bool CG = false>
+// MODE_POWER: ss += the squares of the rows the warp completes (as stored;
+// rows that a fix-up completes are left to the fix-up).
 __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
                                           XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
-                                          AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol) {
+                                          AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol, double& ss) {
     using S = WarpStage<VT, IPT, C16>;
     constexpr int NS = kMliStages;
     constexpr int W = NT / 32;
@@ -221,12 +224,13 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit on a timeout
         AT xv[IPT];
         gather_subtile<VT, XT, AT, IPT, XCOH, C16, CG>(st, x, xv);
+        constexpr bool NORM = MODE == MODE_POWER;
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
-            finish_subtile<MODE, true, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
-                                                             cval, hval);
+            finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
+                                                                   crow, cval, hval, ss);
         else
-            finish_subtile<MODE, false, VT, XT, AT, IPT, C16>(s, st, xv, a.row_start, y, a.carries, a.nor, e, crow,
-                                                              cval, hval);
+            finish_subtile<MODE, false, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
+                                                                    crow, cval, hval, ss);
         // every lane is done with this stage (finish_subtile ends with a warp
         // barrier): refill it with the warp's sub-tile i + NS
         if (lane == 0 && i + NS < n) {
@@ -278,9 +282,17 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     uint32_t ticket = 0;
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
+    double ss = 0.0;
     warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16, CG>(a, a.x, a.y, stages, bars[w], crow + 32 * w,
                                                          cval + 32 * w, hval + 32 * w, ticket, e,
-                                                         policy_evict_first());
+                                                         policy_evict_first(), ss);
+    if (MODE == MODE_POWER && a.npart) {
+        // this CTA's share of ||y||^2 (k_fix_runs adds the fixed-up rows and
+        // sums the shares in a fixed order)
+        __shared__ double red[NT / 32];
+        const double t = block_sum<NT>(ss, red);
+        if (threadIdx.x == 0) a.npart[blockIdx.x] = t;
+    }
 }
 
 template <typename XT, typename AT>
@@ -300,7 +312,8 @@ __global__ void __launch_bounds__(256) k_merge_fixup(FixArgs<XT, AT> a) {
     const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
     const int t0 = a.t_lo + blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     const int t_end = a.t_hi < 0 ? a.num_tiles : a.t_hi;
-    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, t_end, stride);
+    double no_ss = 0.0;
+    fixup_pass<MODE, XT, AT>(a.row_start, a.tiles, a.nor, a.num_tiles, a.y, a.carries, e, t0, t_end, stride, no_ss);
 }
 
 // Fix-up runs, found once per matrix: sub-tile t starts a run when it leaves
@@ -329,21 +342,55 @@ __global__ void k_run_compact(const int* __restrict__ pre, const int4* __restric
         if (pre[t + 1] != pre[t]) runs[pre[t]] = desc[t];
 }
 
+// ||y||^2 of a power step, summed inside its SpMV and fix-up kernels:
+// npart[0, nspmv) hold the SpMV CTAs' shares; the fix-up CTAs add theirs
+// after them and the last fix-up CTA sums all shares in order into *nsq_out.
+struct FixNorm {
+    double* npart = nullptr;  // null: no norm
+    int nspmv = 0;
+    unsigned int* counter = nullptr;  // zero between launches
+    double* nsq_out = nullptr;
+};
+
 // One thread per run: y[r] += (carries[t] + ... + carries[n-1]) -- the sums of
 // fixup_pass in the same order, without its search (one descriptor load, then
 // the carries and y[r] together).
 template <int MODE, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_fix_runs(const int4* __restrict__ runs, int k0, int k1, XT* __restrict__ y,
-                                                  const AT* __restrict__ carries, const double* nsq_in) {
+                                                  const AT* __restrict__ carries, const double* nsq_in, FixNorm nrm) {
     const int kk = k0 + blockIdx.x * blockDim.x + threadIdx.x;
     const int4 d0 = kk < k1 ? runs[kk] : make_int4(0, 0, 0, 0);  // plan data: before the wait
     pdl_wait();  // carries and y come from the SpMV before on the stream
     const int e = (MODE == MODE_POWER && nsq_in) ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
+    double ss = 0.0;
     for (int k = kk; k < k1; k += gridDim.x * blockDim.x) {
         const int4 d = k == kk ? d0 : runs[k];
         AT sum = __ldcg(carries + d.x);
         for (int j = d.x + 1; j < d.y; ++j) sum += __ldcg(carries + j);
-        y[d.z] = (XT)((AT)__ldcg(y + d.z) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+        const XT v = (XT)((AT)__ldcg(y + d.z) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+        y[d.z] = v;
+        if (MODE == MODE_POWER) ss = fma((double)v, (double)v, ss);
+    }
+    if (MODE != MODE_POWER || !nrm.npart) return;
+    __shared__ double red[8];
+    __shared__ bool am_last;
+    const double t = block_sum<256>(ss, red);
+    if (threadIdx.x == 0) {
+        nrm.npart[nrm.nspmv + blockIdx.x] = t;
+        __threadfence();
+        am_last = atomicAdd(nrm.counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (am_last && threadIdx.x < 32) {
+        __threadfence();
+        const int n = nrm.nspmv + (int)gridDim.x;
+        double s0 = 0.0;
+        for (int i = threadIdx.x; i < n; i += 32) s0 += __ldcg(nrm.npart + i);
+        for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        if (threadIdx.x == 0) {
+            *nrm.nsq_out = s0;
+            *nrm.counter = 0u;
+        }
     }
 }
 
@@ -453,15 +500,19 @@ __device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
 //                                     rescale, applied only when the norm
 //                                     leaves a wide window)
 //   carries of v_{k+1}               (fix-up pass)
-//   ||v_{k+1}||^2                    (row pass, deterministic)
-//   v_k . v_{k+1} in the same row pass on the last iteration when `result`
-//   is set, then the Rayleigh quotient lambda_k = 2^{-e_k} v_k.v_{k+1} /
+//   ||v_{k+1}||^2                    (squares in both passes; per-CTA shares
+//                                     summed in a fixed order)
+//   v_k . v_{k+1} and ||v_{k+1}||^2 in a row pass on the last iteration when
+//   `result` is set, then the Rayleigh quotient lambda_k = 2^{-e_k} v_k.v_{k+1} /
 //   ||v_k||^2 and the eigen-residual ||2^{-e_k} v_{k+1} - lambda_k v_k||^2
-// Vectors ping-pong: iteration k reads X when k is even, Y when odd.  Three
-// grid barriers per iteration (SpMV | fix-up | row pass | total).  Keeping
-// the squares out of the SpMV pass keeps its FP64 work at one FMA per
-// nonzero (GB300's FP64 pipe is 2 operations per clock per SM).  The
-// normalisation of
+// Vectors ping-pong: iteration k reads X when k is even, Y when odd.  Two
+// grid barriers per iteration (SpMV | fix-up | total): the squares of
+// ||v_{k+1}||^2 are taken where the rows are stored -- the SpMV pass squares
+// the rows it completes from its coalesced row buffer (about one FP64 FMA
+// per 32 rows per warp instruction, beside one per nonzero: GB300's FP64
+// pipe is 2 operations per clock per SM), the fix-up pass the rows it
+// completes; the last iteration of a chunk with a result adds a row pass
+// (and a barrier) for v_k . v_{k+1}.  The normalisation of
 // the reference (y /= ||y||, Util/VectorUtill.hpp:34-41) is carried by the
 // exponent and applied once at the end (k_power_finalize).  All reductions
 // are FP64 and in a fixed order, whatever the vector type.
@@ -535,14 +586,18 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
         e = k > 0 ? pow2_rescale_exponent(nsq_cur, rescale_window<XT>()) : 0;
         nsq_last = nsq_cur;
         const bool want_dot = p.result && k == p.k0 + p.nk - 1;
-        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
-                                                              cval + 32 * w, hval + 32 * w, ticket, e, pol);
-        if (!grid_sync(p.barrier, a.status)) return;
-        fixup_pass<MODE_POWER, XT, AT>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub, nthr);
-        if (!grid_sync(p.barrier, a.status)) return;
         double ss = 0.0, dd = 0.0;
-        if (want_dot) norm_rows<XT, true>(out, in, 0, a.nor, tid, nthr, ss, dd);
-        else norm_rows<XT, false>(out, in, 0, a.nor, tid, nthr, ss, dd);
+        warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
+                                                              cval + 32 * w, hval + 32 * w, ticket, e, pol, ss);
+        if (!grid_sync(p.barrier, a.status)) return;
+        fixup_pass<MODE_POWER, XT, AT, true>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
+                                             nthr, ss);
+        if (want_dot) {
+            // the Rayleigh dot needs v_k: a row pass for both sums
+            if (!grid_sync(p.barrier, a.status)) return;
+            ss = 0.0;
+            norm_rows<XT, true>(out, in, 0, a.nor, tid, nthr, ss, dd);
+        }
         const double t_ss = block_sum<NT>(ss, red);
         const double t_dd = block_sum<NT>(dd, red);
         if (threadIdx.x == 0) {
@@ -905,12 +960,13 @@ struct MergeKernels {
 
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                            cudaStream_t st, int v, int tile0 = 0, int nsub = -1, bool pdl = true) {
+                            cudaStream_t st, int v, int tile0 = 0, int nsub = -1, bool pdl = true,
+                            double* npart = nullptr) {
         if (!P.colp16) v &= ~2;
         geom(v);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
                                 nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
-                                tile0, P.colp16};
+                                tile0, P.colp16, npart};
         const bool cg = (v >> 2) & 1;
         switch (v & 3) {
             case 1: launch_spmv_cg<1, false>(cg, mode, a, grid, st, pdl); break;
@@ -1031,12 +1087,15 @@ cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, in
 
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st, int l1) {
+                              cudaStream_t st, int l1, double* npart) {
     if (P.nsub == 0) return cudaSuccess;
     switch (cfg) {
-        case kCfgF32: return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
-        case kCfgBF16: return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
-        default: return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1);
+        case kCfgF32:
+            return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
+        case kCfgBF16:
+            return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
+        default:
+            return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
     }
 }
 
@@ -1199,10 +1258,10 @@ int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, 
 
 template <typename XT, typename AT>
 static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT* y, const AT* carries,
-                                 const double* nsq_in, cudaStream_t st) {
-    if (k1 <= k0) return cudaSuccess;
+                                 const double* nsq_in, cudaStream_t st, const FixNorm& nrm = FixNorm{}) {
+    if (k1 <= k0 && !nrm.npart) return cudaSuccess;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((k1 - k0 + 255) / 256);
+    cfg.gridDim = dim3(k1 > k0 ? (k1 - k0 + 255) / 256 : 1);  // the norm's last CTA runs even without runs
     cfg.blockDim = dim3(256);
     cfg.stream = st;
     cudaLaunchAttribute attr{};
@@ -1211,8 +1270,10 @@ static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT*
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
     const int4* runs = P.runs;
-    if (mode == MODE_POWER) cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_POWER, XT, AT>, runs, k0, k1, y, carries, nsq_in);
-    else cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_SPMV, XT, AT>, runs, k0, k1, y, carries, nsq_in);
+    if (mode == MODE_POWER)
+        cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_POWER, XT, AT>, runs, k0, k1, y, carries, nsq_in, nrm);
+    else
+        cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_SPMV, XT, AT>, runs, k0, k1, y, carries, nsq_in, FixNorm{});
     return cudaGetLastError();
 }
 
@@ -1224,6 +1285,25 @@ cudaError_t launch_fix_runs_f64(int mode, const MliPlan& P, int k0, int k1, doub
 cudaError_t launch_fix_runs_f32(int mode, const MliPlan& P, int k0, int k1, float* y, const float* carries,
                                 const double* nsq_in, cudaStream_t st) {
     return fix_runs_impl<float, float>(mode, P, k0, k1, y, carries, nsq_in, st);
+}
+
+int power_norm_parts(const MliPlan& P, int spmv_grid) {
+    return spmv_grid + (P.nruns > 0 ? (P.nruns + 255) / 256 : 1);
+}
+
+cudaError_t launch_fix_runs_norm(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
+                                 double* npart, int spmv_grid, unsigned int* counter, double* nsq_out,
+                                 cudaStream_t st) {
+    FixNorm nrm;
+    nrm.npart = npart;
+    nrm.nspmv = spmv_grid;
+    nrm.counter = counter;
+    nrm.nsq_out = nsq_out;
+    if (f32)
+        return fix_runs_impl<float, float>(MODE_POWER, P, 0, P.nruns, (float*)y, (const float*)carries, nsq_in, st,
+                                           nrm);
+    return fix_runs_impl<double, double>(MODE_POWER, P, 0, P.nruns, (double*)y, (const double*)carries, nsq_in, st,
+                                         nrm);
 }
 
 int fixup_grid(int num_tiles, int sm_count) {

@@ -269,7 +269,11 @@ int build_plan(pwmgpu_matrix* m) {
     TRY(ensure_cap(&m->carries, &m->carries_cap, (size_t)m->num_tiles + 1));
     TRY(ensure_cap(&m->partials, &m->partials_cap,
                    (size_t)std::max(std::max(m->grid, 2 * pmax), 2 * dot_grid(m->M.nor, m->sm_count)) + 64));
-    TRY(ensure_cap(&m->fix_partials, &m->fix_cap, (size_t)m->fix_grid + 64));
+    // shares of a power step's ||y||^2: at most one per SpMV CTA (16 resident
+    // CTAs per SM at most, 4 warps per CTA) and one per fix-up CTA
+    TRY(ensure_cap(&m->npart, &m->npart_cap,
+                   (size_t)power_norm_parts(m->P, (int)std::min<long long>(((long long)m->num_tiles + 3) / 4,
+                                                                           16LL * m->sm_count)) + 64));
     CU(cudaStreamSynchronize(m->stream));
     m->loaded = true;
     return tune(m);
@@ -350,9 +354,24 @@ int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
     return PWMGPU_OK;
 }
 
+// ||y||^2 of a power step taken inside its SpMV and fix-up kernels (needs the
+// fix-up run descriptors and room for the shares of a `grid`-CTA SpMV).
+bool norm_in_step(const pwmgpu_matrix* m, int grid) {
+    return m->P.runs && m->npart && (size_t)power_norm_parts(m->P, grid) <= m->npart_cap;
+}
+
 // One power-method step on device vectors: out = 2^e(nsq_in) * A in (SpMV +
-// fix-up), then nsq_out = ||out||^2 (row pass, deterministic).
+// fix-up), and nsq_out = ||out||^2 (deterministic): summed by the two kernels
+// from the rows they store, or a row pass where the plan has no run
+// descriptors.
 int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
+    if (norm_in_step(m, m->grid)) {
+        CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
+                             m->status, m->stream, m->l1, m->npart));
+        CU(launch_fix_runs_norm(false, m->P, out, m->carries, nsq_in, m->npart, m->grid, m->counter + 1, nsq_out,
+                                m->stream));
+        return PWMGPU_OK;
+    }
     CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
                          m->status, m->stream, m->l1));
     if (m->P.runs)
@@ -498,6 +517,13 @@ int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X,
             void* out = (k & 1) ? X : Y;
             const double* nsq_in = k > 0 ? m->nsq + k : nullptr;
             const bool last = k == k0 + nk - 1;
+            if (!last && norm_in_step(m, grid)) {
+                CU(launch_merge_spmv(cfg, kModePower, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
+                                     m->stream, m->l1, m->npart));
+                CU(launch_fix_runs_norm(f32, m->P, out, m->carries, nsq_in, m->npart, grid, m->counter + 1,
+                                        m->nsq + k + 1, m->stream));
+                continue;
+            }
             CU(launch_merge_spmv(cfg, kModePower, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
                                  m->stream, m->l1));
             if (f32) {
