@@ -19,6 +19,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "batch.h"
 #include "internal.h"
 #include "merge.cuh"
@@ -201,8 +203,74 @@ __global__ void __launch_bounds__(256) k_batch_fixup(const BatchTable* __restric
     }
 }
 
+// Sum of squares of y[lo, hi) (and, with DOT, sum of x y) by the CTA's
+// threads: 16-byte vector loads (lo is a multiple of 4 rows; vectors start
+// 16-byte aligned), U vectors per thread in flight, one accumulator per
+// vector slot combined in a fixed order, then the scalar tail.
+template <typename XT, bool DOT>
+__device__ __forceinline__ void chunk_sums(const XT* __restrict__ y, const XT* __restrict__ x, int lo, int hi,
+                                           double& ss, double& dd) {
+    using VecT = typename std::conditional<sizeof(XT) == 4, float4, double2>::type;
+    constexpr int V = 16 / (int)sizeof(XT);
+    constexpr int U = 4;
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int nv = (hi - lo) / V;
+    const VecT* yv = reinterpret_cast<const VecT*>(y + lo);
+    const VecT* xv = reinterpret_cast<const VecT*>(x + lo);
+    double s[U] = {}, d[U] = {};
+    for (int b = t; b < nv; b += U * nt) {
+        VecT a[U], c[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (b + u * nt < nv) {
+                a[u] = __ldcg(yv + b + u * nt);
+                if (DOT) c[u] = __ldcg(xv + b + u * nt);
+            } else {
+                a[u] = VecT{};
+                c[u] = VecT{};
+            }
+        }
+        // FP32 vectors: widened on the integer pipes unless a lane of the
+        // warp holds a subnormal, infinity or NaN (rare: then the conversion
+        // instruction, warp-uniformly)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const XT* av = reinterpret_cast<const XT*>(&a[u]);
+            const XT* cv = reinterpret_cast<const XT*>(&c[u]);
+            bool special = false;
+            if (sizeof(XT) == 4) {
+#pragma unroll
+                for (int k = 0; k < V; ++k) special |= widen_special((float)av[k]) || (DOT && widen_special((float)cv[k]));
+            }
+            if (sizeof(XT) == 8 || __any_sync(__activemask(), special)) {
+#pragma unroll
+                for (int k = 0; k < V; ++k) {
+                    const double w = (double)av[k];
+                    s[u] = fma(w, w, s[u]);
+                    if (DOT) d[u] = fma((double)cv[k], w, d[u]);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < V; ++k) {
+                    const double w = widen_normal((float)av[k]);
+                    s[u] = fma(w, w, s[u]);
+                    if (DOT) d[u] = fma(widen_normal((float)cv[k]), w, d[u]);
+                }
+            }
+        }
+    }
+    double sr = 0.0, dr = 0.0;
+    for (int r = lo + nv * V + t; r < hi; r += nt) {
+        const double w = (double)__ldcg(y + r);
+        sr = fma(w, w, sr);
+        if (DOT) dr = fma((double)__ldcg(x + r), w, dr);
+    }
+    ss += ((s[0] + s[1]) + (s[2] + s[3])) + sr;
+    if (DOT) dd += ((d[0] + d[1]) + (d[2] + d[3])) + dr;
+}
+
 template <typename XT>
-__global__ void __launch_bounds__(256) k_batch_norm(const BatchTable* __restrict__ Tp, int want_dot) {
+__global__ void __launch_bounds__(256, 3) k_batch_norm(const BatchTable* __restrict__ Tp, int want_dot) {
     __shared__ double red[32];
     __shared__ int last;
     const BatchTable T = *Tp;
@@ -216,8 +284,8 @@ __global__ void __launch_bounds__(256) k_batch_norm(const BatchTable* __restrict
         const int lo = (c - d.row0) * kRowChunk;
         const int hi = min(d.nor, lo + kRowChunk);
         double sq = 0.0, dd = 0.0;
-        if (want_dot) norm_rows<XT, true>(out, in, lo, hi, threadIdx.x, blockDim.x, sq, dd);
-        else norm_rows<XT, false>(out, in, lo, hi, threadIdx.x, blockDim.x, sq, dd);
+        if (want_dot) chunk_sums<XT, true>(out, in, lo, hi, sq, dd);
+        else chunk_sums<XT, false>(out, in, lo, hi, sq, dd);
         sq = block_sum<256>(sq, red);
         if (want_dot) dd = block_sum<256>(dd, red);
         if (threadIdx.x == 0) {
@@ -262,14 +330,31 @@ __global__ void __launch_bounds__(256) k_batch_resid(const BatchTable* __restric
         const int kit = stt->k;  // >= 2 after a round
         const double nsq_prev = stt->nsq_prev;
         const int e = kit - 1 > 0 ? pow2_rescale_exponent(nsq_prev, rescale_window<XT>()) : 0;
-        const double lam = scale_pow2(stt->dot, -e) / nsq_prev;
+        const double dot = scale_pow2(stt->dot, -e);
+        const double lam = dot / nsq_prev;
+        // ||2^-e v_k - lam v_{k-1}||^2 = 2^-2e ||v_k||^2 - lam 2^-e (v_{k-1} . v_k)
+        // from the round's sums (no pass over the rows): exact in exact
+        // arithmetic, and in FP64 good to a few digits while the relative
+        // residual is far above the sums' rounding (~1e-7); so it stands in
+        // for the row pass while the relative residual is above 1e-3 -- no
+        // stopping or phase rule looks at residuals that large -- unless the
+        // host asked for the pass (a solve's last round).  The choice depends
+        // only on the solve's own state, so it is the same in any mix.
+        const double est = fma(-lam, dot, scale_pow2(stt->nsq, -2 * e));
+        if (!stt->exact_res && est >= 1e-6 * nsq_prev * lam * lam) {
+            if (threadIdx.x == 0) {  // every chunk of the solve writes the same values
+                stt->lambda = lam;
+                stt->res2 = est;
+            }
+            continue;
+        }
         const XT* cur = static_cast<const XT*>((kit & 1) ? d.Y : d.X);
         const XT* prev = static_cast<const XT*>((kit & 1) ? d.X : d.Y);
         const int lo = (c - d.row0) * kRowChunk;
         const int hi = min(d.nor, lo + kRowChunk);
         double rr = 0.0;
         for (int r = lo + threadIdx.x; r < hi; r += blockDim.x) {
-            const double dl = scale_pow2((double)cur[r], -e) - lam * (double)prev[r];
+            const double dl = scale_pow2((double)__ldcg(cur + r), -e) - lam * (double)__ldcg(prev + r);
             rr = fma(dl, dl, rr);
         }
         rr = block_sum<256>(rr, red);
@@ -325,7 +410,7 @@ struct BatchKernels {
     static cudaError_t step(const BatchTable* T, int want_dot, int sm_count, cudaStream_t st) {
         k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid(sm_count), kBatchNT, SMEM, st>>>(T);
         k_batch_fixup<XT, AT><<<8 * sm_count, 256, 0, st>>>(T);
-        k_batch_norm<XT><<<4 * sm_count, 256, 0, st>>>(T, want_dot);
+        k_batch_norm<XT><<<3 * sm_count, 256, 0, st>>>(T, want_dot);
         return cudaGetLastError();
     }
 };
@@ -349,8 +434,8 @@ cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_c
         }
         if (e != cudaSuccess) return e;
     }
-    if (cfg == kCfgF64) k_batch_resid<double><<<2 * sm_count, 256, 0, st>>>(T);
-    else k_batch_resid<float><<<2 * sm_count, 256, 0, st>>>(T);
+    if (cfg == kCfgF64) k_batch_resid<double><<<4 * sm_count, 256, 0, st>>>(T);
+    else k_batch_resid<float><<<4 * sm_count, 256, 0, st>>>(T);
     return cudaGetLastError();
 }
 

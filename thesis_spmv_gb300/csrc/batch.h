@@ -16,7 +16,7 @@
 namespace pwmgpu {
 
 constexpr int kFixTiles = 256;    // sub-tiles per fix-up chunk (one per thread: a fix-up is latency-bound)
-constexpr int kRowChunk = 32768;  // rows per norm / residual chunk
+constexpr int kRowChunk = 16384;  // rows per norm / residual chunk (a multiple of 4)
 
 struct BatchSlot {
     const int32_t* row_start;
@@ -39,7 +39,7 @@ struct BatchSlot {
 // Per-solve iteration state, advanced on the device.
 struct SlotState {
     int k;              // steps done in the current phase: v_k is the newest iterate
-    int pad0;
+    int exact_res;      // set by the host: the round's residual pass must run over the rows
     double nsq;         // ||v_k||^2 (k >= 1)
     double nsq_prev;    // ||v_{k-1}||^2
     double dot;         // v_{k-1} . v_k, from the last step of a round

@@ -180,6 +180,24 @@ template <> __device__ __forceinline__ double to_f64<double>(double v) { return 
 template <> __device__ __forceinline__ double to_f64<float>(float v) { return (double)v; }
 template <> __device__ __forceinline__ double to_f64<__nv_bfloat16>(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
 
+// FP32 -> FP64 widening on the integer pipes: for a normal float the IEEE-754
+// fields move over (exponent rebiased by 1023 - 127 = 896, mantissa to the top
+// of the 52-bit field), a zero keeps its sign.  Subnormals, infinities and
+// NaNs (widen_special) are left to the conversion instruction.  On GB300 the
+// FP64 pipe runs 2 operations per clock per SM, so row passes over FP32
+// vectors keep it for their FMAs.
+__device__ __forceinline__ bool widen_special(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    return ex == 0xFFu || (ex == 0u && (u & 0x7FFFFFu) != 0u);
+}
+__device__ __forceinline__ double widen_normal(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    const unsigned hi = (u & 0x80000000u) | (ex != 0u ? (ex + 896u) << 20 : 0u) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 template <typename T> __device__ __forceinline__ float to_f32(T v);
 template <> __device__ __forceinline__ float to_f32<double>(double v) { return (float)v; }
 template <> __device__ __forceinline__ float to_f32<float>(float v) { return v; }

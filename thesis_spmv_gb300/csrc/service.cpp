@@ -52,6 +52,7 @@ struct Req {
     const void* valp_low = nullptr;
     int iterations = 0, iterations_low = 0, rounds_in_phase = 0, converged = 0;
     double prev_rel = 1.0, rel = INFINITY, lambda = 0.0;
+    bool exact_set = false;  // the state asks for the residual's row pass
     std::vector<double> u;
 };
 
@@ -376,6 +377,7 @@ int after_round(pwmsvc* S, int* finished) {
                 float* newest = (st.k & 1) ? m->fy : m->fx;
                 CU(launch_convert_f32_f64(newest, m->dx, r->n, m->sm_count, S->stream));
                 TRY(reset_state(S, r->slot));
+                r->exact_set = false;
                 r->low = false;
                 r->cls = kClsF64;
                 r->rounds_in_phase = 0;
@@ -551,6 +553,18 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
     }
     if (!s->live.empty()) {
         if (s->dirty) TRY(rebuild_tables(s));
+        // a solve's last possible round reports its residual from the row
+        // pass (earlier rounds may take it from the round's sums while it is
+        // large)
+        for (Req* r : s->live) {
+            const bool result_phase = !r->low || r->spec.precision == PWMGPU_PREC_F32;
+            if (result_phase && !r->exact_set && r->iterations + s->cfg.round_iterations >= r->spec.max_it) {
+                static const int one = 1;
+                CU(cudaMemcpyAsync(&s->d_states[r->slot].exact_res, &one, sizeof(int), cudaMemcpyHostToDevice,
+                                   s->stream));
+                r->exact_set = true;
+            }
+        }
         TRY(run_round(s));
         CU(cudaMemcpyAsync(s->h_states, s->d_states, sizeof(SlotState) * (size_t)s->cfg.max_live,
                            cudaMemcpyDeviceToHost, s->stream));
