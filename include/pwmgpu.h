@@ -161,6 +161,21 @@ int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
 #define PWMGPU_POWER_MULTI 2
 int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
 
+/* Storage the FP32 / BF16 iterations (pwmgpu_solve's low-precision phase,
+ * pwmgpu_mv_device_f32) stream (not in the reference).  AUTO (default): a
+ * SELL-32 copy (slices of 32 rows, one row per lane, 16-bit column offsets;
+ * built on first use) for matrices whose columns all lie within 32768 rows
+ * of their row's slice and whose padding is within a quarter of the
+ * nonzeros -- stencils and banded matrices -- the merge-path layout
+ * otherwise; MERGE: always the merge-path layout.  The SELL kernel sums each
+ * row left to right in CRS order; results differ from the merge layout's
+ * only by rounding (within the FP32 row bound either way).  The power modes
+ * above apply to the merge layout; POWER_FUSED keeps the low-precision
+ * iterations on it too. */
+#define PWMGPU_LOWFMT_AUTO 0
+#define PWMGPU_LOWFMT_MERGE 1
+int pwmgpu_set_low_format(pwmgpu_matrix* m, int fmt);
+
 /* Power solve with an eigenvalue estimate, the eigen-residual and a stopping
  * test (not in the reference: the benchmark spec extension).  x (host, length nor)
  * holds the start vector on entry and the normalised eigenvector estimate on

@@ -180,6 +180,7 @@ def test_solve_modes_agree_on_a_large_poisson_grid(pwm):
     g = 600
     M = pwm.CRSCuda(1)
     M.generatePoissonMatrix(g, g, 1)
+    M.set_low_format(pwm.LOWFMT_MERGE)  # both modes on the merge layout (the SELL layout is another SpMV)
     x0 = np.random.default_rng(4).random(g * g)
     lam = {}
     for mode in POWER_MODES:

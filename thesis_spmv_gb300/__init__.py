@@ -5,6 +5,6 @@ A from-scratch GPU implementation of the hot path of KobeBergmans/Thesis_SPMV
 reference's pwm::SparseMatrix interface.  The compute lives in
 libpwmgpu.so (C ABI: include/pwmgpu.h); this package is its Python front end.
 """
-from ._lib import (POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32, PREC_F64, PREC_MIXED,  # noqa: F401
+from ._lib import (LOWFMT_AUTO, LOWFMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32, PREC_F64, PREC_MIXED,  # noqa: F401
                    PwmGpuError, lib, lib_path)
 from .matrix import COHCuda, CRSCuda, CSBCuda, CudaSparseMatrix, Triplet, selectType  # noqa: F401

@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ER
 FMT_MERGE, FMT_CSB, FMT_COH = 0, 1, 2
 PREC_F64, PREC_F32, PREC_MIXED = 0, 1, 2
 POWER_AUTO, POWER_FUSED, POWER_MULTI = 0, 1, 2
+LOWFMT_AUTO, LOWFMT_MERGE = 0, 1
 RAND_LOGNORMAL, RAND_POISSON = 0, 1
 
 
@@ -65,6 +66,7 @@ SIGNATURES = {
     "pwmgpu_power": (C.c_int, [vp, vp, vp, i32]),
     "pwmgpu_power_device": (C.c_int, [vp, vp, vp, i32]),
     "pwmgpu_set_power_mode": (C.c_int, [vp, C.c_int]),
+    "pwmgpu_set_low_format": (C.c_int, [vp, C.c_int]),
     "pwmgpu_solve": (C.c_int, [vp, vp, i32, C.c_double, C.c_int, C.POINTER(SolveInfo)]),
     "pwmgpu_merge_partition": (C.c_int, [vp, i32, vp]),
     "pwmgpu_tile_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),

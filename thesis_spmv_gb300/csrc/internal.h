@@ -55,6 +55,33 @@ struct MliPlan {
 };
 long long mli_storage_elems(long long nnz, long long nsub);
 
+// sell.cu: SELL-32 copy of a matrix for the FP32 / BF16 iterations (slices
+// of 32 rows, column-major in the slice, 16-bit column offsets from
+// 32 s - 32768, padding skipped); built when every column fits and the
+// padding is within a quarter of the nonzeros.
+struct SellPlan {
+    int state = 0;  // 0: not built, 1: built, -1: the matrix does not fit the format
+    int nslices = 0;
+    long long stored = 0;        // padded elements
+    int32_t* soff = nullptr;     // nslices + 1 element offsets
+    uint16_t* col16 = nullptr;   // column - (32 s - 32768)
+    float* val32 = nullptr;      // FP32 values (built on first use)
+    void* valbf = nullptr;       // BF16 values (built on first use)
+    double* npart = nullptr;     // per-CTA shares of ||y||^2
+    void release();
+};
+int sell_grid(int nslices, int sm_count);
+// Build the slices (first call) and the value array of the requested type
+// from CRS arrays; 0 = built, 1 = the matrix does not fit (state -1), 2 = a
+// CUDA error or no memory (state 0).
+int sell_build(SellPlan& S, const int32_t* row_start, const int32_t* col, const double* val, int nor, long long nnz,
+               bool bf16, int sm_count, cudaStream_t st);
+// y = 2^e A x (e from nsq_in, or 0 when null) on FP32 vectors; with nsq_out,
+// also *nsq_out = ||y||^2 (deterministic; counter zero between launches).
+cudaError_t launch_sell_spmv(const SellPlan& S, bool bf16, const int32_t* row_start, int nor, const float* x, float* y,
+                             const double* nsq_in, double* nsq_out, unsigned int* counter, int sm_count,
+                             cudaStream_t st);
+
 // l1: launch variant of the merge kernels.  Bit 0: 0 = most resident CTAs,
 // 1 = a smaller shared-memory carveout, more L1 for irregular gathers; bit 1:
 // stream the plan's 16-bit column offsets (set only when the plan has them);

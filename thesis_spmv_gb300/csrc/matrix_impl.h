@@ -82,6 +82,10 @@ struct pwmgpu_matrix {
     float* val32 = nullptr;
     void* valbf = nullptr;
     int bf16_exact = -1;
+    // SELL-32 copy for the FP32 / BF16 iterations (lazy), and whether they
+    // may use it (PWMGPU_LOWFMT_*)
+    pwmgpu::SellPlan sell;
+    int low_format = PWMGPU_LOWFMT_AUTO;
 
     // scratch
     double* carries = nullptr;  // max(num_tiles, num_tiles32) doubles (also used as floats)
@@ -174,6 +178,7 @@ struct pwmgpu_matrix {
         if (valbf) cudaFree(valbf);
         valbf = nullptr;
         bf16_exact = -1;
+        sell.release();
         M = DevMatrix();
         num_tiles = 0;
         loaded = false;
@@ -218,5 +223,6 @@ int ensure_vectors(pwmgpu_matrix* m);
 int ensure_fvectors(pwmgpu_matrix* m);
 int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** valp, int* pgrid);
 bool low_precision_floor(double rel, double prev_rel);
+bool sell_for(pwmgpu_matrix* m, int cfg);
 
 }  // namespace pwmgpu

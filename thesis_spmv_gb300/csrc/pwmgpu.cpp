@@ -473,6 +473,38 @@ int ensure_low_values(pwmgpu_matrix* m, bool allow_bf16, int* cfg, const void** 
     *pgrid = m->pgrid32;
     return PWMGPU_OK;
 }
+
+// The SELL-32 copy with values of configuration cfg (FP32 or BF16), built on
+// first use from the CRS order of the merge plan; false where the matrix does
+// not fit the format, the handle asks for the merge layout, or the iterations
+// run in the persistent merge kernel.
+bool sell_for(pwmgpu_matrix* m, int cfg) {
+    if (cfg == kCfgF64 || m->low_format != PWMGPU_LOWFMT_AUTO || m->power_mode == PWMGPU_POWER_FUSED) return false;
+    SellPlan& S = m->sell;
+    const bool bf = cfg == kCfgBF16;
+    if (S.state < 0) return false;
+    if (S.state == 1 && (bf ? S.valbf != nullptr : S.val32 != nullptr)) return true;
+    const long long nnz = m->M.nnz;
+    int32_t* tcol = nullptr;
+    double* tval = nullptr;
+    const int32_t* col = m->M.col;
+    const double* val = m->M.val;
+    int rc = 2;
+    if (!col || !val) {
+        // the merge format keeps only its lane-interleaved copy: CRS order back
+        if (dalloc(&tcol, (size_t)nnz + 1) == PWMGPU_OK && dalloc(&tval, (size_t)nnz + 1) == PWMGPU_OK &&
+            launch_mli_unpermute(m->P, tcol, tval, m->sm_count, m->stream) == cudaSuccess) {
+            col = tcol;
+            val = tval;
+        }
+    }
+    if (col && val) rc = sell_build(S, m->M.row_start, col, val, m->M.nor, nnz, bf, m->sm_count, m->stream);
+    (void)cudaStreamSynchronize(m->stream);
+    dfree(tcol);
+    dfree(tval);
+    (void)cudaGetLastError();
+    return rc == 0;
+}
 }  // namespace pwmgpu
 namespace {
 
@@ -505,7 +537,25 @@ struct ChunkOut {
 // differs.
 int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X, void* Y, int k0, int nk,
                 ChunkOut* o) {
-    if (use_fused(m, pgrid)) {
+    if (sell_for(m, cfg)) {
+        // SELL-32: one kernel per step (no fix-up; ||y||^2 summed in it), the
+        // chunk's last step with the norm pass for the Rayleigh dot
+        const bool bf = cfg == kCfgBF16;
+        const int dg = dot_grid(m->M.nor, m->sm_count);
+        for (int k = k0; k < k0 + nk; ++k) {
+            const float* in = static_cast<const float*>((k & 1) ? Y : X);
+            float* out = static_cast<float*>((k & 1) ? X : Y);
+            const double* nsq_in = k > 0 ? m->nsq + k : nullptr;
+            const bool last = k == k0 + nk - 1;
+            CU(launch_sell_spmv(m->sell, bf, m->M.row_start, m->M.nor, in, out, nsq_in, last ? nullptr : m->nsq + k + 1,
+                                m->counter + 2, m->sm_count, m->stream));
+            if (last) {
+                CU(launch_power_norm_f32(out, in, m->M.nor, m->partials, m->counter, m->small + 6, dg, m->stream));
+                CU(launch_solve_result(true, in, out, m->M.nor, m->nsq + k, m->small + 6, m->nsq + k + 1, m->small,
+                                       m->partials, m->counter, dg, m->stream));
+            }
+        }
+    } else if (use_fused(m, pgrid)) {
         CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
                                    m->partials, m->barrier, m->status, m->stream, m->l1));
     } else {
@@ -1327,6 +1377,11 @@ int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     if (m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_UNSUPPORTED, "FP32 SpMV runs on the merge format");
     if (m->M.nor > 0 && (!dx || !dy)) return fail(PWMGPU_ERR_INVALID, "null vector");
     if (m->num_tiles == 0) return PWMGPU_OK;
+    if (sell_for(m, kCfgF32)) {
+        CU(launch_sell_spmv(m->sell, false, m->M.row_start, m->M.nor, dx, dy, nullptr, nullptr, m->counter + 2,
+                            m->sm_count, m->stream));
+        return PWMGPU_OK;
+    }
     int cfg = kCfgF32, pg = 0;
     const void* valp = nullptr;
     TRY(ensure_low_values(m, false, &cfg, &valp, &pg));
@@ -1338,6 +1393,14 @@ int pwmgpu_mv_device_f32(pwmgpu_matrix* m, const float* dx, float* dy) {
     else
         CU(launch_merge_fixup_f32(kModeSpmv, m->M, m->P.subc, m->num_tiles, dy, reinterpret_cast<float*>(m->carries),
                                   nullptr, m->fix_grid, m->stream));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_set_low_format(pwmgpu_matrix* m, int fmt) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (fmt != PWMGPU_LOWFMT_AUTO && fmt != PWMGPU_LOWFMT_MERGE)
+        return fail(PWMGPU_ERR_INVALID, "unknown low-precision format %d", fmt);
+    m->low_format = fmt;
     return PWMGPU_OK;
 }
 

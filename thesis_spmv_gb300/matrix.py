@@ -14,7 +14,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import (FMT_COH, FMT_CSB, FMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32,  # noqa: F401
+from ._lib import (FMT_COH, FMT_CSB, FMT_MERGE, LOWFMT_AUTO, LOWFMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32,  # noqa: F401
                    PREC_F64, PREC_MIXED, SolveInfo, check)
 
 _I32 = np.int32
@@ -229,6 +229,11 @@ class CudaSparseMatrix:
         """POWER_AUTO / POWER_FUSED (one persistent kernel) / POWER_MULTI
         (two kernels per iteration)."""
         check(_lib.lib().pwmgpu_set_power_mode(self._h, int(mode)), "set_power_mode")
+
+    def set_low_format(self, fmt):
+        """LOWFMT_AUTO (SELL-32 for the FP32 / BF16 iterations where the
+        matrix fits it) / LOWFMT_MERGE (always the merge-path layout)."""
+        check(_lib.lib().pwmgpu_set_low_format(self._h, int(fmt)), "set_low_format")
 
     def solve(self, x, max_it, tol, precision=PREC_F64):
         """Power solve to ||A u - lambda u|| / |lambda| <= tol (or max_it
