@@ -24,6 +24,7 @@
 #include "batch.h"
 #include "internal.h"
 #include "merge.cuh"
+#include "sell.cuh"
 
 namespace pwmgpu {
 
@@ -172,6 +173,71 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
             for (int t = i; t < n && t < i + NS; ++t)
                 mbar_wait_bounded(&bars[w][t % NS], (uint32_t)(t / NS) & 1u, T.status, kWaitCycles / 8, false);
         __syncwarp();
+    }
+}
+
+// ---- SELL-32 classes ------------------------------------------------------
+// What a warp needs of a slice's slot (FP32 vectors).
+struct SellSlotRegs {
+    const int32_t* soff;
+    const uint16_t* col16;
+    const void* valp;
+    const float* in;
+    float* out;
+    int nor, tile0, e;
+};
+
+__device__ __forceinline__ void load_sell_slot(const BatchTable& T, int j, SellSlotRegs& r) {
+    const BatchSlot* d = T.slots + j;
+    const SlotState* st = T.states + d->state;
+    const int k = st->k;
+    r.soff = d->soff;
+    r.col16 = d->col16;
+    r.valp = d->valp;
+    r.in = static_cast<const float*>((k & 1) ? d->Y : d->X);
+    r.out = static_cast<float*>((k & 1) ? d->X : d->Y);
+    r.nor = d->nor;
+    r.tile0 = d->tile0;
+    r.e = k > 0 ? pow2_rescale_exponent(st->nsq, rescale_window<float>()) : 0;
+}
+
+// One power step of every live solve of a SELL-32 class: v_{k+1} = 2^{e_k}
+// A_j v_k, one lane per row.  Warp w takes the consecutive global slices
+// [w K, w K + K) (K = slices / warps, rounded up), two at a time; slots own
+// consecutive slices, so the warp's slot advances by a comparison, not a
+// lookup.  Each row is one lane's sum in CRS order: the same bits in any mix.
+template <typename VT>
+__global__ void __launch_bounds__(256, 4) k_batch_sell(const BatchTable* __restrict__ Tp) {
+    const BatchTable T = *Tp;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, tw = (gridDim.x * blockDim.x) >> 5;
+    const int K = (T.ntiles + tw - 1) / tw;
+    int g = gw * K;
+    const int g1 = min(g + K, T.ntiles);
+    if (g >= g1) return;
+    int j = __ldg(T.tile_slot + g);
+    SellSlotRegs A;
+    load_sell_slot(T, j, A);
+    int end = A.tile0 + __ldg(&T.slots[j].nsub);
+    while (g < g1) {
+        while (g >= end) {  // the next slot (slots own consecutive slices)
+            ++j;
+            load_sell_slot(T, j, A);
+            end = A.tile0 + __ldg(&T.slots[j].nsub);
+        }
+        const bool two = g + 1 < g1 && g + 1 < end;
+        const int sa = g - A.tile0;
+        const int oa = __ldg(A.soff + sa), ob = __ldg(A.soff + sa + 1);
+        const int oc = two ? __ldg(A.soff + sa + 2) : ob;
+        const int wa = (ob - oa) >> 5, wb = (oc - ob) >> 5;
+        float ya, yb;
+        sell_rows2<VT, 6>(A.col16 + oa + lane, static_cast<const VT*>(A.valp) + oa + lane, A.in, sa * 32 - 32768,
+                          wa, A.col16 + ob + lane, static_cast<const VT*>(A.valp) + ob + lane, A.in,
+                          sa * 32 + 32 - 32768, wb, ya, yb);
+        const int ra = sa * 32 + lane, rb = ra + 32;
+        if (ra < A.nor) A.out[ra] = A.e ? scale_pow2(ya, A.e) : ya;
+        if (two && rb < A.nor) A.out[rb] = A.e ? scale_pow2(yb, A.e) : yb;
+        g += two ? 2 : 1;
     }
 }
 
@@ -417,16 +483,34 @@ struct BatchKernels {
 
 }  // namespace
 
+static int sell_batch_grid(int sm_count) {
+    static int occ = 0;
+    if (occ == 0) {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_batch_sell<float>, 256, 0) != cudaSuccess || o < 1) o = 1;
+        occ = o;
+    }
+    return occ * sm_count;
+}
+
 void batch_prepare(int sm_count) {
     BatchKernels<double, double, double>::grid(sm_count);
     BatchKernels<float, float, float>::grid(sm_count);
     BatchKernels<__nv_bfloat16, float, float>::grid(sm_count);
+    sell_batch_grid(sm_count);
 }
 
-cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st) {
+cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st, bool sell) {
     for (int it = 0; it < steps; ++it) {
         const int want_dot = it == steps - 1;
         cudaError_t e;
+        if (sell) {
+            if (cfg == kCfgBF16) k_batch_sell<__nv_bfloat16><<<sell_batch_grid(sm_count), 256, 0, st>>>(T);
+            else k_batch_sell<float><<<sell_batch_grid(sm_count), 256, 0, st>>>(T);
+            k_batch_norm<float><<<3 * sm_count, 256, 0, st>>>(T, want_dot);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            continue;
+        }
         switch (cfg) {
             case kCfgF32: e = BatchKernels<float, float, float>::step(T, want_dot, sm_count, st); break;
             case kCfgBF16: e = BatchKernels<__nv_bfloat16, float, float>::step(T, want_dot, sm_count, st); break;

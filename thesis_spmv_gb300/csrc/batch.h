@@ -2,7 +2,9 @@
 // loop's rounds).  Shared by batch.cu (kernels) and service.cpp (host).
 //
 // A class table lists the live solves ("slots") that iterate with one value
-// / vector type.  The sub-tiles of all its slots form one list: slot j owns
+// / vector type and one layout (merge path, or SELL-32 slices for the FP32 /
+// BF16 iterations of stencil and banded matrices: then "sub-tiles" below are
+// 32-row slices and there is no fix-up).  The sub-tiles of all its slots form one list: slot j owns
 // global sub-tiles [tile0_j, tile0_j + nsub_j), cut from its own merge path,
 // so the list is the merge path of the block-diagonal matrix of all slots,
 // cut at the matrix boundaries.  One launch runs an SpMV step of every slot;
@@ -28,6 +30,8 @@ struct BatchSlot {
     void* X;  // v_k for even k
     void* Y;  // v_k for odd k
     void* carries;
+    const int32_t* soff;    // SELL-32 classes: slice offsets (nsub = slices, tile0 = first global slice)
+    const uint16_t* col16;  // SELL-32 classes: 16-bit column offsets (values in valp)
     int nor, nsub;
     int tile0;       // first global sub-tile
     int fix0, nfix;  // fix-up chunks [fix0, fix0 + nfix) (kFixTiles sub-tiles each)

@@ -210,7 +210,9 @@ cudaError_t launch_host_copy(const double* src, double* dst, long long n, cudaSt
 // of a class table; seeded uniform start vectors
 struct BatchTable;
 void batch_prepare(int sm_count);
-cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st);
+// sell: the class's slots are SELL-32 copies (FP32 / BF16 values).
+cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st,
+                               bool sell = false);
 cudaError_t launch_tile_slots(const BatchTable* T, int nslots, cudaStream_t st);
 cudaError_t launch_fill_uniform(double* x, int n, uint64_t seed, int sm_count, cudaStream_t st);
 

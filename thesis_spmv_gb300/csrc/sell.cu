@@ -25,14 +25,13 @@
 
 #include "internal.h"
 #include "merge.cuh"
+#include "sell.cuh"
 
 namespace pwmgpu {
 
 namespace {
 
 constexpr int kSellNT = 256;  // threads per CTA
-constexpr int kSellJ = 8;     // elements per lane issued together
-constexpr uint16_t kSellPad = 0xFFFF;
 
 // soff[s + 1] = 32 * longest row of slice s (scanned afterwards); *total +=
 // the same in 64 bits (the padded size, checked before the 32-bit scan).
@@ -97,43 +96,6 @@ struct SellArgs {
     double* nsq_out;        // ... into *nsq_out
 };
 
-// Rows 32 s + lane of two slices at once (widths wa, wb; wb = 0 for none):
-// products in CRS order; the column and value loads of kSellJ elements of
-// both rows are issued together, then the x gathers, then the FMAs.
-template <typename VT>
-__device__ __forceinline__ void sell_rows2(const SellArgs<VT>& a, int oa, int wa, int cba, int ob, int wb, int cbb,
-                                           int lane, float& ya, float& yb) {
-    const uint16_t* cpa = a.col16 + oa + lane;
-    const uint16_t* cpb = a.col16 + ob + lane;
-    const VT* vpa = a.val + oa + lane;
-    const VT* vpb = a.val + ob + lane;
-    float acca = 0.0f, accb = 0.0f;
-    const int w = max(wa, wb);
-    for (int j = 0; j < w; j += kSellJ) {
-        uint16_t ca[kSellJ], cb[kSellJ];
-        float va[kSellJ], vb[kSellJ], xa[kSellJ], xb[kSellJ];
-#pragma unroll
-        for (int u = 0; u < kSellJ; ++u) {
-            ca[u] = j + u < wa ? __ldg(cpa + 32 * (j + u)) : kSellPad;
-            cb[u] = j + u < wb ? __ldg(cpb + 32 * (j + u)) : kSellPad;
-            va[u] = j + u < wa ? to_f32(__ldg(vpa + 32 * (j + u))) : 0.0f;
-            vb[u] = j + u < wb ? to_f32(__ldg(vpb + 32 * (j + u))) : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < kSellJ; ++u) {
-            xa[u] = ca[u] != kSellPad ? __ldg(a.x + cba + (int)ca[u]) : 0.0f;
-            xb[u] = cb[u] != kSellPad ? __ldg(a.x + cbb + (int)cb[u]) : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < kSellJ; ++u) {
-            if (ca[u] != kSellPad) acca = fmaf(va[u], xa[u], acca);
-            if (cb[u] != kSellPad) accb = fmaf(vb[u], xb[u], accb);
-        }
-    }
-    ya = acca;
-    yb = accb;
-}
-
 // y = 2^e A x, one lane per row; a warp takes slices s and s + (warps in the
 // grid) together, then moves on by twice that.  With npart, also ||y||^2
 // (FP64, widened on the integer pipes; deterministic for a fixed grid).
@@ -150,7 +112,8 @@ __global__ void __launch_bounds__(kSellNT) k_sell_spmv(SellArgs<VT> a) {
         const int oa = __ldg(a.soff + s), wa = (__ldg(a.soff + s + 1) - oa) >> 5;
         const int ob = two ? __ldg(a.soff + s2) : 0, wb = two ? (__ldg(a.soff + s2 + 1) - ob) >> 5 : 0;
         float ya, yb;
-        sell_rows2(a, oa, wa, s * 32 - 32768, ob, wb, s2 * 32 - 32768, lane, ya, yb);
+        sell_rows2(a.col16 + oa + lane, a.val + oa + lane, a.x, s * 32 - 32768, wa, a.col16 + ob + lane,
+                   a.val + ob + lane, a.x, s2 * 32 - 32768, wb, ya, yb);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int r = (h ? s2 : s) * 32 + lane;

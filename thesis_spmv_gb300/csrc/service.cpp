@@ -29,7 +29,10 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-enum { kClsF64 = 0, kClsF32 = 1, kClsBF16 = 2, kNumCls = 3 };
+// Precision classes; the FP32 / BF16 iterations of matrices that fit the
+// SELL-32 layout run in their own classes (kernel per layout).
+enum { kClsF64 = 0, kClsF32 = 1, kClsBF16 = 2, kClsF32Sell = 3, kClsBF16Sell = 4, kNumCls = 5 };
+constexpr int kSides = kNumCls - 1;  // forked streams of a round (the F64 class runs on the service stream)
 
 // Residual at which a mixed solve leaves the FP32 / BF16 phase (as in
 // pwmgpu_solve).
@@ -86,7 +89,9 @@ size_t solve_bytes(long long nor, long long nnz, int precision) {
     const long long nsub = (nor + nnz + 32 * kMliIpt - 1) / (32 * kMliIpt);
     const long long elems = nnz + 7 * nsub + 16;
     long long b = 4 * (nor + 1) + 12 * elems + nsub * (32 + 64 + 8 + 8) + 12 * nnz + 2 * 8 * (nor + 16) + 65536;
-    if (precision != PWMGPU_PREC_F64) b += 4 * elems + 2 * 4 * (nor + 16);
+    // FP32 values and vectors; a SELL-32 copy (at most 1.25 nnz elements of
+    // 2-byte columns and 4-byte values) where the matrix fits it
+    if (precision != PWMGPU_PREC_F64) b += 4 * elems + 2 * 4 * (nor + 16) + 8 * nnz;
     return (size_t)b;
 }
 
@@ -96,8 +101,8 @@ struct pwmsvc {
     pwmsvc_config cfg{};
     int device = 0, sm_count = 1;
     cudaStream_t stream = nullptr;
-    cudaStream_t side[2] = {nullptr, nullptr};
-    cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr}, ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t side[kSides] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[kSides] = {}, ev0 = nullptr, ev1 = nullptr;
     Clock::time_point t0;
     int64_t next_id = 1;
     std::deque<Req*> queue;
@@ -132,9 +137,12 @@ struct pwmsvc {
         dfree(d_states);
         dfree(d_status);
         if (h_states) cudaFreeHost(h_states);
-        for (cudaEvent_t e : {fork_ev, join_ev[0], join_ev[1], ev0, ev1})
+        for (cudaEvent_t e : {fork_ev, ev0, ev1})
             if (e) cudaEventDestroy(e);
-        for (cudaStream_t s : {stream, side[0], side[1]})
+        for (cudaEvent_t e : join_ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+        for (cudaStream_t s : side)
             if (s) cudaStreamDestroy(s);
     }
 };
@@ -183,7 +191,12 @@ int admit(pwmsvc* S, Req* r) {
         TRY(ensure_low_values(m, q.precision == PWMGPU_PREC_MIXED, &cfg, &r->valp_low, &pg));
         TRY(ensure_fvectors(m));
         CU(launch_convert_f64_f32(m->dx, m->fx, r->n, m->sm_count, m->stream));
-        r->cls = cfg == kCfgBF16 ? kClsBF16 : kClsF32;
+        if (sell_for(m, cfg)) {
+            r->valp_low = cfg == kCfgBF16 ? m->sell.valbf : (const void*)m->sell.val32;
+            r->cls = cfg == kCfgBF16 ? kClsBF16Sell : kClsF32Sell;
+        } else {
+            r->cls = cfg == kCfgBF16 ? kClsBF16 : kClsF32;
+        }
     }
     CU(cudaStreamSynchronize(m->stream));
     r->bytes = solve_bytes(m->M.nor, m->M.nnz, q.precision);
@@ -215,8 +228,13 @@ int rebuild_tables(pwmsvc* S) {
             b.carries = m->carries;
             b.nor = m->M.nor;
             b.nsub = m->P.nsub;
+            if (c == kClsF32Sell || c == kClsBF16Sell) {  // slices instead of sub-tiles, no fix-up
+                b.soff = m->sell.soff;
+                b.col16 = m->sell.col16;
+                b.nsub = m->sell.nslices;
+            }
             b.tile0 = tiles;
-            b.nfix = (b.nsub + kFixTiles - 1) / kFixTiles;
+            b.nfix = (c == kClsF32Sell || c == kClsBF16Sell) ? 0 : (b.nsub + kFixTiles - 1) / kFixTiles;
             b.fix0 = fix;
             b.nrow = (b.nor + kRowChunk - 1) / kRowChunk;
             b.row0 = rows;
@@ -268,15 +286,16 @@ int rebuild_tables(pwmsvc* S) {
 int enqueue_round(pwmsvc* S) {
     const int C = S->cfg.round_iterations;
     CU(cudaEventRecord(S->fork_ev, S->stream));
-    CU(cudaStreamWaitEvent(S->side[0], S->fork_ev, 0));
-    CU(cudaStreamWaitEvent(S->side[1], S->fork_ev, 0));
+    for (int i = 0; i < kSides; ++i) CU(cudaStreamWaitEvent(S->side[i], S->fork_ev, 0));
     CU(launch_batch_round(kCfgF64, S->cls[kClsF64].dT, C, S->sm_count, S->stream));
     CU(launch_batch_round(kCfgF32, S->cls[kClsF32].dT, C, S->sm_count, S->side[0]));
     CU(launch_batch_round(kCfgBF16, S->cls[kClsBF16].dT, C, S->sm_count, S->side[1]));
-    CU(cudaEventRecord(S->join_ev[0], S->side[0]));
-    CU(cudaEventRecord(S->join_ev[1], S->side[1]));
-    CU(cudaStreamWaitEvent(S->stream, S->join_ev[0], 0));
-    CU(cudaStreamWaitEvent(S->stream, S->join_ev[1], 0));
+    CU(launch_batch_round(kCfgF32, S->cls[kClsF32Sell].dT, C, S->sm_count, S->side[2], true));
+    CU(launch_batch_round(kCfgBF16, S->cls[kClsBF16Sell].dT, C, S->sm_count, S->side[3], true));
+    for (int i = 0; i < kSides; ++i) {
+        CU(cudaEventRecord(S->join_ev[i], S->side[i]));
+        CU(cudaStreamWaitEvent(S->stream, S->join_ev[i], 0));
+    }
     return PWMGPU_OK;
 }
 
@@ -415,11 +434,11 @@ int pwmsvc_create(const pwmsvc_config* cfg, pwmsvc** out) {
         cudaError_t e = cudaGetDevice(&S->device);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&S->sm_count, cudaDevAttrMultiProcessorCount, S->device);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->side[0], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->side[1], cudaStreamNonBlocking);
+        for (int i = 0; i < kSides && e == cudaSuccess; ++i)
+            e = cudaStreamCreateWithFlags(&S->side[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->fork_ev, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->join_ev[0], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->join_ev[1], cudaEventDisableTiming);
+        for (int i = 0; i < kSides && e == cudaSuccess; ++i)
+            e = cudaEventCreateWithFlags(&S->join_ev[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreate(&S->ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&S->ev1);
         if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "pwmsvc_create: %s", cudaGetErrorString(e)); break; }
