@@ -201,43 +201,86 @@ __device__ __forceinline__ void load_sell_slot(const BatchTable& T, int j, SellS
     r.e = k > 0 ? pow2_rescale_exponent(st->nsq, rescale_window<float>()) : 0;
 }
 
-// One power step of every live solve of a SELL-32 class: v_{k+1} = 2^{e_k}
-// A_j v_k, one lane per row.  Warp w takes the consecutive global slices
-// [w K, w K + K) (K = slices / warps, rounded up), two at a time; slots own
-// consecutive slices, so the warp's slot advances by a comparison, not a
-// lookup.  Each row is one lane's sum in CRS order: the same bits in any mix.
-template <typename VT>
-__global__ void __launch_bounds__(256, 4) k_batch_sell(const BatchTable* __restrict__ Tp) {
+// One power step of every live solve of a SELL-32 class: v_{k+1} =
+// 2^{e_k} A_j v_k, one lane per row; with NORM also the sums of squares of
+// ||v_{k+1}||^2 per slice group.  A slot's slices form groups of kSellGroup,
+// in the slot's own slice order; warp w takes the consecutive global groups
+// [w K, w K + K) (K = groups / warps, rounded up), two slices at a time, so
+// its slot advances by a comparison.  Per group the lanes' FP64 sums of
+// their rows (widened on the integer pipes) meet in a fixed shuffle tree and
+// land in grp_part; k_batch_grp then sums a slot's groups in order.  Rows
+// are one lane's sums in CRS order and the grouping depends only on the
+// slot: the same bits in any mix.
+template <typename VT, bool NORM>
+__global__ void __launch_bounds__(256, sizeof(VT) == 2 ? 4 : 3) k_batch_sell(const BatchTable* __restrict__ Tp) {
     const BatchTable T = *Tp;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, tw = (gridDim.x * blockDim.x) >> 5;
-    const int K = (T.ntiles + tw - 1) / tw;
-    int g = gw * K;
-    const int g1 = min(g + K, T.ntiles);
-    if (g >= g1) return;
-    int j = __ldg(T.tile_slot + g);
+    const int K = (T.nfix + tw - 1) / tw;
+    int q = gw * K;
+    const int q1 = min(q + K, T.nfix);
+    if (q >= q1) return;
+    int j = find_slot<1>(T.slots, T.nslots, q);
     SellSlotRegs A;
     load_sell_slot(T, j, A);
-    int end = A.tile0 + __ldg(&T.slots[j].nsub);
-    while (g < g1) {
-        while (g >= end) {  // the next slot (slots own consecutive slices)
+    int fix0 = __ldg(&T.slots[j].fix0), nfix = __ldg(&T.slots[j].nfix), nsub = __ldg(&T.slots[j].nsub);
+    for (; q < q1; ++q) {
+        while (q >= fix0 + nfix) {  // the next slot (slots own consecutive groups)
             ++j;
             load_sell_slot(T, j, A);
-            end = A.tile0 + __ldg(&T.slots[j].nsub);
+            fix0 = __ldg(&T.slots[j].fix0);
+            nfix = __ldg(&T.slots[j].nfix);
+            nsub = __ldg(&T.slots[j].nsub);
         }
-        const bool two = g + 1 < g1 && g + 1 < end;
-        const int sa = g - A.tile0;
-        const int oa = __ldg(A.soff + sa), ob = __ldg(A.soff + sa + 1);
-        const int oc = two ? __ldg(A.soff + sa + 2) : ob;
-        const int wa = (ob - oa) >> 5, wb = (oc - ob) >> 5;
-        float ya, yb;
-        sell_rows2<VT, 6>(A.col16 + oa + lane, static_cast<const VT*>(A.valp) + oa + lane, A.in, sa * 32 - 32768,
-                          wa, A.col16 + ob + lane, static_cast<const VT*>(A.valp) + ob + lane, A.in,
-                          sa * 32 + 32 - 32768, wb, ya, yb);
-        const int ra = sa * 32 + lane, rb = ra + 32;
-        if (ra < A.nor) A.out[ra] = A.e ? scale_pow2(ya, A.e) : ya;
-        if (two && rb < A.nor) A.out[rb] = A.e ? scale_pow2(yb, A.e) : yb;
-        g += two ? 2 : 1;
+        const int s1 = min((q - fix0 + 1) * kSellGroup, nsub);
+        double ss = 0.0;
+        for (int s = (q - fix0) * kSellGroup; s < s1; s += 2) {
+            const bool two = s + 1 < s1;
+            const int oa = __ldg(A.soff + s), ob = __ldg(A.soff + s + 1);
+            const int oc = two ? __ldg(A.soff + s + 2) : ob;
+            float ya, yb;
+            sell_rows2<VT, 5>(A.col16 + oa + lane, static_cast<const VT*>(A.valp) + oa + lane, A.in,
+                              s * 32 - 32768, (ob - oa) >> 5, A.col16 + ob + lane,
+                              static_cast<const VT*>(A.valp) + ob + lane, A.in, s * 32 + 32 - 32768, (oc - ob) >> 5,
+                              ya, yb);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = s * 32 + h * 32 + lane;
+                const bool live = (h == 0 || two) && r < A.nor;
+                float out = h ? yb : ya;
+                if (A.e) out = scale_pow2(out, A.e);
+                if (live) A.out[r] = out;
+                else out = 0.0f;
+                if (NORM) {
+                    const double wo = __any_sync(0xffffffffu, widen_special(out)) ? (double)out : widen_normal(out);
+                    ss = fma(wo, wo, ss);
+                }
+            }
+        }
+        if (NORM) {
+            for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+            if (lane == 0) T.grp_part[q] = ss;
+        }
+    }
+}
+
+// After a NORM step: per slot (one warp each) ||v_{k+1}||^2 = its groups'
+// sums in group order, and the slot's state advanced.
+__global__ void __launch_bounds__(256) k_batch_grp(const BatchTable* __restrict__ Tp) {
+    const BatchTable T = *Tp;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, tw = (gridDim.x * blockDim.x) >> 5;
+    for (int j = gw; j < T.nslots; j += tw) {
+        const BatchSlot& d = T.slots[j];
+        double s0 = 0.0;
+        for (int i = lane; i < d.nfix; i += 32) s0 += T.grp_part[d.fix0 + i];
+        for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        if (lane == 0) {
+            SlotState* stt = T.states + d.state;
+            stt->nsq_prev = stt->nsq;
+            stt->nsq = s0;
+            stt->k = stt->k + 1;
+        }
     }
 }
 
@@ -483,31 +526,51 @@ struct BatchKernels {
 
 }  // namespace
 
+// Resident grid of a k_batch_sell instance: every warp's range of slice
+// groups starts at once (a second wave would double the step).
+template <typename VT, bool DOT>
 static int sell_batch_grid(int sm_count) {
     static int occ = 0;
     if (occ == 0) {
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_batch_sell<float>, 256, 0) != cudaSuccess || o < 1) o = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_batch_sell<VT, DOT>, 256, 0) != cudaSuccess || o < 1)
+            o = 1;
         occ = o;
     }
     return occ * sm_count;
+}
+
+// A step of a SELL-32 class: the SpMV with the group sums and the per-slot
+// totals; the round's last step (which also needs v_k . v_{k+1}) takes the
+// row pass instead.
+template <typename VT>
+static void launch_batch_sell(const BatchTable* T, bool dot, int sm_count, cudaStream_t st) {
+    if (dot) {
+        k_batch_sell<VT, false><<<sell_batch_grid<VT, false>(sm_count), 256, 0, st>>>(T);
+        k_batch_norm<float><<<3 * sm_count, 256, 0, st>>>(T, 1);
+    } else {
+        k_batch_sell<VT, true><<<sell_batch_grid<VT, true>(sm_count), 256, 0, st>>>(T);
+        k_batch_grp<<<sm_count, 256, 0, st>>>(T);
+    }
 }
 
 void batch_prepare(int sm_count) {
     BatchKernels<double, double, double>::grid(sm_count);
     BatchKernels<float, float, float>::grid(sm_count);
     BatchKernels<__nv_bfloat16, float, float>::grid(sm_count);
-    sell_batch_grid(sm_count);
+    sell_batch_grid<float, false>(sm_count);
+    sell_batch_grid<float, true>(sm_count);
+    sell_batch_grid<__nv_bfloat16, false>(sm_count);
+    sell_batch_grid<__nv_bfloat16, true>(sm_count);
 }
 
 cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st, bool sell) {
     for (int it = 0; it < steps; ++it) {
         const int want_dot = it == steps - 1;
         cudaError_t e;
-        if (sell) {
-            if (cfg == kCfgBF16) k_batch_sell<__nv_bfloat16><<<sell_batch_grid(sm_count), 256, 0, st>>>(T);
-            else k_batch_sell<float><<<sell_batch_grid(sm_count), 256, 0, st>>>(T);
-            k_batch_norm<float><<<3 * sm_count, 256, 0, st>>>(T, want_dot);
+        if (sell) {  // one kernel per step: SpMV and norm
+            if (cfg == kCfgBF16) launch_batch_sell<__nv_bfloat16>(T, want_dot, sm_count, st);
+            else launch_batch_sell<float>(T, want_dot, sm_count, st);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             continue;
         }

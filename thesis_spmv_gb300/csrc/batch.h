@@ -18,6 +18,7 @@
 namespace pwmgpu {
 
 constexpr int kFixTiles = 256;    // sub-tiles per fix-up chunk (one per thread: a fix-up is latency-bound)
+constexpr int kSellGroup = 16;    // SELL-32 classes: slices per group of the in-kernel norm
 constexpr int kRowChunk = 16384;  // rows per norm / residual chunk (a multiple of 4)
 
 struct BatchSlot {
@@ -34,7 +35,8 @@ struct BatchSlot {
     const uint16_t* col16;  // SELL-32 classes: 16-bit column offsets (values in valp)
     int nor, nsub;
     int tile0;       // first global sub-tile
-    int fix0, nfix;  // fix-up chunks [fix0, fix0 + nfix) (kFixTiles sub-tiles each)
+    int fix0, nfix;  // fix-up chunks [fix0, fix0 + nfix) (kFixTiles sub-tiles each); SELL-32
+                     // classes: slice groups (kSellGroup slices each) of the norm
     int row0, nrow;  // row chunks [row0, row0 + nrow) (kRowChunk rows each)
     int state;       // index into the state array
     int pad;
@@ -59,6 +61,7 @@ struct BatchTable {
     int* tile_slot;     // slot of each global sub-tile
     double* row_part;   // 2 per row chunk: sum of squares, dot
     double* res_part;   // 1 per row chunk
+    double* grp_part;   // SELL-32 classes: 1 per slice group (sum of squares)
     int* status;
 };
 

@@ -69,6 +69,8 @@ struct ClassDev {
     size_t row_cap = 0;
     double* res_part = nullptr;
     size_t res_cap = 0;
+    double* grp_part = nullptr;
+    size_t grp_cap = 0;
 };
 
 int grow(double** p, size_t* cap, size_t need) {
@@ -133,6 +135,7 @@ struct pwmsvc {
             dfree(c.tile_slot);
             dfree(c.row_part);
             dfree(c.res_part);
+            dfree(c.grp_part);
         }
         dfree(d_states);
         dfree(d_status);
@@ -234,7 +237,8 @@ int rebuild_tables(pwmsvc* S) {
                 b.nsub = m->sell.nslices;
             }
             b.tile0 = tiles;
-            b.nfix = (c == kClsF32Sell || c == kClsBF16Sell) ? 0 : (b.nsub + kFixTiles - 1) / kFixTiles;
+            b.nfix = (c == kClsF32Sell || c == kClsBF16Sell) ? (b.nsub + kSellGroup - 1) / kSellGroup
+                                                              : (b.nsub + kFixTiles - 1) / kFixTiles;
             b.fix0 = fix;
             b.nrow = (b.nor + kRowChunk - 1) / kRowChunk;
             b.row0 = rows;
@@ -259,6 +263,7 @@ int rebuild_tables(pwmsvc* S) {
         }
         TRY(grow(&D.row_part, &D.row_cap, 2 * (size_t)rows + 2));
         TRY(grow(&D.res_part, &D.res_cap, (size_t)rows + 1));
+        if (c == kClsF32Sell || c == kClsBF16Sell) TRY(grow(&D.grp_part, &D.grp_cap, (size_t)fix + 1));
         if (!hs.empty())
             CU(cudaMemcpyAsync(D.d_slots, hs.data(), hs.size() * sizeof(BatchSlot), cudaMemcpyHostToDevice,
                                S->stream));
@@ -272,6 +277,7 @@ int rebuild_tables(pwmsvc* S) {
         T.tile_slot = D.tile_slot;
         T.row_part = D.row_part;
         T.res_part = D.res_part;
+        T.grp_part = D.grp_part;
         T.status = S->d_status;
         // pageable source: the copy is staged before the call returns
         CU(cudaMemcpyAsync(D.dT, &T, sizeof T, cudaMemcpyHostToDevice, S->stream));
