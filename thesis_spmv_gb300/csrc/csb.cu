@@ -12,18 +12,32 @@
 // are cut into windows of S rows; one CTA owns a window: it zeroes an S-row
 // y window in shared memory, walks its sub-squares ("units": every block of
 // the block row, every column window) and adds each element's product into
-// the y window (shared-memory atomics), then writes its rows of y once.
-// Dense units (at least kDenseUnit elements) stage their S-column x window in
-// shared memory with a TMA bulk copy (double-buffered, mbarriers) and are
-// taken by the whole CTA; sparse units (a random matrix's blocks hold a few
-// elements each) are taken one per warp, gathering x through L1/L2 -- staging
-// 8 KB of x for a handful of elements would cost more than it saves.  y is
-// written once per row and no CTA touches another's rows.  The summation
-// order within a row follows the order the atomics land in (the per-row
-// error bound holds for any order).
+// the y window, then writes its rows of y once.  Dense units (at least
+// kDenseUnit elements) stage their S-column x window in shared memory with a
+// TMA bulk copy (double-buffered, mbarriers) and are taken by the whole CTA;
+// sparse units (a random matrix's blocks hold a few elements each) are taken
+// one per warp, gathering x through L1/L2 -- staging 8 KB of x for a handful
+// of elements would cost more than it saves -- and add with shared-memory
+// atomics.  y is written once per row and no CTA touches another's rows.
+//
+// The device copy (csb_kernel_layout) keeps the blocks, their block-column
+// order and the Z-Morton order of the sub-squares, but stores each dense
+// unit row-major (rows ascending, columns ascending within a row, duplicates
+// in build order) from a multiple of 4 elements: the order inside a
+// sub-square is free for y += A x, and on this GPU a shared-memory FP64
+// atomic add is a compare-and-swap loop that bounded the Z-ordered kernel.
+// A warp takes 128 elements of a dense unit (4 per lane: one 16-byte load of
+// ind, two of data), sums each lane's runs of a row in registers, joins runs
+// that cross lanes with a segmented scan over the lanes, and adds every row
+// once; only the rows touching a chunk's first or last element (they may
+// continue in another warp's chunk) are added atomically.  The host arrays
+// (pwmgpu_get_csb) stay the reference's.  Per row, the summation order is the
+// column order inside each dense unit and the order the atomics land in
+// elsewhere (the per-row error bound holds for any order).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -36,7 +50,8 @@ namespace pwmgpu {
 
 namespace {
 
-constexpr int kCsbNT = 256;
+constexpr int kCsbNT = 128;
+constexpr int kCsbOcc = 8;  // resident CTAs per SM (64 registers, 24.6 KB shared memory)
 constexpr int kCsbMaxS = 1024;
 constexpr int kDenseUnit = 256;  // elements from which a unit's x window is staged
 
@@ -59,9 +74,152 @@ struct Unit {
     int pad;
 };
 
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kLaneElems = 8;                // elements of a dense unit per lane per step
+constexpr int kChunk = 32 * kLaneElems;      // elements of a dense unit per warp step
+
+// One lane's elements of a row-major dense unit.
+struct Oct {
+    uint4 id[2];
+    double2 d[4];
+    int nv;    // valid elements (0..8)
+    int rout;  // lane 0: row of the element before the chunk, lane 1: after it (-1: none)
+};
+
+// Lane `lane`'s elements of the chunk at k0 of unit [lo, hi), and the row of
+// the element just outside the chunk (lanes 0 and 1).
+__device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const double* __restrict__ data, int k0,
+                                        int lo, int hi, int S, int lane) {
+    Oct q;
+    const int k = k0 + kLaneElems * lane;
+    q.nv = k < hi ? min(kLaneElems, hi - k) : 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) q.id[i] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q.d[i] = make_double2(0.0, 0.0);
+    if (q.nv) {  // k is a multiple of 4 and the arrays are padded past the last unit by 8
+        const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
+        const double2* dp = reinterpret_cast<const double2*>(data + k);
+        q.id[0] = __ldg(ip);
+        q.d[0] = __ldg(dp);
+        q.d[1] = __ldg(dp + 1);
+        if (q.nv > 4) {
+            q.id[1] = __ldg(ip + 1);
+            q.d[2] = __ldg(dp + 2);
+            q.d[3] = __ldg(dp + 3);
+        }
+    }
+    q.rout = -1;
+    if (k0 >= hi) return q;  // a warp past the unit's end
+    if (lane == 0 && k0 > lo) q.rout = (int)(__ldg(ind + k0 - 1) >> 16) & (S - 1);
+    if (lane == 1 && k0 + kChunk < hi) q.rout = (int)(__ldg(ind + k0 + kChunk) >> 16) & (S - 1);
+    return q;
+}
+
+// Add a warp's chunk (lane l holds elements 8l..8l+7 of it, rows sorted)
+// into the y window with one FMA per element wherever a row lies inside one
+// lane: such a row starts from ys[row] and is stored back.  The rest are
+// "partial" rows, summed from zero: a lane's first row rf when it continues
+// the previous lane's last row ("joins"), its last row rl when the next lane
+// joins it, and the chunk's first / last row when the element just outside
+// the chunk has the same row (then another warp adds to it as well).  The
+// lane where a partial row ends adds the partials of its chain of lanes
+// (a few shuffles, or a segmented scan for long chains) -- atomically for
+// rows that cross the chunk, with a plain add otherwise.
+__device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw, double* ys, int lane) {
+    // the rows of the elements just before and after the chunk (-1: none)
+    const int row_before = __shfl_sync(kFull, q.rout, 0), row_after = __shfl_sync(kFull, q.rout, 1);
+    const uint32_t ids[kLaneElems] = {q.id[0].x, q.id[0].y, q.id[0].z, q.id[0].w,
+                                      q.id[1].x, q.id[1].y, q.id[1].z, q.id[1].w};
+    const double vs[kLaneElems] = {q.d[0].x, q.d[0].y, q.d[1].x, q.d[1].y, q.d[2].x, q.d[2].y, q.d[3].x, q.d[3].y};
+    const int nv = q.nv;
+    const int rf = (int)(ids[0] >> 16) & (S - 1);
+    int rl = rf;
+#pragma unroll
+    for (int j = 1; j < kLaneElems; ++j)
+        if (j < nv) rl = (int)(ids[j] >> 16) & (S - 1);
+    const int rl_prev = __shfl_up_sync(kFull, rl, 1);
+    const int nv_prev = __shfl_up_sync(kFull, nv, 1);
+    const bool joins = lane > 0 && nv > 0 && nv_prev > 0 && rl_prev == rf;
+    const bool next_joins = __shfl_down_sync(kFull, joins, 1) && lane < 31;
+    const int last_lane = __reduce_max_sync(kFull, nv > 0 ? lane : 0);
+    const int first_row = __shfl_sync(kFull, rf, 0);
+    const int last_row = __shfl_sync(kFull, rl, last_lane);
+    const bool cross_lo = row_before == first_row, cross_hi = row_after == last_row;
+    const bool one_row = rf == rl;
+    const bool bnd_f = (rf == first_row && cross_lo) || (rf == last_row && cross_hi);
+    const bool bnd_l = (rl == first_row && cross_lo) || (rl == last_row && cross_hi);
+    const bool part_f = nv > 0 && (joins || bnd_f || (one_row && next_joins));
+    const bool part_l = nv > 0 && !one_row && (next_joins || bnd_l);
+    // accumulate: rows inside the lane start from ys, partial rows from zero
+    double pf = 0.0, pl = 0.0, acc = 0.0;
+    int cur = -1;
+#pragma unroll
+    for (int j = 0; j < kLaneElems; ++j) {
+        if (j < nv) {
+            const int r = (int)(ids[j] >> 16) & (S - 1);
+            if (r != cur) {
+                if (cur >= 0) {
+                    if (cur == rf && part_f)
+                        pf = acc;
+                    else
+                        ys[cur] = acc;
+                }
+                cur = r;
+                acc = (r == rf && part_f) || (r == rl && part_l) ? 0.0 : ys[r];
+            }
+            acc = fma(vs[j], xw[ids[j] & (uint32_t)(S - 1)], acc);
+        }
+    }
+    if (cur >= 0) {
+        if (cur == rf && part_f)
+            pf = acc;
+        else if (cur == rl && part_l)
+            pl = acc;
+        else
+            ys[cur] = acc;
+    }
+    // chains: lane l's tail value is the partial of its last row
+    const double t = one_row ? pf : pl;
+    const bool add_f = part_f && (!one_row || !next_joins);  // partial first row ends here
+    // a chain of lanes starts at a lane that is not a one-row lane joining
+    // its predecessor; len = the earlier lanes of this lane's chain
+    const unsigned starts = __ballot_sync(kFull, !(one_row && joins));
+    const int len = joins ? lane - (31 - __clz(starts & ((1u << lane) - 1u))) : 0;
+    const int maxlen = __reduce_max_sync(kFull, add_f ? len : 0);
+    double tot = pf;
+    if (maxlen <= 6) {
+        for (int i = 1; i <= maxlen; ++i) {
+            const double v = __shfl_up_sync(kFull, t, i);
+            if (i <= len) tot += v;
+        }
+    } else {  // long rows: segmented scan of the tail values
+        double a = t;
+        bool head = !(one_row && joins);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const double a2 = __shfl_up_sync(kFull, a, d);
+            const bool h2 = __shfl_up_sync(kFull, head, d);
+            if (lane >= d && !head) {
+                a += a2;
+                head = h2;
+            }
+        }
+        const double carry = __shfl_up_sync(kFull, a, 1);
+        if (joins) tot += carry;
+    }
+    if (add_f) {
+        if (bnd_f)
+            atomicAdd(&ys[rf], tot);
+        else
+            ys[rf] += tot;
+    }
+    if (part_l && !next_joins) atomicAdd(&ys[rl], pl);  // the chunk's last row, continued by another warp
+}
+
 // win_ptr[2w] = the window's first unit, win_ptr[2w+1] = its first dense
 // unit, win_ptr[2w+2] = the next window's first unit.
-__global__ void __launch_bounds__(kCsbNT) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
+__global__ void __launch_bounds__(kCsbNT, kCsbOcc) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
                                                      const int* __restrict__ win_ptr, const int4* __restrict__ units,
                                                      int nwin, int S, int nor, int noc, const double* __restrict__ x,
                                                      double* __restrict__ y, const double* nsq_in, int* status) {
@@ -117,15 +275,20 @@ __global__ void __launch_bounds__(kCsbNT) k_csb_spmv(const uint32_t* __restrict_
             const int b = (u - u0) & 1;
             __syncthreads();  // buffer b^1 is free (its unit is done), ys zeroed
             if (u + 1 < u1) stage(u + 1, b ^ 1);
+            // row-major unit: warp chunks of kChunk elements; the first
+            // chunk's loads are in flight while the x window lands
+            const int4 un = __ldg(units + u);
+            constexpr int kStep = (kCsbNT / 32) * kChunk;
+            int k = un.x + warp * kChunk;
+            Oct q = load_oct(ind, data, k, un.x, un.y, S, lane);
             ok = mbar_wait_bounded(&bar[b], uses[b] & 1u, status);
             uses[b]++;
             if (!__syncthreads_and(ok)) break;
-            const int4 un = __ldg(units + u);
             const double* xw = xs[b];
-            for (int k = un.x + tid; k < un.y; k += kCsbNT) {
-                const uint32_t id = __ldg(ind + k);
-                const int r = (int)(id >> 16) & (S - 1), c = (int)(id & 0xFFFFu) & (S - 1);
-                atomicAdd(&ys[r], __ldg(data + k) * xw[c]);
+            while (k < un.y) {
+                dense_oct(q, S, xw, ys, lane);
+                k += kStep;
+                if (k < un.y) q = load_oct(ind, data, k, un.x, un.y, S, lane);
             }
         }
         if (!ok) {
@@ -231,6 +394,64 @@ int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
     return 0;
 }
 
+// Device copy for k_csb_spmv from the built arrays: per window its sparse
+// units as built (Z-Morton order), then its dense units, each re-ordered
+// row-major (a stable sort by ind = local row << 16 | local column) from a
+// multiple of 4 elements; the gaps hold zeros and are never read as
+// elements.  units (4 ints per unit, win_ptr order) is rewritten to the new
+// ranges.  Windows are independent: filled by a few host threads.  Returns
+// false when the padded copy would not fit 32-bit element offsets.
+bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data,
+                       const std::vector<int>& win_ptr, std::vector<int>& units, std::vector<uint32_t>& kind,
+                       std::vector<double>& kdata) {
+    const int nunits = (int)(units.size() / 4);
+    const int nwin = (int)(win_ptr.size() / 2);
+    std::vector<int> dense(nunits, 0), lo_new(nunits + 1, 0);
+    for (int w = 0; w < nwin; ++w)
+        for (int u = win_ptr[2 * (size_t)w + 1]; u < win_ptr[2 * (size_t)w + 2]; ++u) dense[u] = 1;
+    long long o = 0;
+    for (int u = 0; u < nunits; ++u) {
+        if (dense[u]) o = (o + 3) & ~3LL;
+        lo_new[u] = (int)o;
+        o += units[4 * (size_t)u + 1] - units[4 * (size_t)u];
+    }
+    if (o + 8 > (long long)INT32_MAX) return false;
+    const size_t total = (size_t)((o + 3) & ~3LL) + 4;
+    kind.assign(total, 0u);
+    kdata.assign(total, 0.0);
+    auto work = [&](int u0, int u1) {
+        std::vector<std::pair<uint32_t, int>> key;
+        for (int u = u0; u < u1; ++u) {
+            const int lo = units[4 * (size_t)u], hi = units[4 * (size_t)u + 1], dst = lo_new[u];
+            if (!dense[u]) {
+                std::copy(ind.begin() + lo, ind.begin() + hi, kind.begin() + dst);
+                std::copy(data.begin() + lo, data.begin() + hi, kdata.begin() + dst);
+                continue;
+            }
+            key.clear();
+            for (int k = lo; k < hi; ++k) key.emplace_back(ind[(size_t)k], k);
+            std::sort(key.begin(), key.end());  // (ind, position): stable by construction
+            for (size_t q = 0; q < key.size(); ++q) {
+                kind[(size_t)dst + q] = key[q].first;
+                kdata[(size_t)dst + q] = data[(size_t)key[q].second];
+            }
+        }
+    };
+    const int nt = std::max(1, std::min<int>(nunits / 64 + 1, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) {
+        const int a = (int)((long long)nunits * t / nt), b = (int)((long long)nunits * (t + 1) / nt);
+        th.emplace_back(work, a, b);
+    }
+    for (auto& t : th) t.join();
+    for (int u = 0; u < nunits; ++u) {
+        const int len = units[4 * (size_t)u + 1] - units[4 * (size_t)u];
+        units[4 * (size_t)u] = lo_new[u];
+        units[4 * (size_t)u + 1] = lo_new[u] + len;
+    }
+    return true;
+}
+
 // CSB.hpp:96-113 with sizeof(T) = 8, L2_CACHE_SIZE_MB = 1, L2_CACHE_MULT =
 // 0.85 (Util/Constants.hpp:27-28).
 void csb_params(int nor, int noc, int* beta, int* bits) {
@@ -262,7 +483,7 @@ cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* 
                             int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
                             int sm_count, cudaStream_t st) {
     if (nwin <= 0) return cudaSuccess;
-    int grid = std::min(nwin, sm_count * 8);
+    int grid = std::min(nwin, sm_count * kCsbOcc);
     k_csb_spmv<<<grid, kCsbNT, 0, st>>>(ind, data, win_ptr, reinterpret_cast<const int4*>(units), nwin, S, nor, noc,
                                         x, y, nsq_in, status);
     return cudaGetLastError();

@@ -93,17 +93,19 @@ int build_format(pwmgpu_matrix* m) {
         std::vector<int> win_ptr, units;
         csb_build_host(nor, noc, nnz, rs.data(), ci.data(), va.data(), c.beta, c.bits, c.h_ind, c.h_data,
                        c.h_blk_ptr, c.S, win_ptr, units);
-        TRY(dalloc(&c.ind, (size_t)nnz + 4));
-        TRY(dalloc(&c.data, (size_t)nnz + 4));
+        // the kernel's copy: dense sub-squares row-major (csb.cu); the
+        // reference's arrays stay on the host for pwmgpu_get_csb
+        std::vector<uint32_t> kind;
+        std::vector<double> kdata;
+        if (!csb_kernel_layout(c.h_ind, c.h_data, win_ptr, units, kind, kdata))
+            return fail(PWMGPU_ERR_INVALID, "CSB: the padded device copy exceeds 32-bit element offsets");
+        TRY(dalloc(&c.ind, kind.size()));
+        TRY(dalloc(&c.data, kdata.size()));
         TRY(dalloc(&c.blk_ptr, c.h_blk_ptr.size()));
         TRY(dalloc(&c.win_ptr, win_ptr.size()));
         TRY(dalloc(&c.units, units.size() + 4));
-        if (nnz > 0) {
-            CU(cudaMemcpyAsync(c.ind, c.h_ind.data(), sizeof(uint32_t) * (size_t)nnz, cudaMemcpyHostToDevice,
-                               m->stream));
-            CU(cudaMemcpyAsync(c.data, c.h_data.data(), sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice,
-                               m->stream));
-        }
+        CU(cudaMemcpyAsync(c.ind, kind.data(), sizeof(uint32_t) * kind.size(), cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(c.data, kdata.data(), sizeof(double) * kdata.size(), cudaMemcpyHostToDevice, m->stream));
         CU(cudaMemcpyAsync(c.blk_ptr, c.h_blk_ptr.data(), sizeof(int32_t) * c.h_blk_ptr.size(),
                            cudaMemcpyHostToDevice, m->stream));
         CU(cudaMemcpyAsync(c.win_ptr, win_ptr.data(), sizeof(int) * win_ptr.size(), cudaMemcpyHostToDevice,
@@ -1444,12 +1446,13 @@ int pwmgpu_get_csb(pwmgpu_matrix* m, uint32_t* ind, double* data, int32_t* blk_p
     if (!m->loaded || m->format != PWMGPU_FMT_CSB) return fail(PWMGPU_ERR_STATE, "no CSB matrix loaded");
     const auto& c = m->csb;
     if (!blk_ptr || (m->M.nnz > 0 && (!ind || !data))) return fail(PWMGPU_ERR_INVALID, "null output array");
+    // the host copies are the reference's arrays (the device copy orders
+    // dense sub-squares row-major for the kernel)
     if (m->M.nnz > 0) {
-        CU(cudaMemcpyAsync(ind, c.ind, sizeof(uint32_t) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
-        CU(cudaMemcpyAsync(data, c.data, sizeof(double) * (size_t)m->M.nnz, cudaMemcpyDeviceToHost, m->stream));
+        std::memcpy(ind, c.h_ind.data(), sizeof(uint32_t) * (size_t)m->M.nnz);
+        std::memcpy(data, c.h_data.data(), sizeof(double) * (size_t)m->M.nnz);
     }
-    CU(cudaMemcpyAsync(blk_ptr, c.blk_ptr, sizeof(int32_t) * c.h_blk_ptr.size(), cudaMemcpyDeviceToHost, m->stream));
-    CU(cudaStreamSynchronize(m->stream));
+    std::memcpy(blk_ptr, c.h_blk_ptr.data(), sizeof(int32_t) * c.h_blk_ptr.size());
     return PWMGPU_OK;
 }
 
