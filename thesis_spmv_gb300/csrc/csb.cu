@@ -27,7 +27,8 @@
 // sub-square is free for y += A x, and on this GPU a shared-memory FP64
 // atomic add is a compare-and-swap loop that bounded the Z-ordered kernel.
 // A warp takes 128 elements of a dense unit (4 per lane: one 16-byte load of
-// ind, two of data), sums each lane's runs of a row in registers, joins runs
+// ind, two of data; 4 rather than 8 keeps the lanes' x / y-window words
+// close together in shared memory), sums each lane's runs of a row in registers, joins runs
 // that cross lanes with a segmented scan over the lanes, and adds every row
 // once; only the rows touching a chunk's first or last element (they may
 // continue in another warp's chunk) are added atomically.  The host arrays
@@ -51,7 +52,7 @@ namespace pwmgpu {
 namespace {
 
 constexpr int kCsbNT = 128;
-constexpr int kCsbOcc = 8;  // resident CTAs per SM (64 registers, 24.6 KB shared memory)
+constexpr int kCsbOcc = 8;  // resident CTAs per SM (at most 64 registers, 24.6 KB shared memory)
 constexpr int kCsbMaxS = 1024;
 constexpr int kDenseUnit = 256;  // elements from which a unit's x window is staged
 
@@ -75,14 +76,14 @@ struct Unit {
 };
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr int kLaneElems = 8;                // elements of a dense unit per lane per step
-constexpr int kChunk = 32 * kLaneElems;      // elements of a dense unit per warp step
+constexpr int kLaneElems = 4;  // elements of a dense unit per lane per step (8: 0.438 ms, 4: 0.336 ms on the 4096^2 stencil)
+constexpr int kChunk = 32 * kLaneElems;  // elements of a dense unit per warp step
 
 // One lane's elements of a row-major dense unit.
 struct Oct {
-    uint4 id[2];
-    double2 d[4];
-    int nv;    // valid elements (0..8)
+    uint4 id[kLaneElems / 4];
+    double2 d[kLaneElems / 2];
+    int nv;    // valid elements (0..kLaneElems)
     int rout;  // lane 0: row of the element before the chunk, lane 1: after it (-1: none)
 };
 
@@ -94,21 +95,20 @@ __device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const 
     const int k = k0 + kLaneElems * lane;
     q.nv = k < hi ? min(kLaneElems, hi - k) : 0;
 #pragma unroll
-    for (int i = 0; i < 2; ++i) q.id[i] = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) q.d[i] = make_double2(0.0, 0.0);
-    if (q.nv) {  // k is a multiple of 4 and the arrays are padded past the last unit by 8
-        const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
-        const double2* dp = reinterpret_cast<const double2*>(data + k);
-        q.id[0] = __ldg(ip);
-        q.d[0] = __ldg(dp);
-        q.d[1] = __ldg(dp + 1);
-        if (q.nv > 4) {
-            q.id[1] = __ldg(ip + 1);
-            q.d[2] = __ldg(dp + 2);
-            q.d[3] = __ldg(dp + 3);
-        }
+    for (int i = 0; i < kLaneElems / 4; ++i) {
+        q.id[i] = make_uint4(0u, 0u, 0u, 0u);
+        q.d[2 * i] = q.d[2 * i + 1] = make_double2(0.0, 0.0);
     }
+    // k is a multiple of 4 and the arrays are padded past the last unit by 8
+    const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
+    const double2* dp = reinterpret_cast<const double2*>(data + k);
+#pragma unroll
+    for (int i = 0; i < kLaneElems / 4; ++i)
+        if (4 * i < q.nv) {
+            q.id[i] = __ldg(ip + i);
+            q.d[2 * i] = __ldg(dp + 2 * i);
+            q.d[2 * i + 1] = __ldg(dp + 2 * i + 1);
+        }
     q.rout = -1;
     if (k0 >= hi) return q;  // a warp past the unit's end
     if (lane == 0 && k0 > lo) q.rout = (int)(__ldg(ind + k0 - 1) >> 16) & (S - 1);
@@ -129,9 +129,14 @@ __device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const 
 __device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw, double* ys, int lane) {
     // the rows of the elements just before and after the chunk (-1: none)
     const int row_before = __shfl_sync(kFull, q.rout, 0), row_after = __shfl_sync(kFull, q.rout, 1);
-    const uint32_t ids[kLaneElems] = {q.id[0].x, q.id[0].y, q.id[0].z, q.id[0].w,
-                                      q.id[1].x, q.id[1].y, q.id[1].z, q.id[1].w};
-    const double vs[kLaneElems] = {q.d[0].x, q.d[0].y, q.d[1].x, q.d[1].y, q.d[2].x, q.d[2].y, q.d[3].x, q.d[3].y};
+    uint32_t ids[kLaneElems];
+    double vs[kLaneElems];
+#pragma unroll
+    for (int j = 0; j < kLaneElems; ++j) {
+        const uint4& u4 = q.id[j >> 2];
+        ids[j] = (j & 3) == 0 ? u4.x : (j & 3) == 1 ? u4.y : (j & 3) == 2 ? u4.z : u4.w;
+        vs[j] = (j & 1) ? q.d[j >> 1].y : q.d[j >> 1].x;
+    }
     const int nv = q.nv;
     const int rf = (int)(ids[0] >> 16) & (S - 1);
     int rl = rf;
