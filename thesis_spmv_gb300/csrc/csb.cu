@@ -28,13 +28,16 @@
 // atomic add is a compare-and-swap loop that bounded the Z-ordered kernel.
 // A warp takes 128 elements of a dense unit (4 per lane: one 16-byte load of
 // ind, two of data; 4 rather than 8 keeps the lanes' x / y-window words
-// close together in shared memory), sums each lane's runs of a row in registers, joins runs
-// that cross lanes with a segmented scan over the lanes, and adds every row
-// once; only the rows touching a chunk's first or last element (they may
-// continue in another warp's chunk) are added atomically.  The host arrays
-// (pwmgpu_get_csb) stay the reference's.  Per row, the summation order is the
-// column order inside each dense unit and the order the atomics land in
-// elsewhere (the per-row error bound holds for any order).
+// close together in shared memory).  A row that lies inside one lane starts
+// from its y-window value and takes one FMA per element (the FP64 pipe, about
+// 2 operations per clock per SM here, is the scarce unit); a row split
+// across lanes is summed from zero in each and added once by the lane where
+// it ends, which gathers the chain's partials with shuffles (a segmented scan
+// for long rows); only a row that continues past the warp's chunk (the
+// element just outside has the same row) is added atomically.  The host
+// arrays (pwmgpu_get_csb) stay the reference's.  Per row, the summation
+// order is the column order inside each dense unit and the order the atomics
+// land in elsewhere (the per-row error bound holds for any order).
 #include <cuda_runtime.h>
 
 #include <algorithm>
