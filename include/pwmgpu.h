@@ -44,6 +44,12 @@ extern "C" {
 #define PWMGPU_FMT_MERGE 0 /* CRS, merge-path SpMV (SOA_Implementations/CRS_Merge.hpp) */
 #define PWMGPU_FMT_CSB 1   /* compressed sparse blocks (SOA_Implementations/CSB.hpp) */
 #define PWMGPU_FMT_COH 2   /* row-distributed Hilbert block CO-H (SOA_Implementations/BlockCOH.hpp) */
+/* Format autotuner (no counterpart in the reference, whose drivers pick the
+ * method by number): the handle keeps the merge-path plan (solves, FP32 and
+ * host-array paths) and runs its FP64 mv / powerIteration with whichever of
+ * merge, CSB or CO-H, and which kernel variant, the tuner found fastest for
+ * the matrix's class (pwmgpu_tuning_info). */
+#define PWMGPU_FMT_AUTO 3
 
 /* ---- precision of a power solve ---- */
 #define PWMGPU_PREC_F64 0   /* FP64 values, vectors and accumulation */
@@ -128,6 +134,53 @@ typedef struct {
     int32_t max_row_nnz; /* longest row */
 } pwmgpu_matrix_stats;
 int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out);
+
+/* ---- format autotuner (PWMGPU_FMT_AUTO handles; no counterpart in the
+ *      reference) ----
+ * A matrix class is a key of the statistics above (Util_Scripts/
+ * calc_stats.cpp:45-98 features) and the SM count: floor(log2 nor),
+ * floor(2 log2 rows_avg), floor(log2(1 + 8 cv_rows)) with cv_rows =
+ * sqrt(rows_var) / rows_avg, floor(log2(1 + cv_blocks)) with cv_blocks =
+ * sqrt(block_var) / block_avg, balanced, floor(log2(1 + max_row_nnz)),
+ * sm_count.  The first matrix of a class loaded into an AUTO handle times
+ * every candidate -- the merge kernels' 4 launch variants (shared-memory /
+ * L1 carveout x gathers through or around L1), CSB with 4 or 8 elements
+ * per lane and 128 or 256 threads per CTA, and CO-H with a warp per
+ * partition (max(32 sm_count, nor / 2000) partitions) -- on a few SpMVs each
+ * and records the fastest in a process-wide table; later matrices of the
+ * class take the recorded choice without timing.  Matrices too small to time
+ * (the merge tuner's threshold) run merge. */
+typedef struct {
+    int32_t format;          /* PWMGPU_FMT_MERGE / _CSB / _COH: the FP64 SpMV in use */
+    int32_t csb_variant;     /* CSB kernel variant: bit 0 = 8 elements per lane, bit 1 = 256 threads */
+    int32_t merge_variant;   /* merge launch variant (pwmgpu_launch_config) */
+    int32_t cache_hit;       /* 1: taken from the class table without timing */
+    int32_t timed;           /* 1: candidates were timed for this matrix */
+    int32_t class_key[7];
+    float merge_ms;          /* ms per SpMV of the best merge variant (0 if not timed) */
+    float csb_ms[4];         /* per CSB variant */
+    float coh_ms;
+    double tune_seconds;     /* wall time of the tuning (builds and timings) */
+} pwmgpu_tuning;
+int pwmgpu_tuning_info(const pwmgpu_matrix* m, pwmgpu_tuning* out);
+/* The class key of a statistics record for `sm_count` SMs (host only). */
+int pwmgpu_class_key(const pwmgpu_matrix_stats* st, int32_t sm_count, int32_t key[7]);
+/* Forget every recorded class choice (the next matrix of each class is
+ * timed again). */
+int pwmgpu_tuner_reset(void);
+/* Number of classes recorded. */
+int pwmgpu_tuner_size(void);
+/* Record a class choice (to carry tunings between processes): format
+ * PWMGPU_FMT_MERGE / _CSB / _COH, csb_variant 0..3, merge_variant one of
+ * the merge launch variants (0, 1, 4, 5). */
+int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant);
+/* Copy up to `max` recorded entries: keys[7 i ..], choices[3 i ..] =
+ * {format, csb_variant, merge_variant}; returns the number copied (or a
+ * negative status). */
+int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices);
+/* CSB kernel variant of a PWMGPU_FMT_CSB handle (0..3, as csb_variant
+ * above; 0 by default). */
+int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant);
 
 /* Replaces mv(x, y) (SparseMatrix.hpp:57, CRS.hpp:99-109): y = A x with
  * caller-owned host arrays x[noc], y[nor]; synchronous. */

@@ -16,7 +16,7 @@ PWMGPU_OK = 0
 STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_TIMEOUT", 5: "ERR_STATE",
                 6: "ERR_NOT_SQUARE", 7: "ERR_BUDGET", 8: "ERR_NUMERIC", 9: "ERR_UNSUPPORTED"}
 
-FMT_MERGE, FMT_CSB, FMT_COH = 0, 1, 2
+FMT_MERGE, FMT_CSB, FMT_COH, FMT_AUTO = 0, 1, 2, 3
 PREC_F64, PREC_F32, PREC_MIXED = 0, 1, 2
 POWER_AUTO, POWER_FUSED, POWER_MULTI = 0, 1, 2
 LOWFMT_AUTO, LOWFMT_MERGE = 0, 1
@@ -34,6 +34,14 @@ class MatrixStats(C.Structure):
     _fields_ = [("size", C.c_int64), ("nnz", C.c_int64), ("rows_avg", C.c_double), ("rows_var", C.c_double),
                 ("block_avg", C.c_double), ("block_var", C.c_double), ("balanced", C.c_int32),
                 ("block_bits", C.c_int32), ("nb_blocks", C.c_int32), ("max_row_nnz", C.c_int32)]
+
+
+class Tuning(C.Structure):
+    """pwmgpu_tuning: what the format autotuner chose for a PWMGPU_FMT_AUTO handle."""
+    _fields_ = [("format", C.c_int32), ("csb_variant", C.c_int32), ("merge_variant", C.c_int32),
+                ("cache_hit", C.c_int32), ("timed", C.c_int32), ("class_key", C.c_int32 * 7),
+                ("merge_ms", C.c_float), ("csb_ms", C.c_float * 4), ("coh_ms", C.c_float),
+                ("tune_seconds", C.c_double)]
 
 
 class SolveInfo(C.Structure):
@@ -59,6 +67,13 @@ SIGNATURES = {
     "pwmgpu_load_triplets_device": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
     "pwmgpu_dims": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64)]),
     "pwmgpu_stats": (C.c_int, [vp, C.POINTER(MatrixStats)]),
+    "pwmgpu_tuning_info": (C.c_int, [vp, C.POINTER(Tuning)]),
+    "pwmgpu_class_key": (C.c_int, [C.POINTER(MatrixStats), i32, C.POINTER(i32)]),
+    "pwmgpu_tuner_reset": (C.c_int, []),
+    "pwmgpu_tuner_size": (C.c_int, []),
+    "pwmgpu_tuner_record": (C.c_int, [C.POINTER(i32), i32, i32, i32]),
+    "pwmgpu_tuner_entries": (C.c_int, [i32, C.POINTER(i32), C.POINTER(i32)]),
+    "pwmgpu_set_csb_variant": (C.c_int, [vp, i32]),
     "pwmgpu_get_csr": (C.c_int, [vp, vp, vp, vp]),
     "pwmgpu_mv": (C.c_int, [vp, vp, vp]),
     "pwmgpu_mv_device": (C.c_int, [vp, vp, vp]),

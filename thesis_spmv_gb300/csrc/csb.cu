@@ -54,8 +54,12 @@ namespace pwmgpu {
 
 namespace {
 
-constexpr int kCsbNT = 128;
-constexpr int kCsbOcc = 8;  // resident CTAs per SM (at most 64 registers, 24.6 KB shared memory)
+// Kernel variants (launch_csb_spmv's `variant`): bit 0 = 8 elements of a
+// dense unit per lane (else 4), bit 1 = 256 threads per CTA (else 128).
+// Every variant is launched with 1024 resident threads per SM (at most 64
+// registers; 24.6 KB of shared memory per CTA).  Variant 0 is the default;
+// the format autotuner times all four.
+constexpr int kCsbThreadsPerSM = 1024;
 constexpr int kCsbMaxS = 1024;
 constexpr int kDenseUnit = 256;  // elements from which a unit's x window is staged
 
@@ -79,26 +83,27 @@ struct Unit {
 };
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
-constexpr int kLaneElems = 4;  // elements of a dense unit per lane per step (8: 0.438 ms, 4: 0.336 ms on the 4096^2 stencil)
-constexpr int kChunk = 32 * kLaneElems;  // elements of a dense unit per warp step
 
-// One lane's elements of a row-major dense unit.
+// One lane's K elements of a row-major dense unit (a warp's chunk is 32 K).
+template <int K>
 struct Oct {
-    uint4 id[kLaneElems / 4];
-    double2 d[kLaneElems / 2];
-    int nv;    // valid elements (0..kLaneElems)
+    uint4 id[K / 4];
+    double2 d[K / 2];
+    int nv;    // valid elements (0..K)
     int rout;  // lane 0: row of the element before the chunk, lane 1: after it (-1: none)
 };
 
 // Lane `lane`'s elements of the chunk at k0 of unit [lo, hi), and the row of
 // the element just outside the chunk (lanes 0 and 1).
-__device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const double* __restrict__ data, int k0,
+template <int K>
+__device__ __forceinline__ Oct<K> load_oct(const uint32_t* __restrict__ ind, const double* __restrict__ data, int k0,
                                         int lo, int hi, int S, int lane) {
-    Oct q;
-    const int k = k0 + kLaneElems * lane;
-    q.nv = k < hi ? min(kLaneElems, hi - k) : 0;
+    constexpr int kChunk = 32 * K;
+    Oct<K> q;
+    const int k = k0 + K * lane;
+    q.nv = k < hi ? min(K, hi - k) : 0;
 #pragma unroll
-    for (int i = 0; i < kLaneElems / 4; ++i) {
+    for (int i = 0; i < K / 4; ++i) {
         q.id[i] = make_uint4(0u, 0u, 0u, 0u);
         q.d[2 * i] = q.d[2 * i + 1] = make_double2(0.0, 0.0);
     }
@@ -106,7 +111,7 @@ __device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const 
     const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
     const double2* dp = reinterpret_cast<const double2*>(data + k);
 #pragma unroll
-    for (int i = 0; i < kLaneElems / 4; ++i)
+    for (int i = 0; i < K / 4; ++i)
         if (4 * i < q.nv) {
             q.id[i] = __ldg(ip + i);
             q.d[2 * i] = __ldg(dp + 2 * i);
@@ -129,13 +134,14 @@ __device__ __forceinline__ Oct load_oct(const uint32_t* __restrict__ ind, const 
 // lane where a partial row ends adds the partials of its chain of lanes
 // (a few shuffles, or a segmented scan for long chains) -- atomically for
 // rows that cross the chunk, with a plain add otherwise.
-__device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw, double* ys, int lane) {
+template <int K>
+__device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* xw, double* ys, int lane) {
     // the rows of the elements just before and after the chunk (-1: none)
     const int row_before = __shfl_sync(kFull, q.rout, 0), row_after = __shfl_sync(kFull, q.rout, 1);
-    uint32_t ids[kLaneElems];
-    double vs[kLaneElems];
+    uint32_t ids[K];
+    double vs[K];
 #pragma unroll
-    for (int j = 0; j < kLaneElems; ++j) {
+    for (int j = 0; j < K; ++j) {
         const uint4& u4 = q.id[j >> 2];
         ids[j] = (j & 3) == 0 ? u4.x : (j & 3) == 1 ? u4.y : (j & 3) == 2 ? u4.z : u4.w;
         vs[j] = (j & 1) ? q.d[j >> 1].y : q.d[j >> 1].x;
@@ -144,7 +150,7 @@ __device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw,
     const int rf = (int)(ids[0] >> 16) & (S - 1);
     int rl = rf;
 #pragma unroll
-    for (int j = 1; j < kLaneElems; ++j)
+    for (int j = 1; j < K; ++j)
         if (j < nv) rl = (int)(ids[j] >> 16) & (S - 1);
     const int rl_prev = __shfl_up_sync(kFull, rl, 1);
     const int nv_prev = __shfl_up_sync(kFull, nv, 1);
@@ -163,7 +169,7 @@ __device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw,
     double pf = 0.0, pl = 0.0, acc = 0.0;
     int cur = -1;
 #pragma unroll
-    for (int j = 0; j < kLaneElems; ++j) {
+    for (int j = 0; j < K; ++j) {
         if (j < nv) {
             const int r = (int)(ids[j] >> 16) & (S - 1);
             if (r != cur) {
@@ -227,7 +233,8 @@ __device__ __forceinline__ void dense_oct(const Oct& q, int S, const double* xw,
 
 // win_ptr[2w] = the window's first unit, win_ptr[2w+1] = its first dense
 // unit, win_ptr[2w+2] = the next window's first unit.
-__global__ void __launch_bounds__(kCsbNT, kCsbOcc) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
+template <int NT, int K>
+__global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
                                                      const int* __restrict__ win_ptr, const int4* __restrict__ units,
                                                      int nwin, int S, int nor, int noc, const double* __restrict__ x,
                                                      double* __restrict__ y, const double* nsq_in, int* status) {
@@ -258,18 +265,18 @@ __global__ void __launch_bounds__(kCsbNT, kCsbOcc) k_csb_spmv(const uint32_t* __
                 if (cnt & 1) xs[b][cnt - 1] = __ldg(x + c0 + cnt - 1);
             }
         } else {
-            for (int i = tid; i < cnt; i += kCsbNT) xs[b][i] = __ldg(x + c0 + i);
+            for (int i = tid; i < cnt; i += NT) xs[b][i] = __ldg(x + c0 + i);
             if (tid == 0) mbar_arrive(&bar[b]);
         }
     };
     const int lane = tid & 31, warp = tid >> 5;
     for (int w = blockIdx.x; w < nwin; w += gridDim.x) {
         const int us = __ldg(win_ptr + 2 * w), u0 = __ldg(win_ptr + 2 * w + 1), u1 = __ldg(win_ptr + 2 * w + 2);
-        for (int i = tid; i < S; i += kCsbNT) ys[i] = 0.0;
+        for (int i = tid; i < S; i += NT) ys[i] = 0.0;
         if (u0 < u1) stage(u0, 0);
         __syncthreads();  // ys zeroed
         // sparse units: one per warp, x gathered through L1 / L2
-        for (int u = us + warp; u < u0; u += kCsbNT / 32) {
+        for (int u = us + warp; u < u0; u += NT / 32) {
             const int4 un = __ldg(units + u);
             const double* xw = x + un.z;
             for (int k = un.x + lane; k < un.y; k += 32) {
@@ -286,17 +293,18 @@ __global__ void __launch_bounds__(kCsbNT, kCsbOcc) k_csb_spmv(const uint32_t* __
             // row-major unit: warp chunks of kChunk elements; the first
             // chunk's loads are in flight while the x window lands
             const int4 un = __ldg(units + u);
-            constexpr int kStep = (kCsbNT / 32) * kChunk;
+            constexpr int kChunk = 32 * K;
+            constexpr int kStep = (NT / 32) * kChunk;
             int k = un.x + warp * kChunk;
-            Oct q = load_oct(ind, data, k, un.x, un.y, S, lane);
+            Oct<K> q = load_oct<K>(ind, data, k, un.x, un.y, S, lane);
             ok = mbar_wait_bounded(&bar[b], uses[b] & 1u, status);
             uses[b]++;
             if (!__syncthreads_and(ok)) break;
             const double* xw = xs[b];
             while (k < un.y) {
-                dense_oct(q, S, xw, ys, lane);
+                dense_oct<K>(q, S, xw, ys, lane);
                 k += kStep;
-                if (k < un.y) q = load_oct(ind, data, k, un.x, un.y, S, lane);
+                if (k < un.y) q = load_oct<K>(ind, data, k, un.x, un.y, S, lane);
             }
         }
         if (!ok) {
@@ -309,7 +317,7 @@ __global__ void __launch_bounds__(kCsbNT, kCsbOcc) k_csb_spmv(const uint32_t* __
         // an unconsumed prefetch cannot exist: the last unit's stage was waited
         __syncthreads();
         const int r0 = w * S;
-        for (int i = tid; i < S && r0 + i < nor; i += kCsbNT) {
+        for (int i = tid; i < S && r0 + i < nor; i += NT) {
             const double v = ys[i];
             y[r0 + i] = e != 0 ? scale_pow2(v, e) : v;
         }
@@ -489,11 +497,17 @@ int csb_window(int nor, int beta, int sm_count) {
 
 cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* win_ptr, const int* units, int nwin,
                             int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
-                            int sm_count, cudaStream_t st) {
+                            int sm_count, cudaStream_t st, int variant) {
     if (nwin <= 0) return cudaSuccess;
-    int grid = std::min(nwin, sm_count * kCsbOcc);
-    k_csb_spmv<<<grid, kCsbNT, 0, st>>>(ind, data, win_ptr, reinterpret_cast<const int4*>(units), nwin, S, nor, noc,
-                                        x, y, nsq_in, status);
+    const int4* un = reinterpret_cast<const int4*>(units);
+    const int nt = (variant & 2) ? 256 : 128;
+    const int grid = std::min(nwin, sm_count * (kCsbThreadsPerSM / nt));
+    switch (variant & 3) {
+        case 1: k_csb_spmv<128, 8><<<grid, 128, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        case 2: k_csb_spmv<256, 4><<<grid, 256, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        case 3: k_csb_spmv<256, 8><<<grid, 256, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        default: k_csb_spmv<128, 4><<<grid, 128, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+    }
     return cudaGetLastError();
 }
 

@@ -227,7 +227,8 @@ bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<doubl
                        std::vector<double>& kdata);
 cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* win_ptr, const int* units, int nwin,
                             int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
-                            int sm_count, cudaStream_t st);
+                            int sm_count, cudaStream_t st, int variant = 0);
+constexpr int kCsbVariants = 4;
 
 // coh.cu: CO-H (BlockCOH.hpp) host build and SpMV
 int coh_build_host(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,

@@ -77,6 +77,13 @@ struct pwmgpu_matrix {
     int l1 = 0;
     float tune_ms[2] = {0.f, 0.f};
     int power_mode = PWMGPU_POWER_AUTO;
+    // format autotuner (PWMGPU_FMT_AUTO handles, tuned on every load): the
+    // format whose FP64 SpMV runs (-1: the handle's own), the CSB kernel
+    // variant, and what the tuner saw
+    bool auto_fmt = false;
+    int tuned_fmt = -1;
+    int csb_var = 0;
+    pwmgpu_tuning tuning{};
     MliPlan P;
     // lane-interleaved FP32 / BF16 copies of the values (lazy)
     float* val32 = nullptr;
@@ -147,6 +154,22 @@ struct pwmgpu_matrix {
     float* fy = nullptr;
     size_t fvec_cap = 0;
 
+    void release_csb() {
+        pwmgpu::dfree(csb.ind);
+        pwmgpu::dfree(csb.data);
+        pwmgpu::dfree(csb.blk_ptr);
+        pwmgpu::dfree(csb.win_ptr);
+        pwmgpu::dfree(csb.units);
+        csb = decltype(csb)();
+    }
+    void release_coh() {
+        pwmgpu::dfree(coh.d_parts);
+        pwmgpu::dfree(coh.d_blocks);
+        pwmgpu::dfree(coh.row_jump);
+        pwmgpu::dfree(coh.col_jump);
+        pwmgpu::dfree(coh.data);
+        coh = decltype(coh)();
+    }
     void release_matrix() {
         pwmgpu::dfree(M.row_start);
         pwmgpu::dfree(M.col);
@@ -161,18 +184,10 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(P.valp);
         P = MliPlan();
         pwmgpu::dfree(val32);
-        pwmgpu::dfree(csb.ind);
-        pwmgpu::dfree(csb.data);
-        pwmgpu::dfree(csb.blk_ptr);
-        pwmgpu::dfree(csb.win_ptr);
-        pwmgpu::dfree(csb.units);
-        csb = decltype(csb)();
-        pwmgpu::dfree(coh.d_parts);
-        pwmgpu::dfree(coh.d_blocks);
-        pwmgpu::dfree(coh.row_jump);
-        pwmgpu::dfree(coh.col_jump);
-        pwmgpu::dfree(coh.data);
-        coh = decltype(coh)();
+        release_csb();
+        release_coh();
+        tuned_fmt = -1;
+        tuning = pwmgpu_tuning{};
         pipe.K = 0;
         pipe.rec.clear();
         if (valbf) cudaFree(valbf);

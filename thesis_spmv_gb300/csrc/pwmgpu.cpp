@@ -7,6 +7,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <chrono>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -150,6 +154,14 @@ int build_format(pwmgpu_matrix* m) {
 // faster.  The variants compute the same bits; only the shared-memory / L1
 // split and the resident CTA count differ (a Poisson-like matrix gains from
 // more CTAs, gathers spread over a large x from more L1).
+void apply_merge_variant(pwmgpu_matrix* m, int v) {
+    m->l1 = v;
+    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, v);
+    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, v);
+    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, v);
+    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, v);
+}
+
 int tune(pwmgpu_matrix* m) {
     const MergeGeom g = merge_geometry(kCfgF64, 0);
     if (m->num_tiles < 8 * g.occ * g.w * m->sm_count) return PWMGPU_OK;
@@ -188,12 +200,7 @@ int tune(pwmgpu_matrix* m) {
     int best = 0;  // another variant only for a clear (3 %) gain
     for (int c = 1; c < 4; ++c)
         if (ms[c] < 0.97f * ms[best]) best = c;
-    const int v = cand[best] | c16;
-    m->l1 = v;
-    m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, v);
-    m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, v);
-    m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, v);
-    m->pgridbf = power_persistent_grid(kCfgBF16, m->num_tiles, m->sm_count, v);
+    apply_merge_variant(m, cand[best] | c16);
     return PWMGPU_OK;
 }
 
@@ -234,8 +241,8 @@ int build_col16(pwmgpu_matrix* m) {
     return PWMGPU_OK;
 }
 
-int build_plan(pwmgpu_matrix* m) {
-    if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
+// The merge-path plan (and, with run_tuner, the load-time launch tuner).
+int build_merge(pwmgpu_matrix* m, bool run_tuner) {
     const long long total = (long long)m->M.nor + m->M.nnz;
     const MergeGeom g = merge_geometry(m->cfg);
     m->tm = g.wm;
@@ -278,7 +285,15 @@ int build_plan(pwmgpu_matrix* m) {
                                                                            16LL * m->sm_count)) + 64));
     CU(cudaStreamSynchronize(m->stream));
     m->loaded = true;
-    return tune(m);
+    return run_tuner ? tune(m) : PWMGPU_OK;
+}
+
+int build_auto(pwmgpu_matrix* m);
+
+int build_plan(pwmgpu_matrix* m) {
+    if (m->auto_fmt) return build_auto(m);
+    if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
+    return build_merge(m, true);
 }
 }  // namespace pwmgpu
 namespace {
@@ -329,12 +344,12 @@ int check_sizes(long long nor, long long noc, long long nnz) {
 namespace {
 
 // y = 2^e(nsq_in) A x with the CSB or CO-H kernel (nsq_in null: e = 0).
-int spmv_format(pwmgpu_matrix* m, const double* dx, double* dy, const double* nsq_in) {
+int spmv_format(pwmgpu_matrix* m, int fmt, const double* dx, double* dy, const double* nsq_in) {
     if (m->M.nor == 0) return PWMGPU_OK;
-    if (m->format == PWMGPU_FMT_CSB) {
+    if (fmt == PWMGPU_FMT_CSB) {
         const auto& c = m->csb;
         CU(launch_csb_spmv(c.ind, c.data, c.win_ptr, c.units, c.nwin, c.S, m->M.nor, m->M.noc, dx, dy, nsq_in,
-                           m->status, m->sm_count, m->stream));
+                           m->status, m->sm_count, m->stream, m->csb_var));
     } else {
         const auto& c = m->coh;
         CU(launch_coh_spmv(c.d_parts, c.parts, c.d_blocks, c.row_jump, c.col_jump, c.data, dx, dy, nsq_in,
@@ -343,8 +358,15 @@ int spmv_format(pwmgpu_matrix* m, const double* dx, double* dy, const double* ns
     return PWMGPU_OK;
 }
 
+// The format whose FP64 SpMV a handle runs: its own, or the autotuner's
+// choice on a PWMGPU_FMT_AUTO handle.
+int fp64_format(const pwmgpu_matrix* m) {
+    if (m->format != PWMGPU_FMT_MERGE) return m->format;
+    return m->tuned_fmt > 0 ? m->tuned_fmt : PWMGPU_FMT_MERGE;
+}
+
 int spmv_f64(pwmgpu_matrix* m, const double* dx, double* dy) {
-    if (m->format != PWMGPU_FMT_MERGE) return spmv_format(m, dx, dy, nullptr);
+    if (fp64_format(m) != PWMGPU_FMT_MERGE) return spmv_format(m, fp64_format(m), dx, dy, nullptr);
     if (m->num_tiles == 0) return PWMGPU_OK;
     CU(launch_merge_spmv(kCfgF64, kModeSpmv, m->M, m->P.valp, m->P, m->grid, dx, dy, m->carries, nullptr, m->status,
                          m->stream, m->l1));
@@ -402,12 +424,12 @@ bool use_fused(const pwmgpu_matrix* m, int pgrid) {
 int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
     if (it <= 0 || m->M.nor == 0) return PWMGPU_OK;
     TRY(ensure_nsq(m, (size_t)it + 1));
-    if (m->format != PWMGPU_FMT_MERGE) {
+    if (fp64_format(m) != PWMGPU_FMT_MERGE) {
         // the format's SpMV (with the rescale) and the row-pass norm per step
         for (int k = 0; k < it; ++k) {
             const double* in = (k % 2 == 0) ? dx : dy;
             double* out = (k % 2 == 0) ? dy : dx;
-            TRY(spmv_format(m, in, out, k ? m->nsq + k : nullptr));
+            TRY(spmv_format(m, fp64_format(m), in, out, k ? m->nsq + k : nullptr));
             CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, m->nsq + k + 1,
                                      dot_grid(m->M.nor, m->sm_count), m->stream));
         }
@@ -902,10 +924,12 @@ int pwmgpu_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes) {
 int pwmgpu_create(int format, int partitions, pwmgpu_matrix** out) {
     if (!out) return fail(PWMGPU_ERR_INVALID, "null output handle");
     *out = nullptr;
-    if (format != PWMGPU_FMT_MERGE && format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH)
+    if (format != PWMGPU_FMT_MERGE && format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH &&
+        format != PWMGPU_FMT_AUTO)
         return fail(PWMGPU_ERR_INVALID, "unknown format %d", format);
     pwmgpu_matrix* m = new pwmgpu_matrix();
-    m->format = format;
+    m->auto_fmt = format == PWMGPU_FMT_AUTO;
+    m->format = m->auto_fmt ? PWMGPU_FMT_MERGE : format;
     m->partitions = partitions > 0 ? partitions : 1;
     int rc = PWMGPU_OK;
     do {
@@ -1311,7 +1335,7 @@ int pwmgpu_mv(pwmgpu_matrix* m, const double* x, double* y) {
     if (m->M.nor == 0) return PWMGPU_OK;
     if (!y || (m->M.noc > 0 && !x)) return fail(PWMGPU_ERR_INVALID, "null vector");
     TRY(ensure_vectors(m));
-    if (m->format == PWMGPU_FMT_MERGE) {
+    if (fp64_format(m) == PWMGPU_FMT_MERGE) {
         int rc = plan_pipeline(m);
         if (rc != PWMGPU_OK) return rc;
         if (m->pipe.K > 0) return mv_pipelined(m, x, y);
@@ -1590,6 +1614,238 @@ int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes, int32_t* gat
     const bool merge = m->format == PWMGPU_FMT_MERGE;
     if (column_bytes) *column_bytes = merge && m->P.colp16 ? 2 : 4;
     if (gathers_bypass_l1) *gathers_bypass_l1 = merge && (m->l1 & 4) ? 1 : 0;
+    return PWMGPU_OK;
+}
+
+}  // extern "C"
+
+// ---- format autotuner (PWMGPU_FMT_AUTO) ------------------------------------
+namespace pwmgpu {
+namespace {
+
+struct TuneChoice {
+    int fmt = PWMGPU_FMT_MERGE;
+    int csb_var = 0;
+    int merge_var = 0;
+};
+using ClassKey = std::array<int32_t, 7>;
+std::mutex g_tune_mu;
+std::map<ClassKey, TuneChoice> g_tune_table;  // one entry per matrix class, process-wide
+
+void class_key_of(const pwmgpu_matrix_stats& st, int sm_count, int32_t* key) {
+    auto flog2 = [](double v) { return v > 0.0 ? (int32_t)std::floor(std::log2(v)) : -1; };
+    const double cv_rows = st.rows_avg > 0.0 ? std::sqrt(std::max(st.rows_var, 0.0)) / st.rows_avg : 0.0;
+    const double cv_blocks = st.block_avg > 0.0 ? std::sqrt(std::max(st.block_var, 0.0)) / st.block_avg : 0.0;
+    key[0] = flog2((double)st.size);
+    key[1] = st.rows_avg > 0.0 ? (int32_t)std::floor(2.0 * std::log2(st.rows_avg)) : -1;
+    key[2] = flog2(1.0 + 8.0 * cv_rows);
+    key[3] = flog2(1.0 + cv_blocks);
+    key[4] = st.balanced;
+    key[5] = flog2(1.0 + (double)st.max_row_nnz);
+    key[6] = sm_count;
+}
+
+// ms per FP64 SpMV of the handle with format `fmt` (x = 0: the kernels'
+// time does not depend on the values): two warm-ups, then 8 timed on the
+// handle's stream.
+int time_format(pwmgpu_matrix* m, int fmt, float* ms) {
+    TRY(ensure_vectors(m));
+    CU(cudaMemsetAsync(m->dx, 0, sizeof(double) * (size_t)std::max(m->M.nor, m->M.noc), m->stream));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CU(cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    int rc = e == cudaSuccess ? PWMGPU_OK : fail(PWMGPU_ERR_CUDA, "cudaEventCreate: %s", cudaGetErrorString(e));
+    const int saved = m->tuned_fmt;
+    m->tuned_fmt = fmt;
+    for (int r = 0; r < 10 && rc == PWMGPU_OK; ++r) {
+        if (r == 2 && (e = cudaEventRecord(e0, m->stream)) != cudaSuccess) rc = fail(PWMGPU_ERR_CUDA, "event");
+        if (rc == PWMGPU_OK) rc = spmv_f64(m, m->dx, m->dy);
+    }
+    m->tuned_fmt = saved;
+    if (rc == PWMGPU_OK) e = cudaEventRecord(e1, m->stream);
+    if (rc == PWMGPU_OK && e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (rc == PWMGPU_OK && e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    if (rc == PWMGPU_OK && e != cudaSuccess) rc = fail(PWMGPU_ERR_CUDA, "format timing: %s", cudaGetErrorString(e));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms /= 8.f;
+    TRY(rc);
+    return check_status(m);
+}
+
+// Build one of the CSB / CO-H formats beside the CRS arrays (still on the
+// device); the CO-H candidate gets a GPU partition count: a warp per
+// partition, at least 32 per SM, about 2000 rows each.
+int build_candidate(pwmgpu_matrix* m, int fmt) {
+    const int saved_fmt = m->format, saved_parts = m->partitions;
+    m->format = fmt;
+    if (fmt == PWMGPU_FMT_COH) m->partitions = std::max(32 * m->sm_count, (m->M.nor + 1999) / 2000);
+    const int rc = build_format(m);
+    m->format = saved_fmt;
+    m->partitions = saved_parts;
+    m->loaded = false;
+    return rc;
+}
+
+}  // namespace
+
+int build_auto(pwmgpu_matrix* m) {
+    const auto t0 = std::chrono::steady_clock::now();
+    pwmgpu_tuning T{};
+    T.format = PWMGPU_FMT_MERGE;
+    m->format = PWMGPU_FMT_MERGE;
+    m->tuned_fmt = -1;
+    m->csb_var = 0;
+    // matrices below the merge tuner's threshold (and non-square ones: the
+    // reference's CSB indexes blocks for square matrices) run merge, untimed
+    const MergeGeom g = merge_geometry(kCfgF64, 0);
+    const long long tiles = ((long long)m->M.nor + m->M.nnz + g.wm - 1) / g.wm;
+    if (m->M.nor == 0 || m->M.nnz == 0 || m->M.nor != m->M.noc || tiles < 8LL * g.occ * g.w * m->sm_count) {
+        TRY(build_merge(m, true));
+        T.merge_variant = m->l1;
+        m->tuning = T;
+        return PWMGPU_OK;
+    }
+    // class key from the statistics of the CRS arrays (still on the device)
+    pwmgpu_matrix_stats st{};
+    m->loaded = true;  // the statistics want a loaded handle
+    int rc = pwmgpu_stats(m, &st);
+    m->loaded = false;
+    TRY(rc);
+    ClassKey key{};
+    class_key_of(st, m->sm_count, key.data());
+    std::copy(key.begin(), key.end(), T.class_key);
+    TuneChoice choice;
+    bool hit = false;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_table.find(key);
+        if (it != g_tune_table.end()) {
+            choice = it->second;
+            hit = true;
+        }
+    }
+    if (hit) {
+        T.cache_hit = 1;
+        if (choice.fmt != PWMGPU_FMT_MERGE) TRY(build_candidate(m, choice.fmt));
+        TRY(build_merge(m, false));
+        apply_merge_variant(m, choice.merge_var | (m->P.colp16 ? 2 : 0));
+    } else {
+        T.timed = 1;
+        // CSB: all four kernel variants
+        TRY(build_candidate(m, PWMGPU_FMT_CSB));
+        m->loaded = true;
+        for (int v = 0; v < kCsbVariants; ++v) {
+            m->csb_var = v;
+            TRY(time_format(m, PWMGPU_FMT_CSB, &T.csb_ms[v]));
+        }
+        m->loaded = false;
+        // CO-H
+        TRY(build_candidate(m, PWMGPU_FMT_COH));
+        m->loaded = true;
+        TRY(time_format(m, PWMGPU_FMT_COH, &T.coh_ms));
+        // merge: plan and launch-variant tuner, then the same timing
+        TRY(build_merge(m, true));
+        TRY(time_format(m, PWMGPU_FMT_MERGE, &T.merge_ms));
+        choice.merge_var = m->l1 & ~2;  // the column width is the plan's, not a choice
+        float best = T.merge_ms;
+        for (int v = 0; v < kCsbVariants; ++v)
+            if (T.csb_ms[v] < best) {
+                best = T.csb_ms[v];
+                choice.fmt = PWMGPU_FMT_CSB;
+                choice.csb_var = v;
+            }
+        if (T.coh_ms < best) {
+            best = T.coh_ms;
+            choice.fmt = PWMGPU_FMT_COH;
+            choice.csb_var = 0;
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_table[key] = choice;
+    }
+    // keep the chosen format's arrays (and the merge plan); drop the others
+    if (choice.fmt != PWMGPU_FMT_CSB) m->release_csb();
+    if (choice.fmt != PWMGPU_FMT_COH) m->release_coh();
+    m->tuned_fmt = choice.fmt;
+    m->csb_var = choice.fmt == PWMGPU_FMT_CSB ? choice.csb_var : 0;
+    T.format = choice.fmt;
+    T.csb_variant = m->csb_var;
+    T.merge_variant = m->l1;
+    T.tune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    m->tuning = T;
+    m->loaded = true;
+    return PWMGPU_OK;
+}
+
+}  // namespace pwmgpu
+
+extern "C" {
+
+int pwmgpu_tuning_info(const pwmgpu_matrix* m, pwmgpu_tuning* out) {
+    if (!m || !out) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null handle or output");
+    if (!m->loaded) return pwmgpu::fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (!m->auto_fmt) return pwmgpu::fail(PWMGPU_ERR_STATE, "not a PWMGPU_FMT_AUTO handle");
+    *out = m->tuning;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_class_key(const pwmgpu_matrix_stats* st, int32_t sm_count, int32_t key[7]) {
+    if (!st || !key) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null statistics or key");
+    pwmgpu::class_key_of(*st, sm_count, key);
+    return PWMGPU_OK;
+}
+
+int pwmgpu_tuner_reset(void) {
+    std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
+    pwmgpu::g_tune_table.clear();
+    return PWMGPU_OK;
+}
+
+int pwmgpu_tuner_size(void) {
+    std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
+    return (int)pwmgpu::g_tune_table.size();
+}
+
+int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant) {
+    if (!key) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null key");
+    if (format != PWMGPU_FMT_MERGE && format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH)
+        return pwmgpu::fail(PWMGPU_ERR_INVALID, "format must be merge, CSB or CO-H");
+    if (csb_variant < 0 || csb_variant >= pwmgpu::kCsbVariants)
+        return pwmgpu::fail(PWMGPU_ERR_INVALID, "CSB variant 0..3");
+    if (merge_variant != 0 && merge_variant != 1 && merge_variant != 4 && merge_variant != 5)
+        return pwmgpu::fail(PWMGPU_ERR_INVALID, "merge variant 0, 1, 4 or 5");
+    pwmgpu::ClassKey k{};
+    std::copy(key, key + 7, k.begin());
+    pwmgpu::TuneChoice c;
+    c.fmt = format;
+    c.csb_var = format == PWMGPU_FMT_CSB ? csb_variant : 0;
+    c.merge_var = merge_variant;
+    std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
+    pwmgpu::g_tune_table[k] = c;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices) {
+    if (max < 0 || (max > 0 && (!keys || !choices)))
+        return -pwmgpu::fail(PWMGPU_ERR_INVALID, "null output arrays or negative count");
+    std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
+    int n = 0;
+    for (const auto& kv : pwmgpu::g_tune_table) {
+        if (n >= max) break;
+        std::copy(kv.first.begin(), kv.first.end(), keys + 7 * (size_t)n);
+        choices[3 * (size_t)n] = kv.second.fmt;
+        choices[3 * (size_t)n + 1] = kv.second.csb_var;
+        choices[3 * (size_t)n + 2] = kv.second.merge_var;
+        ++n;
+    }
+    return n;
+}
+
+int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant) {
+    if (!m) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null handle");
+    if (variant < 0 || variant >= pwmgpu::kCsbVariants) return pwmgpu::fail(PWMGPU_ERR_INVALID, "CSB variant 0..3");
+    if (m->format != PWMGPU_FMT_CSB) return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB handle");
+    m->csb_var = variant;
     return PWMGPU_OK;
 }
 

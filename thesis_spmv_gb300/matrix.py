@@ -14,7 +14,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import (FMT_COH, FMT_CSB, FMT_MERGE, LOWFMT_AUTO, LOWFMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32,  # noqa: F401
+from ._lib import (FMT_AUTO, FMT_COH, FMT_CSB, FMT_MERGE, LOWFMT_AUTO, LOWFMT_MERGE, POWER_AUTO, POWER_FUSED, POWER_MULTI, PREC_F32,  # noqa: F401
                    PREC_F64, PREC_MIXED, SolveInfo, check)
 
 _I32 = np.int32
@@ -278,6 +278,10 @@ class CudaSparseMatrix:
         return a.value, b.value, c.value
 
 
+    def set_csb_variant(self, variant):
+        """CSB kernel variant (CSB handles): bit 0 = 8 elements per lane, bit 1 = 256 threads per CTA."""
+        check(_lib.lib().pwmgpu_set_csb_variant(self._h, int(variant)), "pwmgpu_set_csb_variant")
+
     def getCSB(self):
         """The CSB arrays (CSB.hpp:464-567) of a CSBCuda handle: dict(ind,
         data, blk_ptr, beta, block_bits, hb, vb)."""
@@ -327,8 +331,63 @@ class COHCuda(CudaSparseMatrix):
     FORMAT = FMT_COH
 
 
+class AutoCuda(CudaSparseMatrix):
+    """Format-autotuned GPU matrix (method 15, no counterpart in the
+    reference): the merge-path plan plus whichever of merge, CSB or CO-H (and
+    kernel variant) the class-keyed tuner found fastest for mv /
+    powerIteration."""
+    FORMAT = FMT_AUTO
+
+    def tuning(self):
+        """dict of pwmgpu_tuning_info: chosen format and variants, cache hit,
+        class key and the timings (ms per SpMV) of every candidate."""
+        t = _lib.Tuning()
+        check(_lib.lib().pwmgpu_tuning_info(self._h, C.byref(t)), "pwmgpu_tuning_info")
+        return dict(format={FMT_MERGE: "merge", FMT_CSB: "csb", FMT_COH: "coh"}[t.format],
+                    csb_variant=t.csb_variant, merge_variant=t.merge_variant, cache_hit=bool(t.cache_hit),
+                    timed=bool(t.timed), class_key=list(t.class_key), merge_ms=t.merge_ms,
+                    csb_ms=list(t.csb_ms), coh_ms=t.coh_ms, tune_seconds=t.tune_seconds)
+
+
+def tuner_reset():
+    """Forget the autotuner's recorded class choices."""
+    check(_lib.lib().pwmgpu_tuner_reset(), "pwmgpu_tuner_reset")
+
+
+def tuner_size():
+    """Number of matrix classes the autotuner has recorded."""
+    return int(_lib.lib().pwmgpu_tuner_size())
+
+
+def tuner_record(key, fmt, csb_variant=0, merge_variant=0):
+    """Record a class choice (fmt "merge" / "csb" / "coh") in the autotuner's table."""
+    k = (C.c_int32 * 7)(*[int(v) for v in key])
+    f = {"merge": FMT_MERGE, "csb": FMT_CSB, "coh": FMT_COH}[fmt]
+    check(_lib.lib().pwmgpu_tuner_record(k, f, int(csb_variant), int(merge_variant)), "pwmgpu_tuner_record")
+
+
+def tuner_entries():
+    """The autotuner's table: list of (class key, format, csb_variant, merge_variant)."""
+    n = tuner_size()
+    keys = (C.c_int32 * (7 * max(n, 1)))()
+    ch = (C.c_int32 * (3 * max(n, 1)))()
+    got = _lib.lib().pwmgpu_tuner_entries(n, keys, ch)
+    if got < 0:
+        check(-got, "pwmgpu_tuner_entries")
+    names = {FMT_MERGE: "merge", FMT_CSB: "csb", FMT_COH: "coh"}
+    return [(list(keys[7 * i:7 * i + 7]), names[ch[3 * i]], ch[3 * i + 1], ch[3 * i + 2]) for i in range(got)]
+
+
+def class_key(stats, sm_count):
+    """The autotuner's class key of a statistics dict (CudaSparseMatrix.stats())."""
+    st = _lib.MatrixStats(**{k: stats[k] for k in (f[0] for f in _lib.MatrixStats._fields_)})
+    key = (C.c_int32 * 7)()
+    check(_lib.lib().pwmgpu_class_key(C.byref(st), int(sm_count), key), "pwmgpu_class_key")
+    return list(key)
+
+
 def selectType(method, threads=1):
     """Util/DriverUtil.hpp:38-84 selectType for the GPU method numbers
-    (12 merge-path CRS, 13 CSB, 14 CO-H); None for any other number, like the
-    reference's NULL."""
-    return {12: CRSCuda, 13: CSBCuda, 14: COHCuda}.get(int(method), lambda t: None)(threads)
+    (12 merge-path CRS, 13 CSB, 14 CO-H, 15 autotuned); None for any other
+    number, like the reference's NULL."""
+    return {12: CRSCuda, 13: CSBCuda, 14: COHCuda, 15: AutoCuda}.get(int(method), lambda t: None)(threads)
