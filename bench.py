@@ -208,6 +208,46 @@ IRREGULAR = dict(n=4194304, seed=20261203, length_dist=0, mean_len=16.0, sigma=1
                  band_permille=300, band_half=4096)
 
 
+def autotune_report(pwm, torch, stream, load, load_same_class, x, y, B):
+    """The format autotuner (PWMGPU_FMT_AUTO, selectType method 15) on one
+    matrix: the first load of its class times every candidate (merge launch
+    variants, CSB lanes x threads variants, CO-H) and records the fastest;
+    a second matrix of the same class takes the recorded choice.  Reports the
+    choice, the candidates' ms per SpMV, the load + tuning wall time of both
+    loads, and the SpMV through the tuned handle."""
+    out = {}
+    for tag, fn in (("first_of_class", load), ("same_class", load_same_class)):
+        A = pwm.AutoCuda(1)
+        A.set_stream(stream.cuda_stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn(A)
+        wall = time.perf_counter() - t0
+        t = A.tuning()
+        rec = {"load_and_tune_s": round(wall, 3), "format": t["format"], "csb_variant": t["csb_variant"],
+               "merge_variant": t["merge_variant"], "cache_hit": t["cache_hit"], "timed": t["timed"],
+               "class_key": t["class_key"]}
+        if t["timed"]:
+            rec["candidates_ms"] = {"merge": round(t["merge_ms"], 5), "coh": round(t["coh_ms"], 5),
+                                    **{"csb_v%d" % v: round(t["csb_ms"][v], 5) for v in range(4)}}
+        if tag == "first_of_class":
+            for _ in range(3):
+                A.mv_device(x.data_ptr(), y.data_ptr())
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(50):
+                A.mv_device(x.data_ptr(), y.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / 50
+            rec["spmv_ms"] = round(ms, 5)
+            rec["gb_s_crs_bytes"] = round(B / (ms * 1e-3) / 1e9, 2)
+        out[tag] = rec
+        del A
+    return out
+
+
 def irregular_and_solves(pwm, torch, dev, stream, args):
     """The irregular lognormal-row matrix (N = 4,194,304, generated on the
     device): FP64 SpMV GB/s, then power solves to 1e-10 relative
@@ -234,6 +274,7 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
     ms = e0.elapsed_time(e1) / steps
     out = {"irregular": {"workload": "lognormal_rows_n4194304_mean16_sigma1.2_band30pct", "N": N, "nnz": nnz,
                          "spmv_ms": round(ms, 5), "spmv_gb_s": round(B / (ms * 1e-3) / 1e9, 2),
+                         "spmv_gflop_s": round(2.0 * nnz / (ms * 1e-3) / 1e9, 2),
                          "frac_of_measured_hbm": round(B / (ms * 1e-3) / 1e9 / measured_peaks()[0], 4)}}
     # the same matrix in the CSB and CO-H formats (the reference's methods 9 and
     # 10): device SpMV time, GB/s on the CRS algorithmic bytes
@@ -255,6 +296,9 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
         del F
     out["irregular"]["formats"] = fm
     out["irregular"]["stats"] = M.stats()
+    out["irregular"]["autotuner"] = autotune_report(
+        pwm, torch, stream, lambda A: A.generateRandom(**IRREGULAR),
+        lambda A: A.generateRandom(**dict(IRREGULAR, seed=IRREGULAR["seed"] + 1)), x, y, B)
     x0 = np.random.default_rng(20261203).random(N)
     solves = {}
     lam = {}
@@ -564,6 +608,10 @@ def run_ours(args, world, rank, local):
             fms = f0.elapsed_time(f1) / 50
             formats[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
             del F
+        # the autotuner on this class: the 4096^2 grid, then a 4200 x 4096 grid
+        formats["autotuner"] = autotune_report(
+            pwm, torch, stream, lambda A: A.generatePoissonMatrix(grid_side, grid_side, 1),
+            lambda A: A.generatePoissonMatrix(grid_side + 104, grid_side, 1), dx, dy, B)
         formats_load = triplet_load(pwm, torch, dev, M, N, cpu=rank == 0 and world == 1 and not args.no_cpu)
 
     # ---- power method: 500 iterations (reference powerIteration semantics),
@@ -632,6 +680,7 @@ def run_ours(args, world, rank, local):
                      "frac": round(B / (ms * 1e-3) / 1e9 / peak, 4), "traffic": traffic,
                      "peak_source": peak_kind, "frac_of_nominal_8TBs": round(B / (ms * 1e-3) / 1e9 / NOMINAL_HBM_GBS, 4),
                      "algorithmic_bytes_per_launch": B, "timed": "k_merge_spmv + k_fix_runs (one SpMV)"},
+        "gflop_s": round(2.0 * nnz * world / (ms * 1e-3) / 1e9, 2),
         "e2e": ({"value": round(e2e_gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 8 * N,
                  "d2h_bytes_per_step": 8 * N, "ms_per_step": round(e2e_s * 1e3, 4),
                  "api": "pwmgpu_mv (host arrays, pinned)",

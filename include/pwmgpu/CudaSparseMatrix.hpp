@@ -103,6 +103,9 @@ template <typename T, typename int_type>
 using CSBCuda = CudaSparseMatrix<T, int_type, PWMGPU_FMT_CSB>;
 template <typename T, typename int_type>
 using BlockCOHCuda = CudaSparseMatrix<T, int_type, PWMGPU_FMT_COH>;
+// format autotuned per matrix class (pwmgpu_tuning_info on handle())
+template <typename T, typename int_type>
+using AutoCuda = CudaSparseMatrix<T, int_type, PWMGPU_FMT_AUTO>;
 
 }  // namespace pwm
 

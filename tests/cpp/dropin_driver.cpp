@@ -1,6 +1,7 @@
 // A driver in the shape of the reference's driver_poisson.cpp / test.cpp,
 // using the GPU classes through pwm::SparseMatrix only (methods 12, 13, 14
-// next to the reference's 1-10 in Util/DriverUtil.hpp:38-84 selectType).
+// and the autotuned 15, next to the reference's 1-10 in
+// Util/DriverUtil.hpp:38-84 selectType).
 //
 //   dropin_driver <method> <m> <n> <it> <out.bin>
 //
@@ -25,6 +26,7 @@ static pwm::SparseMatrix<double, I>* select_type(int method, int threads) {
         case 12: return new pwm::CRSCuda<double, I>(threads);
         case 13: return new pwm::CSBCuda<double, I>(threads);
         case 14: return new pwm::BlockCOHCuda<double, I>(threads);
+        case 15: return new pwm::AutoCuda<double, I>(threads);
         default: return nullptr;  // like selectType's NULL (DriverUtil.hpp:81-82)
     }
 }

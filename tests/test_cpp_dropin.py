@@ -1,12 +1,12 @@
 """The header-only C++ drop-in classes (include/pwmgpu/CudaSparseMatrix.hpp):
-pwm::CRSCuda / CSBCuda / BlockCOHCuda derive from the reference's
+pwm::CRSCuda / CSBCuda / BlockCOHCuda / AutoCuda derive from the reference's
 pwm::SparseMatrix and are used through that interface by a driver in the
 shape of the reference's drivers (tests/cpp/dropin_driver.cpp).
 
 CPU: the header and the driver compile against the real reference interface
 (Matrix/SparseMatrix.hpp, Matrix/Triplet.hpp) where the reference tree is
 present.  GPU: the driver, built against the interface stand-in, runs all
-three methods; its outputs match the oracle (mv rows within the row bound,
+four methods (15: the format autotuner); its outputs match the oracle (mv rows within the row bound,
 powerIteration within 1e-10, the triplet sorted like TripletToCRS)."""
 import os
 import shutil
@@ -58,7 +58,7 @@ def test_driver_builds_against_stand_in(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method", [12, 13, 14])
+@pytest.mark.parametrize("method", [12, 13, 14, 15])
 def test_driver_runs_through_the_interface(tmp_path, method):
     exe = _build_driver(tmp_path)
     m, n, it = 37, 23, 9
