@@ -146,7 +146,7 @@ int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out);
  * every candidate -- the merge kernels' 4 launch variants (shared-memory /
  * L1 carveout x gathers through or around L1), CSB with 4 or 8 elements
  * per lane and 128 or 256 threads per CTA, and CO-H with a warp per
- * partition (max(32 sm_count, nor / 2000) partitions) -- on a few SpMVs each
+ * partition (32 sm_count partitions) -- on a few SpMVs each
  * and records the fastest in a process-wide table; later matrices of the
  * class take the recorded choice without timing.  Matrices too small to time
  * (the merge tuner's threshold) run merge. */

@@ -19,11 +19,14 @@
 // rows from a warp prefix sum of the row jumps, staged in shared memory).  A
 // lane accumulates its runs of equal rows with one FMA per nonzero; a run
 // that crosses lanes is summed by the lane where it starts (lane order) and
-// one crossing the chunk end is carried.  A partition of at most kCohWinRows
-// rows accumulates its rows in a shared-memory window (written to y once at
-// the end); a larger one adds into y directly.  Rows are written by one lane
-// at a time and blocks in order: no atomics, a fixed summation order (per
-// row, Hilbert block order, as in the reference).
+// one crossing the chunk end is carried.  A partition adds into its own rows
+// of y (zeroed first; the read-modify-writes stay in L2).  The walk is
+// latency-bound, so residency is what counts: 8 CTAs of 4 warps per SM
+// (64 registers); an earlier shared-memory y window of 2048 rows per warp
+// capped residency at 3 CTAs per SM and was 1.66x slower on the 4096^2
+// stencil.  Rows are written by one lane at a time and blocks in order: no
+// atomics, a fixed summation order (per row, Hilbert block order, as in the
+// reference).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,7 +45,7 @@ namespace {
 
 constexpr int kCohK = 8;           // elements per lane per chunk
 constexpr int kCohWarps = 4;       // warps per CTA
-constexpr int kCohWinRows = 2048;  // rows of a warp's shared-memory y window
+constexpr int kCohOcc = 8;         // resident CTAs per SM (64 registers): 32 warps
 
 // BlockCOH.hpp:79-114 rowColToHilbert: index of cell (row, col) on the
 // Hilbert curve over a size x size grid.
@@ -63,7 +66,7 @@ int hilbert_index(int size, int row, int col) {
     return index;
 }
 
-__global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restrict__ parts, int nparts,
+__global__ void __launch_bounds__(32 * kCohWarps, kCohOcc) k_coh_spmv(const int4* __restrict__ parts, int nparts,
                                                              const int4* __restrict__ blocks,
                                                              const uint16_t* __restrict__ row_jump,
                                                              const uint16_t* __restrict__ col_jump,
@@ -80,9 +83,7 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
     __shared__ int multi_s[kCohWarps][32];
     __shared__ int carry_row_s[kCohWarps];
     __shared__ double carry_s[kCohWarps];
-    extern __shared__ double ywin_s[];  // kCohWarps x kCohWinRows
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    double* ywin = ywin_s + (size_t)w * kCohWinRows;
     int* rbuf = rbuf_s[w];
     int* frow = frow_s[w];
     int* crow = crow_s[w];
@@ -98,8 +99,7 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
         const int nb = __ldg(&parts[2 * p + 1].x);
         const int trs = pa.x, nrows = pa.y, bits = pa.z, b0 = pa.w;
         const int beta = 1 << bits;
-        const bool win = nrows <= kCohWinRows;
-        double* yp = win ? ywin : y + trs;  // the partition's rows
+        double* yp = y + trs;  // the partition's rows (no other warp writes them)
         for (int r = lane; r < nrows; r += 32) yp[r] = 0.0;
         __syncwarp();
         for (int b = b0; b < b0 + nb; ++b) {
@@ -237,8 +237,6 @@ __global__ void __launch_bounds__(32 * kCohWarps) k_coh_spmv(const int4* __restr
             if (lane == 0 && carry_row >= 0) yb[carry_row] = yb[carry_row] + (e != 0 ? scale_pow2(carry, e) : carry);
             __syncwarp();
         }
-        if (win)
-            for (int r = lane; r < nrows; r += 32) y[trs + r] = ywin[r];
         __syncwarp();
     }
 }
@@ -412,15 +410,9 @@ cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, con
                             const uint16_t* col_jump, const double* data, const double* x, double* y,
                             const double* nsq_in, int sm_count, cudaStream_t st) {
     if (nparts <= 0) return cudaSuccess;
-    constexpr int kWinBytes = kCohWarps * kCohWinRows * (int)sizeof(double);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_coh_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kWinBytes);
-        attr = true;
-    }
     long long grid = (nparts + kCohWarps - 1) / kCohWarps;
-    if (grid > (long long)sm_count * 16) grid = (long long)sm_count * 16;
-    k_coh_spmv<<<(int)grid, 32 * kCohWarps, kWinBytes, st>>>(reinterpret_cast<const int4*>(parts), nparts,
+    if (grid > (long long)sm_count * kCohOcc) grid = (long long)sm_count * kCohOcc;
+    k_coh_spmv<<<(int)grid, 32 * kCohWarps, 0, st>>>(reinterpret_cast<const int4*>(parts), nparts,
                                                     reinterpret_cast<const int4*>(blocks), row_jump, col_jump, data,
                                                     x, y, nsq_in);
     return cudaGetLastError();

@@ -1675,11 +1675,11 @@ int time_format(pwmgpu_matrix* m, int fmt, float* ms) {
 
 // Build one of the CSB / CO-H formats beside the CRS arrays (still on the
 // device); the CO-H candidate gets a GPU partition count: a warp per
-// partition, at least 32 per SM, about 2000 rows each.
+// partition, one per resident warp (32 per SM).
 int build_candidate(pwmgpu_matrix* m, int fmt) {
     const int saved_fmt = m->format, saved_parts = m->partitions;
     m->format = fmt;
-    if (fmt == PWMGPU_FMT_COH) m->partitions = std::max(32 * m->sm_count, (m->M.nor + 1999) / 2000);
+    if (fmt == PWMGPU_FMT_COH) m->partitions = 32 * m->sm_count;
     const int rc = build_format(m);
     m->format = saved_fmt;
     m->partitions = saved_parts;
