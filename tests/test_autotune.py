@@ -157,3 +157,42 @@ def test_auto_small_matrix_runs_merge(pwm):
     t = M.tuning()
     assert t["format"] == "merge" and not t["timed"] and not t["cache_hit"]
     _check_mv(M, A, 9)
+
+
+def _long_row_matrix(n, seed):
+    """Rows of very different lengths inside dense sub-squares: most rows hold
+    a few entries near the diagonal, every 97th row 200-900 entries within
+    +-30 columns, so mostly repeated coordinates (CRS keeps duplicates): in a
+    dense sub-square such a row is a chain over many lanes (the
+    segmented-scan branch) and longer than a warp's chunk (the atomic
+    branch); some rows are empty."""
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    for r in range(n):
+        if r % 13 == 5:
+            continue  # empty row
+        if r % 97 == 0:
+            k = int(rng.integers(200, 900))
+            lo, hi = max(0, r - 30), min(n, r + 31)
+            c = np.sort(rng.integers(lo, hi, k))  # with repeats
+        else:
+            c = np.unique(np.clip(r + rng.integers(-3, 4, int(rng.integers(1, 6))), 0, n - 1))
+        rows.append(np.full(c.size, r))
+        cols.append(c)
+    r = np.concatenate(rows).astype(np.int32)
+    c = np.concatenate(cols).astype(np.int32)
+    rs = np.zeros(n + 1, np.int32)
+    np.add.at(rs, r + 1, 1)
+    rs = np.cumsum(rs).astype(np.int32)
+    return O.CRSArrays(n, n, rs, c, rng.uniform(-1, 1, c.size))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_csb_long_rows_and_duplicates(pwm, variant):
+    A = _long_row_matrix(60000, 21)
+    M = pwm.CSBCuda(1)
+    M.loadCSR(A.nor, A.noc, A.row_start, A.col_ind, A.data)
+    M.set_csb_variant(variant)
+    for seed in (1, 2):
+        _check_mv(M, A, 30 + seed)
