@@ -15,14 +15,16 @@
 // the y window, then writes its rows of y once.  Dense units (at least
 // kDenseUnit elements) stage their S-column x window in shared memory with a
 // TMA bulk copy (double-buffered, mbarriers) and are taken by the whole CTA;
-// sparse units (a random matrix's blocks hold a few elements each) are taken
-// one per warp, gathering x through L1/L2 -- staging 8 KB of x for a handful
-// of elements would cost more than it saves -- and add with shared-memory
-// atomics.  y is written once per row and no CTA touches another's rows.
+// a window's sparse units (a random matrix's blocks hold a few elements
+// each) are merged into one "flat" unit taken by the whole CTA, gathering x
+// through L1/L2 by global column -- staging 8 KB of x for a handful of
+// elements would cost more than it saves.  y is written once per row and no
+// CTA touches another's rows.
 //
 // The device copy (csb_kernel_layout) keeps the blocks, their block-column
-// order and the Z-Morton order of the sub-squares, but stores each dense
-// unit row-major (rows ascending, columns ascending within a row, duplicates
+// order and the Z-Morton order of the dense sub-squares, stores each
+// window's flat unit row-major with a global column per element (kcol), and
+// stores each dense unit row-major (rows ascending, columns ascending within a row, duplicates
 // in build order) from a multiple of 4 elements: the order inside a
 // sub-square is free for y += A x, and on this GPU a shared-memory FP64
 // atomic add is a compare-and-swap loop that bounded the Z-ordered kernel.
@@ -45,6 +47,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -88,6 +91,7 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 template <int K>
 struct Oct {
     uint4 id[K / 4];
+    uint4 gc[K / 4];  // global columns (flat units only)
     double2 d[K / 2];
     int nv;    // valid elements (0..K)
     int rout;  // lane 0: row of the element before the chunk, lane 1: after it (-1: none)
@@ -95,25 +99,27 @@ struct Oct {
 
 // Lane `lane`'s elements of the chunk at k0 of unit [lo, hi), and the row of
 // the element just outside the chunk (lanes 0 and 1).
-template <int K>
-__device__ __forceinline__ Oct<K> load_oct(const uint32_t* __restrict__ ind, const double* __restrict__ data, int k0,
-                                        int lo, int hi, int S, int lane) {
+template <int K, bool GX>
+__device__ __forceinline__ Oct<K> load_oct(const uint32_t* __restrict__ ind, const int32_t* __restrict__ kcol,
+                                           const double* __restrict__ data, int k0, int lo, int hi, int S, int lane) {
     constexpr int kChunk = 32 * K;
     Oct<K> q;
     const int k = k0 + K * lane;
     q.nv = k < hi ? min(K, hi - k) : 0;
 #pragma unroll
     for (int i = 0; i < K / 4; ++i) {
-        q.id[i] = make_uint4(0u, 0u, 0u, 0u);
+        q.id[i] = q.gc[i] = make_uint4(0u, 0u, 0u, 0u);
         q.d[2 * i] = q.d[2 * i + 1] = make_double2(0.0, 0.0);
     }
     // k is a multiple of 4 and the arrays are padded past the last unit by 8
     const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
+    const uint4* cp = reinterpret_cast<const uint4*>(kcol + k);
     const double2* dp = reinterpret_cast<const double2*>(data + k);
 #pragma unroll
     for (int i = 0; i < K / 4; ++i)
         if (4 * i < q.nv) {
             q.id[i] = __ldg(ip + i);
+            if (GX) q.gc[i] = __ldg(cp + i);
             q.d[2 * i] = __ldg(dp + 2 * i);
             q.d[2 * i + 1] = __ldg(dp + 2 * i + 1);
         }
@@ -134,16 +140,19 @@ __device__ __forceinline__ Oct<K> load_oct(const uint32_t* __restrict__ ind, con
 // lane where a partial row ends adds the partials of its chain of lanes
 // (a few shuffles, or a segmented scan for long chains) -- atomically for
 // rows that cross the chunk, with a plain add otherwise.
-template <int K>
-__device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* xw, double* ys, int lane) {
+template <int K, bool GX>
+__device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* xw, const double* __restrict__ xg,
+                                          double* ys, int lane) {
     // the rows of the elements just before and after the chunk (-1: none)
     const int row_before = __shfl_sync(kFull, q.rout, 0), row_after = __shfl_sync(kFull, q.rout, 1);
-    uint32_t ids[K];
+    uint32_t ids[K], gcs[K];
     double vs[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         const uint4& u4 = q.id[j >> 2];
         ids[j] = (j & 3) == 0 ? u4.x : (j & 3) == 1 ? u4.y : (j & 3) == 2 ? u4.z : u4.w;
+        const uint4& g4 = q.gc[j >> 2];
+        gcs[j] = (j & 3) == 0 ? g4.x : (j & 3) == 1 ? g4.y : (j & 3) == 2 ? g4.z : g4.w;
         vs[j] = (j & 1) ? q.d[j >> 1].y : q.d[j >> 1].x;
     }
     const int nv = q.nv;
@@ -182,7 +191,8 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
                 cur = r;
                 acc = (r == rf && part_f) || (r == rl && part_l) ? 0.0 : ys[r];
             }
-            acc = fma(vs[j], xw[ids[j] & (uint32_t)(S - 1)], acc);
+            const double xv = GX ? __ldg(xg + gcs[j]) : xw[ids[j] & (uint32_t)(S - 1)];
+            acc = fma(vs[j], xv, acc);
         }
     }
     if (cur >= 0) {
@@ -234,7 +244,7 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
 // win_ptr[2w] = the window's first unit, win_ptr[2w+1] = its first dense
 // unit, win_ptr[2w+2] = the next window's first unit.
 template <int NT, int K>
-__global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const uint32_t* __restrict__ ind, const double* __restrict__ data,
+__global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const uint32_t* __restrict__ ind, const int32_t* __restrict__ kcol, const double* __restrict__ data,
                                                      const int* __restrict__ win_ptr, const int4* __restrict__ units,
                                                      int nwin, int S, int nor, int noc, const double* __restrict__ x,
                                                      double* __restrict__ y, const double* nsq_in, int* status) {
@@ -275,14 +285,15 @@ __global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const ui
         for (int i = tid; i < S; i += NT) ys[i] = 0.0;
         if (u0 < u1) stage(u0, 0);
         __syncthreads();  // ys zeroed
-        // sparse units: one per warp, x gathered through L1 / L2
-        for (int u = us + warp; u < u0; u += NT / 32) {
-            const int4 un = __ldg(units + u);
-            const double* xw = x + un.z;
-            for (int k = un.x + lane; k < un.y; k += 32) {
-                const uint32_t id = __ldg(ind + k);
-                const int r = (int)(id >> 16) & (S - 1), c = (int)(id & 0xFFFFu) & (S - 1);
-                atomicAdd(&ys[r], __ldg(data + k) * __ldg(xw + c));
+        // the window's sparse sub-squares as one flat row-major unit, x
+        // gathered through L1 / L2 by global column
+        if (u0 > us) {
+            const int4 un = __ldg(units + us);
+            constexpr int kChunk = 32 * K;
+            constexpr int kStep = (NT / 32) * kChunk;
+            for (int k = un.x + warp * kChunk; k < un.y; k += kStep) {
+                const Oct<K> q = load_oct<K, true>(ind, kcol, data, k, un.x, un.y, S, lane);
+                dense_oct<K, true>(q, S, nullptr, x, ys, lane);
             }
         }
         bool ok = true;
@@ -296,15 +307,15 @@ __global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const ui
             constexpr int kChunk = 32 * K;
             constexpr int kStep = (NT / 32) * kChunk;
             int k = un.x + warp * kChunk;
-            Oct<K> q = load_oct<K>(ind, data, k, un.x, un.y, S, lane);
+            Oct<K> q = load_oct<K, false>(ind, kcol, data, k, un.x, un.y, S, lane);
             ok = mbar_wait_bounded(&bar[b], uses[b] & 1u, status);
             uses[b]++;
             if (!__syncthreads_and(ok)) break;
             const double* xw = xs[b];
             while (k < un.y) {
-                dense_oct<K>(q, S, xw, ys, lane);
+                dense_oct<K, false>(q, S, xw, nullptr, ys, lane);
                 k += kStep;
-                if (k < un.y) q = load_oct<K>(ind, data, k, un.x, un.y, S, lane);
+                if (k < un.y) q = load_oct<K, false>(ind, kcol, data, k, un.x, un.y, S, lane);
             }
         }
         if (!ok) {
@@ -410,61 +421,92 @@ int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
     return 0;
 }
 
-// Device copy for k_csb_spmv from the built arrays: per window its sparse
-// units as built (Z-Morton order), then its dense units, each re-ordered
-// row-major (a stable sort by ind = local row << 16 | local column) from a
-// multiple of 4 elements; the gaps hold zeros and are never read as
-// elements.  units (4 ints per unit, win_ptr order) is rewritten to the new
-// ranges.  Windows are independent: filled by a few host threads.  Returns
-// false when the padded copy would not fit 32-bit element offsets.
-bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data,
-                       const std::vector<int>& win_ptr, std::vector<int>& units, std::vector<uint32_t>& kind,
-                       std::vector<double>& kdata) {
-    const int nunits = (int)(units.size() / 4);
+// Device copy for k_csb_spmv from the built arrays.  Per window: its sparse
+// units merged into one "flat" unit, row-major over the window (a stable
+// sort by (local row, global column)), with each element's global column in
+// kcol (x is gathered from global memory there); then its dense units, each
+// row-major (a stable sort by ind = local row << 16 | local column).  Every
+// unit starts on a multiple of 4 elements; the gaps hold zeros and are never
+// read as elements.  win_ptr and units (4 ints per unit: {lo, hi, c0, 0},
+// c0 = -1 for a flat unit) are rewritten: a window has at most one unit
+// before its first dense unit.  Windows are independent: filled by a few
+// host threads.  Returns false when the copy would not fit 32-bit element
+// offsets.
+bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data, int S,
+                       std::vector<int>& win_ptr, std::vector<int>& units, std::vector<uint32_t>& kind,
+                       std::vector<double>& kdata, std::vector<int32_t>& kcol) {
     const int nwin = (int)(win_ptr.size() / 2);
-    std::vector<int> dense(nunits, 0), lo_new(nunits + 1, 0);
-    for (int w = 0; w < nwin; ++w)
-        for (int u = win_ptr[2 * (size_t)w + 1]; u < win_ptr[2 * (size_t)w + 2]; ++u) dense[u] = 1;
+    std::vector<int> new_ptr(2 * (size_t)nwin + 1, 0), new_units;
+    std::vector<long long> src_first;  // first source unit of each new unit
+    std::vector<int> src_last;         // one past its last source unit
     long long o = 0;
-    for (int u = 0; u < nunits; ++u) {
-        if (dense[u]) o = (o + 3) & ~3LL;
-        lo_new[u] = (int)o;
-        o += units[4 * (size_t)u + 1] - units[4 * (size_t)u];
+    for (int w = 0; w < nwin; ++w) {
+        const int us = win_ptr[2 * (size_t)w], ud = win_ptr[2 * (size_t)w + 1], ue = win_ptr[2 * (size_t)w + 2];
+        new_ptr[2 * (size_t)w] = (int)(new_units.size() / 4);
+        if (ud > us) {
+            long long n = 0;
+            for (int u = us; u < ud; ++u) n += units[4 * (size_t)u + 1] - units[4 * (size_t)u];
+            o = (o + 3) & ~3LL;
+            new_units.insert(new_units.end(), {(int)o, (int)(o + n), -1, 0});
+            src_first.push_back(us);
+            src_last.push_back(ud);
+            o += n;
+            if (o + 8 > (long long)INT32_MAX) return false;
+        }
+        new_ptr[2 * (size_t)w + 1] = (int)(new_units.size() / 4);
+        for (int u = ud; u < ue; ++u) {
+            const int n = units[4 * (size_t)u + 1] - units[4 * (size_t)u];
+            o = (o + 3) & ~3LL;
+            new_units.insert(new_units.end(), {(int)o, (int)(o + n), units[4 * (size_t)u + 2], 0});
+            src_first.push_back(u);
+            src_last.push_back(u + 1);
+            o += n;
+            if (o + 8 > (long long)INT32_MAX) return false;
+        }
     }
-    if (o + 8 > (long long)INT32_MAX) return false;
-    const size_t total = (size_t)((o + 3) & ~3LL) + 4;
+    new_ptr[2 * (size_t)nwin] = (int)(new_units.size() / 4);
+    const size_t total = (size_t)((o + 3) & ~3LL) + 8;
     kind.assign(total, 0u);
     kdata.assign(total, 0.0);
-    auto work = [&](int u0, int u1) {
-        std::vector<std::pair<uint32_t, int>> key;
-        for (int u = u0; u < u1; ++u) {
-            const int lo = units[4 * (size_t)u], hi = units[4 * (size_t)u + 1], dst = lo_new[u];
-            if (!dense[u]) {
-                std::copy(ind.begin() + lo, ind.begin() + hi, kind.begin() + dst);
-                std::copy(data.begin() + lo, data.begin() + hi, kdata.begin() + dst);
-                continue;
-            }
+    kcol.assign(total, 0);
+    const int nnew = (int)(new_units.size() / 4);
+    auto work = [&](int v0, int v1) {
+        // (row key, column key, source position)
+        std::vector<std::tuple<uint32_t, uint32_t, long long>> key;
+        for (int v = v0; v < v1; ++v) {
+            const bool flat = new_units[4 * (size_t)v + 2] < 0;
+            const int dst = new_units[4 * (size_t)v];
             key.clear();
-            for (int k = lo; k < hi; ++k) key.emplace_back(ind[(size_t)k], k);
-            std::sort(key.begin(), key.end());  // (ind, position): stable by construction
+            for (long long u = src_first[v]; u < src_last[v]; ++u) {
+                const int lo = units[4 * (size_t)u], hi = units[4 * (size_t)u + 1], c0 = units[4 * (size_t)u + 2];
+                for (int k = lo; k < hi; ++k) {
+                    const uint32_t id = ind[(size_t)k];
+                    // a flat unit sorts by row, then global column (the unit's
+                    // first column + the local column mod S, as the kernel reads x)
+                    if (flat)
+                        key.emplace_back(id >> 16, (uint32_t)c0 + ((id & 0xFFFFu) & (uint32_t)(S - 1)), k);
+                    else
+                        key.emplace_back(id, 0u, k);
+                }
+            }
+            std::sort(key.begin(), key.end());  // position last: stable by construction
             for (size_t q = 0; q < key.size(); ++q) {
-                kind[(size_t)dst + q] = key[q].first;
-                kdata[(size_t)dst + q] = data[(size_t)key[q].second];
+                const long long k = std::get<2>(key[q]);
+                kind[(size_t)dst + q] = ind[(size_t)k];
+                kdata[(size_t)dst + q] = data[(size_t)k];
+                if (flat) kcol[(size_t)dst + q] = (int32_t)std::get<1>(key[q]);
             }
         }
     };
-    const int nt = std::max(1, std::min<int>(nunits / 64 + 1, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+    const int nt = std::max(1, std::min<int>(nnew / 64 + 1, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t) {
-        const int a = (int)((long long)nunits * t / nt), b = (int)((long long)nunits * (t + 1) / nt);
+        const int a = (int)((long long)nnew * t / nt), b = (int)((long long)nnew * (t + 1) / nt);
         th.emplace_back(work, a, b);
     }
     for (auto& t : th) t.join();
-    for (int u = 0; u < nunits; ++u) {
-        const int len = units[4 * (size_t)u + 1] - units[4 * (size_t)u];
-        units[4 * (size_t)u] = lo_new[u];
-        units[4 * (size_t)u + 1] = lo_new[u] + len;
-    }
+    win_ptr.swap(new_ptr);
+    units.swap(new_units);
     return true;
 }
 
@@ -495,7 +537,8 @@ int csb_window(int nor, int beta, int sm_count) {
     return S;
 }
 
-cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* win_ptr, const int* units, int nwin,
+cudaError_t launch_csb_spmv(const uint32_t* ind, const int32_t* kcol, const double* data, const int* win_ptr,
+                            const int* units, int nwin,
                             int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
                             int sm_count, cudaStream_t st, int variant) {
     if (nwin <= 0) return cudaSuccess;
@@ -503,10 +546,10 @@ cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* 
     const int nt = (variant & 2) ? 256 : 128;
     const int grid = std::min(nwin, sm_count * (kCsbThreadsPerSM / nt));
     switch (variant & 3) {
-        case 1: k_csb_spmv<128, 8><<<grid, 128, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
-        case 2: k_csb_spmv<256, 4><<<grid, 256, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
-        case 3: k_csb_spmv<256, 8><<<grid, 256, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
-        default: k_csb_spmv<128, 4><<<grid, 128, 0, st>>>(ind, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        case 1: k_csb_spmv<128, 8><<<grid, 128, 0, st>>>(ind, kcol, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        case 2: k_csb_spmv<256, 4><<<grid, 256, 0, st>>>(ind, kcol, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        case 3: k_csb_spmv<256, 8><<<grid, 256, 0, st>>>(ind, kcol, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
+        default: k_csb_spmv<128, 4><<<grid, 128, 0, st>>>(ind, kcol, data, win_ptr, un, nwin, S, nor, noc, x, y, nsq_in, status); break;
     }
     return cudaGetLastError();
 }

@@ -222,10 +222,10 @@ int csb_window(int nor, int beta, int sm_count);
 int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,
                    int beta, int bits, std::vector<uint32_t>& ind, std::vector<double>& data,
                    std::vector<int32_t>& blk_ptr, int S, std::vector<int>& win_ptr, std::vector<int>& unit_data);
-bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data,
-                       const std::vector<int>& win_ptr, std::vector<int>& units, std::vector<uint32_t>& kind,
-                       std::vector<double>& kdata);
-cudaError_t launch_csb_spmv(const uint32_t* ind, const double* data, const int* win_ptr, const int* units, int nwin,
+bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data, int S,
+                       std::vector<int>& win_ptr, std::vector<int>& units, std::vector<uint32_t>& kind,
+                       std::vector<double>& kdata, std::vector<int32_t>& kcol);
+cudaError_t launch_csb_spmv(const uint32_t* ind, const int32_t* kcol, const double* data, const int* win_ptr, const int* units, int nwin,
                             int S, int nor, int noc, const double* x, double* y, const double* nsq_in, int* status,
                             int sm_count, cudaStream_t st, int variant = 0);
 constexpr int kCsbVariants = 4;

@@ -113,6 +113,7 @@ struct pwmgpu_matrix {
     struct {
         int beta = 0, bits = 0, hb = 0, vb = 0, S = 0, nwin = 0;
         uint32_t* ind = nullptr;
+        int32_t* kcol = nullptr;  // global columns of the flat (merged sparse) units
         double* data = nullptr;
         int32_t* blk_ptr = nullptr;
         int* win_ptr = nullptr;
@@ -156,6 +157,7 @@ struct pwmgpu_matrix {
 
     void release_csb() {
         pwmgpu::dfree(csb.ind);
+        pwmgpu::dfree(csb.kcol);
         pwmgpu::dfree(csb.data);
         pwmgpu::dfree(csb.blk_ptr);
         pwmgpu::dfree(csb.win_ptr);

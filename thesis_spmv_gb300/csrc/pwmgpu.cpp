@@ -101,10 +101,13 @@ int build_format(pwmgpu_matrix* m) {
         // reference's arrays stay on the host for pwmgpu_get_csb
         std::vector<uint32_t> kind;
         std::vector<double> kdata;
-        if (!csb_kernel_layout(c.h_ind, c.h_data, win_ptr, units, kind, kdata))
+        std::vector<int32_t> kcol;
+        if (!csb_kernel_layout(c.h_ind, c.h_data, c.S, win_ptr, units, kind, kdata, kcol))
             return fail(PWMGPU_ERR_INVALID, "CSB: the padded device copy exceeds 32-bit element offsets");
         TRY(dalloc(&c.ind, kind.size()));
+        TRY(dalloc(&c.kcol, kcol.size()));
         TRY(dalloc(&c.data, kdata.size()));
+        CU(cudaMemcpyAsync(c.kcol, kcol.data(), sizeof(int32_t) * kcol.size(), cudaMemcpyHostToDevice, m->stream));
         TRY(dalloc(&c.blk_ptr, c.h_blk_ptr.size()));
         TRY(dalloc(&c.win_ptr, win_ptr.size()));
         TRY(dalloc(&c.units, units.size() + 4));
@@ -348,7 +351,7 @@ int spmv_format(pwmgpu_matrix* m, int fmt, const double* dx, double* dy, const d
     if (m->M.nor == 0) return PWMGPU_OK;
     if (fmt == PWMGPU_FMT_CSB) {
         const auto& c = m->csb;
-        CU(launch_csb_spmv(c.ind, c.data, c.win_ptr, c.units, c.nwin, c.S, m->M.nor, m->M.noc, dx, dy, nsq_in,
+        CU(launch_csb_spmv(c.ind, c.kcol, c.data, c.win_ptr, c.units, c.nwin, c.S, m->M.nor, m->M.noc, dx, dy, nsq_in,
                            m->status, m->sm_count, m->stream, m->csb_var));
     } else {
         const auto& c = m->coh;
