@@ -293,6 +293,8 @@ def irregular_and_solves(pwm, torch, dev, stream, args):
         e1.synchronize()
         fms = e0.elapsed_time(e1) / 50
         fm[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
+        if name == "csb":
+            fm[name]["variant"] = F.csb_variant()
         del F
     out["irregular"]["formats"] = fm
     out["irregular"]["stats"] = M.stats()
@@ -607,6 +609,8 @@ def run_ours(args, world, rank, local):
             f1.synchronize()
             fms = f0.elapsed_time(f1) / 50
             formats[name] = {"spmv_ms": round(fms, 5), "gb_s_crs_bytes": round(B / (fms * 1e-3) / 1e9, 2)}
+            if name == "csb":
+                formats[name]["variant"] = F.csb_variant()
             del F
         # the autotuner on this class: the 4096^2 grid, then a 4200 x 4096 grid
         formats["autotuner"] = autotune_report(

@@ -179,8 +179,10 @@ int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_varian
  * negative status). */
 int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices);
 /* CSB kernel variant of a PWMGPU_FMT_CSB handle (0..3, as csb_variant
- * above; 0 by default). */
+ * above).  Loading a matrix large enough to time (the merge tuner's
+ * threshold) picks the fastest of the four; smaller ones get 0. */
 int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant);
+int pwmgpu_get_csb_variant(const pwmgpu_matrix* m, int32_t* variant);
 
 /* Replaces mv(x, y) (SparseMatrix.hpp:57, CRS.hpp:99-109): y = A x with
  * caller-owned host arrays x[noc], y[nor]; synchronous. */

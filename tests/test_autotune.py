@@ -196,3 +196,17 @@ def test_csb_long_rows_and_duplicates(pwm, variant):
     M.set_csb_variant(variant)
     for seed in (1, 2):
         _check_mv(M, A, 30 + seed)
+
+
+@pytest.mark.gpu
+def test_csb_handle_picks_variant_at_load(pwm, poisson):
+    """A CSB handle on a matrix large enough to time picks one of the four
+    variants at load time; the result matches the oracle; the variant can be
+    overridden."""
+    M = pwm.CSBCuda(1)
+    M.generatePoissonMatrix(GRID, GRID, 1)
+    assert M.csb_variant() in (0, 1, 2, 3)
+    _check_mv(M, poisson, 41)
+    M.set_csb_variant(3)
+    assert M.csb_variant() == 3
+    _check_mv(M, poisson, 42)

@@ -74,6 +74,7 @@ SIGNATURES = {
     "pwmgpu_tuner_record": (C.c_int, [C.POINTER(i32), i32, i32, i32]),
     "pwmgpu_tuner_entries": (C.c_int, [i32, C.POINTER(i32), C.POINTER(i32)]),
     "pwmgpu_set_csb_variant": (C.c_int, [vp, i32]),
+    "pwmgpu_get_csb_variant": (C.c_int, [vp, C.POINTER(i32)]),
     "pwmgpu_get_csr": (C.c_int, [vp, vp, vp, vp]),
     "pwmgpu_mv": (C.c_int, [vp, vp, vp]),
     "pwmgpu_mv_device": (C.c_int, [vp, vp, vp]),

@@ -293,8 +293,14 @@ int build_merge(pwmgpu_matrix* m, bool run_tuner) {
 
 int build_auto(pwmgpu_matrix* m);
 
+int tune_csb(pwmgpu_matrix* m);
+
 int build_plan(pwmgpu_matrix* m) {
     if (m->auto_fmt) return build_auto(m);
+    if (m->format == PWMGPU_FMT_CSB) {
+        TRY(build_format(m));
+        return tune_csb(m);
+    }
     if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
     return build_merge(m, true);
 }
@@ -1692,6 +1698,26 @@ int build_candidate(pwmgpu_matrix* m, int fmt) {
 
 }  // namespace
 
+// Load-time variant tuner of a CSB handle: with enough work to measure (the
+// merge tuner's threshold), time the four kernel variants and keep the
+// fastest (pwmgpu_set_csb_variant overrides it).  4096^2 stencil: 4 elements
+// per lane, 128 threads; irregular matrix: 256 threads.
+int tune_csb(pwmgpu_matrix* m) {
+    m->csb_var = 0;
+    const MergeGeom g = merge_geometry(kCfgF64, 0);
+    const long long tiles = ((long long)m->M.nor + m->M.nnz + g.wm - 1) / g.wm;
+    if (m->M.nor == 0 || tiles < 8LL * g.occ * g.w * m->sm_count) return PWMGPU_OK;
+    float ms[kCsbVariants];
+    int best = 0;
+    for (int v = 0; v < kCsbVariants; ++v) {
+        m->csb_var = v;
+        TRY(time_format(m, PWMGPU_FMT_CSB, &ms[v]));
+        if (ms[v] < 0.97f * ms[best]) best = v;  // another variant only for a clear (3 %) gain
+    }
+    m->csb_var = best;
+    return PWMGPU_OK;
+}
+
 int build_auto(pwmgpu_matrix* m) {
     const auto t0 = std::chrono::steady_clock::now();
     pwmgpu_tuning T{};
@@ -1842,6 +1868,13 @@ int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices) {
         ++n;
     }
     return n;
+}
+
+int pwmgpu_get_csb_variant(const pwmgpu_matrix* m, int32_t* variant) {
+    if (!m || !variant) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null handle or output");
+    if (m->format != PWMGPU_FMT_CSB) return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB handle");
+    *variant = m->csb_var;
+    return PWMGPU_OK;
 }
 
 int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant) {

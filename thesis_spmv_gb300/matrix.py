@@ -282,6 +282,12 @@ class CudaSparseMatrix:
         """CSB kernel variant (CSB handles): bit 0 = 8 elements per lane, bit 1 = 256 threads per CTA."""
         check(_lib.lib().pwmgpu_set_csb_variant(self._h, int(variant)), "pwmgpu_set_csb_variant")
 
+    def csb_variant(self):
+        """The CSB kernel variant in use (picked at load time on large matrices)."""
+        v = C.c_int32()
+        check(_lib.lib().pwmgpu_get_csb_variant(self._h, C.byref(v)), "pwmgpu_get_csb_variant")
+        return v.value
+
     def getCSB(self):
         """The CSB arrays (CSB.hpp:464-567) of a CSBCuda handle: dict(ind,
         data, blk_ptr, beta, block_bits, hb, vb)."""
