@@ -198,10 +198,12 @@ def run_reference(args, world, rank):
 
 def coh_partitions(n, nnz, sm_count):
     """CO-H partition count (the reference's thread count) for the GPU: a warp
-    per partition, one per resident warp (32 per SM).  More partitions make
-    more, emptier blocks (4096^2 stencil: 0.85 ms at 4864 partitions, 1.41 ms
-    at 16777, 5.39 ms at 67108); n and nnz are unused."""
-    return 32 * sm_count
+    per partition, 24 per SM.  More partitions make more, emptier blocks,
+    fewer leave warps idle (4096^2 stencil: 0.70 ms at 24 per SM, 0.85 at
+    32, 1.51 at 8; the irregular matrix prefers 8 per SM, 4.4 ms -- the
+    format autotuner times 8, 16, 24 and 32 per SM per matrix class); n and
+    nnz are unused."""
+    return 24 * sm_count
 
 
 IRREGULAR = dict(n=4194304, seed=20261203, length_dist=0, mean_len=16.0, sigma=1.2, max_len=20000,
@@ -228,8 +230,10 @@ def autotune_report(pwm, torch, stream, load, load_same_class, x, y, B):
                "merge_variant": t["merge_variant"], "cache_hit": t["cache_hit"], "timed": t["timed"],
                "class_key": t["class_key"]}
         if t["timed"]:
-            rec["candidates_ms"] = {"merge": round(t["merge_ms"], 5), "coh": round(t["coh_ms"], 5),
-                                    **{"csb_v%d" % v: round(t["csb_ms"][v], 5) for v in range(4)}}
+            rec["candidates_ms"] = {"merge": round(t["merge_ms"], 5),
+                                    **{"csb_v%d" % v: round(t["csb_ms"][v], 5) for v in range(4)},
+                                    **{"coh_%d_per_sm" % p: round(t["coh_ms"][i], 5)
+                                       for i, p in enumerate((8, 16, 24, 32))}}
         if tag == "first_of_class":
             for _ in range(3):
                 A.mv_device(x.data_ptr(), y.data_ptr())

@@ -146,7 +146,7 @@ int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out);
  * every candidate -- the merge kernels' 4 launch variants (shared-memory /
  * L1 carveout x gathers through or around L1), CSB with 4 or 8 elements
  * per lane and 128 or 256 threads per CTA, and CO-H with a warp per
- * partition (32 sm_count partitions) -- on a few SpMVs each
+ * partition and 8, 16, 24 or 32 partitions per SM -- on a few SpMVs each
  * and records the fastest in a process-wide table; later matrices of the
  * class take the recorded choice without timing.  Matrices too small to time
  * (the merge tuner's threshold) run merge. */
@@ -157,9 +157,10 @@ typedef struct {
     int32_t cache_hit;       /* 1: taken from the class table without timing */
     int32_t timed;           /* 1: candidates were timed for this matrix */
     int32_t class_key[7];
+    int32_t coh_partitions;  /* CO-H partitions when CO-H is the format */
     float merge_ms;          /* ms per SpMV of the best merge variant (0 if not timed) */
     float csb_ms[4];         /* per CSB variant */
-    float coh_ms;
+    float coh_ms[4];         /* per CO-H partition count: 8, 16, 24, 32 per SM */
     double tune_seconds;     /* wall time of the tuning (builds and timings) */
 } pwmgpu_tuning;
 int pwmgpu_tuning_info(const pwmgpu_matrix* m, pwmgpu_tuning* out);
@@ -172,11 +173,13 @@ int pwmgpu_tuner_reset(void);
 int pwmgpu_tuner_size(void);
 /* Record a class choice (to carry tunings between processes): format
  * PWMGPU_FMT_MERGE / _CSB / _COH, csb_variant 0..3, merge_variant one of
- * the merge launch variants (0, 1, 4, 5). */
-int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant);
-/* Copy up to `max` recorded entries: keys[7 i ..], choices[3 i ..] =
- * {format, csb_variant, merge_variant}; returns the number copied (or a
- * negative status). */
+ * the merge launch variants (0, 1, 4, 5), coh_parts_per_sm 1..64 (CO-H
+ * partitions per SM; 0: 24). */
+int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant,
+                        int32_t coh_parts_per_sm);
+/* Copy up to `max` recorded entries: keys[7 i ..], choices[4 i ..] =
+ * {format, csb_variant, merge_variant, coh_parts_per_sm}; returns the number
+ * copied (or a negative status). */
 int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices);
 /* CSB kernel variant of a PWMGPU_FMT_CSB handle (0..3, as csb_variant
  * above).  Loading a matrix large enough to time (the merge tuner's

@@ -43,12 +43,16 @@ def test_tuner_table_record_and_reset(pwm):
     pwm.tuner_record([1, 2, 3, 4, 1, 5, 152], "csb", 3, 1)
     pwm.tuner_record([1, 2, 3, 4, 1, 5, 152], "coh")  # replaces the entry
     pwm.tuner_record([9, 2, 3, 4, 1, 5, 152], "merge", 0, 5)
-    assert sorted(pwm.tuner_entries()) == [([1, 2, 3, 4, 1, 5, 152], "coh", 0, 0),
-                                            ([9, 2, 3, 4, 1, 5, 152], "merge", 0, 5)]
+    pwm.tuner_record([5, 2, 3, 4, 1, 5, 152], "coh", 0, 0, 8)
+    assert sorted(pwm.tuner_entries()) == [([1, 2, 3, 4, 1, 5, 152], "coh", 0, 0, 24),
+                                            ([5, 2, 3, 4, 1, 5, 152], "coh", 0, 0, 8),
+                                            ([9, 2, 3, 4, 1, 5, 152], "merge", 0, 5, 24)]
     with pytest.raises(pwm.PwmGpuError):
         pwm.tuner_record([0] * 7, "csb", 4, 0)
     with pytest.raises(pwm.PwmGpuError):
         pwm.tuner_record([0] * 7, "merge", 0, 2)
+    with pytest.raises(pwm.PwmGpuError):
+        pwm.tuner_record([0] * 7, "coh", 0, 0, 65)
     pwm.tuner_reset()
     assert pwm.tuner_entries() == []
 
@@ -99,9 +103,9 @@ def test_auto_times_then_reuses_class(pwm, poisson):
     t = M.tuning()
     assert t["timed"] and not t["cache_hit"]
     assert t["format"] in ("merge", "csb", "coh")
-    assert t["merge_ms"] > 0 and t["coh_ms"] > 0 and all(v > 0 for v in t["csb_ms"])
-    best = min([t["merge_ms"], t["coh_ms"]] + t["csb_ms"])
-    chosen = {"merge": t["merge_ms"], "coh": t["coh_ms"], "csb": t["csb_ms"][t["csb_variant"]]}[t["format"]]
+    assert t["merge_ms"] > 0 and all(v > 0 for v in t["coh_ms"]) and all(v > 0 for v in t["csb_ms"])
+    best = min([t["merge_ms"]] + t["coh_ms"] + t["csb_ms"])
+    chosen = {"merge": t["merge_ms"], "coh": min(t["coh_ms"]), "csb": t["csb_ms"][t["csb_variant"]]}[t["format"]]
     assert chosen == best
     assert pwm.tuner_size() == 1
     _check_mv(M, poisson, 3)
@@ -121,8 +125,9 @@ def test_auto_times_then_reuses_class(pwm, poisson):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fmt,variant", [("csb", 0), ("csb", 3), ("coh", 0), ("merge", 0)])
-def test_auto_recorded_choice_runs_that_format(pwm, poisson, fmt, variant):
+@pytest.mark.parametrize("fmt,variant,pps", [("csb", 0, 0), ("csb", 3, 0), ("coh", 0, 0), ("coh", 0, 8),
+                                             ("merge", 0, 0)])
+def test_auto_recorded_choice_runs_that_format(pwm, poisson, fmt, variant, pps):
     """A recorded class choice (as a tuning carried from another process)
     makes the AUTO handle run that format's kernel; results match the oracle
     and the merge-only paths (the solve) still work."""
@@ -133,11 +138,12 @@ def test_auto_recorded_choice_runs_that_format(pwm, poisson, fmt, variant):
     sm = C.c_int()
     pwm.lib().pwmgpu_device_info(C.byref(sm), None, None)
     key = pwm.class_key(probe.stats(), sm.value)
-    pwm.tuner_record(key, fmt, variant, 0)
+    pwm.tuner_record(key, fmt, variant, 0, pps)
     M = pwm.AutoCuda(1)
     M.generatePoissonMatrix(GRID, GRID, 1)
     t = M.tuning()
     assert t["cache_hit"] and (t["format"], t["csb_variant"]) == (fmt, variant if fmt == "csb" else 0)
+    assert t["coh_partitions"] == ((pps or 24) * sm.value if fmt == "coh" else 0)
     _check_mv(M, poisson, 6)
     x0 = np.random.default_rng(7).random(poisson.noc)
     xr, yr = O.power(poisson, x0, 5)

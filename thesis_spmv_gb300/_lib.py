@@ -40,7 +40,8 @@ class Tuning(C.Structure):
     """pwmgpu_tuning: what the format autotuner chose for a PWMGPU_FMT_AUTO handle."""
     _fields_ = [("format", C.c_int32), ("csb_variant", C.c_int32), ("merge_variant", C.c_int32),
                 ("cache_hit", C.c_int32), ("timed", C.c_int32), ("class_key", C.c_int32 * 7),
-                ("merge_ms", C.c_float), ("csb_ms", C.c_float * 4), ("coh_ms", C.c_float),
+                ("coh_partitions", C.c_int32), ("merge_ms", C.c_float), ("csb_ms", C.c_float * 4),
+                ("coh_ms", C.c_float * 4),
                 ("tune_seconds", C.c_double)]
 
 
@@ -71,7 +72,7 @@ SIGNATURES = {
     "pwmgpu_class_key": (C.c_int, [C.POINTER(MatrixStats), i32, C.POINTER(i32)]),
     "pwmgpu_tuner_reset": (C.c_int, []),
     "pwmgpu_tuner_size": (C.c_int, []),
-    "pwmgpu_tuner_record": (C.c_int, [C.POINTER(i32), i32, i32, i32]),
+    "pwmgpu_tuner_record": (C.c_int, [C.POINTER(i32), i32, i32, i32, i32]),
     "pwmgpu_tuner_entries": (C.c_int, [i32, C.POINTER(i32), C.POINTER(i32)]),
     "pwmgpu_set_csb_variant": (C.c_int, [vp, i32]),
     "pwmgpu_get_csb_variant": (C.c_int, [vp, C.POINTER(i32)]),

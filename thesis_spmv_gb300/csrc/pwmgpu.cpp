@@ -1632,10 +1632,14 @@ int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes, int32_t* gat
 namespace pwmgpu {
 namespace {
 
+constexpr int kCohPartsPerSM[4] = {8, 16, 24, 32};  // CO-H candidates (partitions per SM)
+constexpr int kCohPartsDefault = 24;
+
 struct TuneChoice {
     int fmt = PWMGPU_FMT_MERGE;
     int csb_var = 0;
     int merge_var = 0;
+    int coh_pps = kCohPartsDefault;  // CO-H partitions per SM
 };
 using ClassKey = std::array<int32_t, 7>;
 std::mutex g_tune_mu;
@@ -1683,12 +1687,14 @@ int time_format(pwmgpu_matrix* m, int fmt, float* ms) {
 }
 
 // Build one of the CSB / CO-H formats beside the CRS arrays (still on the
-// device); the CO-H candidate gets a GPU partition count: a warp per
-// partition, one per resident warp (32 per SM).
-int build_candidate(pwmgpu_matrix* m, int fmt) {
+// device); a CO-H candidate has coh_pps partitions (warps) per SM.
+int build_candidate(pwmgpu_matrix* m, int fmt, int coh_pps = kCohPartsDefault) {
     const int saved_fmt = m->format, saved_parts = m->partitions;
     m->format = fmt;
-    if (fmt == PWMGPU_FMT_COH) m->partitions = 32 * m->sm_count;
+    if (fmt == PWMGPU_FMT_COH) {
+        m->release_coh();
+        m->partitions = coh_pps * m->sm_count;
+    }
     const int rc = build_format(m);
     m->format = saved_fmt;
     m->partitions = saved_parts;
@@ -1756,7 +1762,7 @@ int build_auto(pwmgpu_matrix* m) {
     }
     if (hit) {
         T.cache_hit = 1;
-        if (choice.fmt != PWMGPU_FMT_MERGE) TRY(build_candidate(m, choice.fmt));
+        if (choice.fmt != PWMGPU_FMT_MERGE) TRY(build_candidate(m, choice.fmt, choice.coh_pps));
         TRY(build_merge(m, false));
         apply_merge_variant(m, choice.merge_var | (m->P.colp16 ? 2 : 0));
     } else {
@@ -1769,10 +1775,18 @@ int build_auto(pwmgpu_matrix* m) {
             TRY(time_format(m, PWMGPU_FMT_CSB, &T.csb_ms[v]));
         }
         m->loaded = false;
-        // CO-H
-        TRY(build_candidate(m, PWMGPU_FMT_COH));
-        m->loaded = true;
-        TRY(time_format(m, PWMGPU_FMT_COH, &T.coh_ms));
+        // CO-H at each partition count (the format's layout depends on it)
+        int coh_best = 0;
+        for (int i = 0; i < 4; ++i) {
+            TRY(build_candidate(m, PWMGPU_FMT_COH, kCohPartsPerSM[i]));
+            m->loaded = true;
+            TRY(time_format(m, PWMGPU_FMT_COH, &T.coh_ms[i]));
+            m->loaded = false;
+            if (T.coh_ms[i] < T.coh_ms[coh_best]) coh_best = i;
+        }
+        // keep the best CO-H arrays (built from the CRS arrays, which the
+        // merge plan below releases)
+        if (coh_best != 3) TRY(build_candidate(m, PWMGPU_FMT_COH, kCohPartsPerSM[coh_best]));
         // merge: plan and launch-variant tuner, then the same timing
         TRY(build_merge(m, true));
         TRY(time_format(m, PWMGPU_FMT_MERGE, &T.merge_ms));
@@ -1784,11 +1798,12 @@ int build_auto(pwmgpu_matrix* m) {
                 choice.fmt = PWMGPU_FMT_CSB;
                 choice.csb_var = v;
             }
-        if (T.coh_ms < best) {
-            best = T.coh_ms;
+        if (T.coh_ms[coh_best] < best) {
+            best = T.coh_ms[coh_best];
             choice.fmt = PWMGPU_FMT_COH;
             choice.csb_var = 0;
         }
+        choice.coh_pps = kCohPartsPerSM[coh_best];
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_table[key] = choice;
     }
@@ -1798,6 +1813,7 @@ int build_auto(pwmgpu_matrix* m) {
     m->tuned_fmt = choice.fmt;
     m->csb_var = choice.fmt == PWMGPU_FMT_CSB ? choice.csb_var : 0;
     T.format = choice.fmt;
+    T.coh_partitions = choice.fmt == PWMGPU_FMT_COH ? choice.coh_pps * m->sm_count : 0;
     T.csb_variant = m->csb_var;
     T.merge_variant = m->l1;
     T.tune_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1835,7 +1851,8 @@ int pwmgpu_tuner_size(void) {
     return (int)pwmgpu::g_tune_table.size();
 }
 
-int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant) {
+int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant,
+                        int32_t coh_parts_per_sm) {
     if (!key) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null key");
     if (format != PWMGPU_FMT_MERGE && format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH)
         return pwmgpu::fail(PWMGPU_ERR_INVALID, "format must be merge, CSB or CO-H");
@@ -1843,12 +1860,15 @@ int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_varian
         return pwmgpu::fail(PWMGPU_ERR_INVALID, "CSB variant 0..3");
     if (merge_variant != 0 && merge_variant != 1 && merge_variant != 4 && merge_variant != 5)
         return pwmgpu::fail(PWMGPU_ERR_INVALID, "merge variant 0, 1, 4 or 5");
+    if (coh_parts_per_sm < 0 || coh_parts_per_sm > 64)
+        return pwmgpu::fail(PWMGPU_ERR_INVALID, "CO-H partitions per SM 0..64");
     pwmgpu::ClassKey k{};
     std::copy(key, key + 7, k.begin());
     pwmgpu::TuneChoice c;
     c.fmt = format;
     c.csb_var = format == PWMGPU_FMT_CSB ? csb_variant : 0;
     c.merge_var = merge_variant;
+    c.coh_pps = coh_parts_per_sm ? coh_parts_per_sm : pwmgpu::kCohPartsDefault;
     std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
     pwmgpu::g_tune_table[k] = c;
     return PWMGPU_OK;
@@ -1862,9 +1882,10 @@ int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices) {
     for (const auto& kv : pwmgpu::g_tune_table) {
         if (n >= max) break;
         std::copy(kv.first.begin(), kv.first.end(), keys + 7 * (size_t)n);
-        choices[3 * (size_t)n] = kv.second.fmt;
-        choices[3 * (size_t)n + 1] = kv.second.csb_var;
-        choices[3 * (size_t)n + 2] = kv.second.merge_var;
+        choices[4 * (size_t)n] = kv.second.fmt;
+        choices[4 * (size_t)n + 1] = kv.second.csb_var;
+        choices[4 * (size_t)n + 2] = kv.second.merge_var;
+        choices[4 * (size_t)n + 3] = kv.second.coh_pps;
         ++n;
     }
     return n;

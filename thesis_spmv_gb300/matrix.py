@@ -351,8 +351,9 @@ class AutoCuda(CudaSparseMatrix):
         check(_lib.lib().pwmgpu_tuning_info(self._h, C.byref(t)), "pwmgpu_tuning_info")
         return dict(format={FMT_MERGE: "merge", FMT_CSB: "csb", FMT_COH: "coh"}[t.format],
                     csb_variant=t.csb_variant, merge_variant=t.merge_variant, cache_hit=bool(t.cache_hit),
-                    timed=bool(t.timed), class_key=list(t.class_key), merge_ms=t.merge_ms,
-                    csb_ms=list(t.csb_ms), coh_ms=t.coh_ms, tune_seconds=t.tune_seconds)
+                    timed=bool(t.timed), class_key=list(t.class_key), coh_partitions=t.coh_partitions,
+                    merge_ms=t.merge_ms, csb_ms=list(t.csb_ms), coh_ms=list(t.coh_ms),
+                    tune_seconds=t.tune_seconds)
 
 
 def tuner_reset():
@@ -365,23 +366,26 @@ def tuner_size():
     return int(_lib.lib().pwmgpu_tuner_size())
 
 
-def tuner_record(key, fmt, csb_variant=0, merge_variant=0):
+def tuner_record(key, fmt, csb_variant=0, merge_variant=0, coh_parts_per_sm=0):
     """Record a class choice (fmt "merge" / "csb" / "coh") in the autotuner's table."""
     k = (C.c_int32 * 7)(*[int(v) for v in key])
     f = {"merge": FMT_MERGE, "csb": FMT_CSB, "coh": FMT_COH}[fmt]
-    check(_lib.lib().pwmgpu_tuner_record(k, f, int(csb_variant), int(merge_variant)), "pwmgpu_tuner_record")
+    check(_lib.lib().pwmgpu_tuner_record(k, f, int(csb_variant), int(merge_variant), int(coh_parts_per_sm)),
+          "pwmgpu_tuner_record")
 
 
 def tuner_entries():
-    """The autotuner's table: list of (class key, format, csb_variant, merge_variant)."""
+    """The autotuner's table: list of (class key, format, csb_variant,
+    merge_variant, coh_parts_per_sm)."""
     n = tuner_size()
     keys = (C.c_int32 * (7 * max(n, 1)))()
-    ch = (C.c_int32 * (3 * max(n, 1)))()
+    ch = (C.c_int32 * (4 * max(n, 1)))()
     got = _lib.lib().pwmgpu_tuner_entries(n, keys, ch)
     if got < 0:
         check(-got, "pwmgpu_tuner_entries")
     names = {FMT_MERGE: "merge", FMT_CSB: "csb", FMT_COH: "coh"}
-    return [(list(keys[7 * i:7 * i + 7]), names[ch[3 * i]], ch[3 * i + 1], ch[3 * i + 2]) for i in range(got)]
+    return [(list(keys[7 * i:7 * i + 7]), names[ch[4 * i]], ch[4 * i + 1], ch[4 * i + 2], ch[4 * i + 3])
+            for i in range(got)]
 
 
 def class_key(stats, sm_count):
