@@ -8,7 +8,10 @@
 // 16-bit column jumps that overflow by +beta at a row change, 16-bit row
 // jumps; between blocks BICRS (:404-445): int16 column jumps that overflow by
 // +hb at a block-row change, int16 block-row jumps.  Built on the host here,
-// bit for bit the reference's arrays.
+// bit for bit the reference's arrays.  The device copy of the column jumps
+// and values starts every block on a multiple of 8 elements (zeros between
+// blocks, never read as elements) so a lane loads its 8 elements with wide
+// loads; the block table holds the padded offsets.
 //
 // The GPU kernel (k_coh_spmv) gives each partition to one warp (a partition
 // owns its rows, as a thread does in BlockCOH::mv :479-510).  The warp walks
@@ -43,7 +46,8 @@ namespace pwmgpu {
 
 namespace {
 
-constexpr int kCohK = 8;           // elements per lane per chunk
+constexpr int kCohK = 8;           // elements per lane per chunk (one 16-byte load of jumps)
+static_assert(kCohK == 8, "a lane loads its column jumps as one uint4");
 constexpr int kCohWarps = 4;       // warps per CTA
 constexpr int kCohOcc = 8;         // resident CTAs per SM (64 registers): 32 warps
 
@@ -121,12 +125,25 @@ __global__ void __launch_bounds__(32 * kCohWarps, kCohOcc) k_coh_spmv(const int4
                 int pos[K];
                 double dv[K];
                 int tot = 0;
+                // the block starts on a multiple of 8 elements in the device
+                // copy, padded past its end: one 16-byte load of jumps, four
+                // of values
+                uint4 cj = make_uint4(0u, 0u, 0u, 0u);
+                double2 dd[K / 2];
+#pragma unroll
+                for (int t = 0; t < K / 2; ++t) dd[t] = make_double2(0.0, 0.0);
+                if (i0 < n) {
+                    cj = __ldg(reinterpret_cast<const uint4*>(col_jump + eb + i0));
+#pragma unroll
+                    for (int t = 0; t < K / 2; ++t) dd[t] = __ldg(reinterpret_cast<const double2*>(data + eb + i0) + t);
+                }
+                const uint32_t cw[4] = {cj.x, cj.y, cj.z, cj.w};
 #pragma unroll
                 for (int t = 0; t < K; ++t) {
-                    const int i = i0 + t;
-                    const bool v = i < n;
-                    tot += v ? (int)__ldg(col_jump + eb + i) : 0;
-                    dv[t] = v ? __ldg(data + eb + i) : 0.0;
+                    const bool v = i0 + t < n;
+                    const int jump = (int)((t & 1) ? (cw[t >> 1] >> 16) : (cw[t >> 1] & 0xFFFFu));
+                    tot += v ? jump : 0;
+                    dv[t] = v ? ((t & 1) ? dd[t >> 1].y : dd[t >> 1].x) : 0.0;
                     pos[t] = tot;
                 }
                 int incl = tot;

@@ -126,11 +126,34 @@ int build_format(pwmgpu_matrix* m) {
                                  c.h_row_jump, c.h_col_jump, c.h_data, c.block_nnz, c.row_jump_block,
                                  c.col_jump_block, parts, blocks);
         c.nblocks = (long long)c.block_nnz.size();
+        // the kernel's copy of the column jumps and values: every block from a
+        // multiple of 8 elements (a lane's 8 elements are one 16-byte load of
+        // jumps and four of values); blocks[8 b + 2] = the block's first element
+        std::vector<uint16_t> kcj;
+        std::vector<double> kd;
+        {
+            long long o = 0;
+            const size_t nb = blocks.size() / 8;
+            for (size_t b = 0; b < nb; ++b) o = ((o + 7) & ~7LL) + blocks[8 * b + 4];
+            if (o + 16 > (long long)INT32_MAX)
+                return fail(PWMGPU_ERR_INVALID, "CO-H: the padded device copy exceeds 32-bit element offsets");
+            kcj.assign((size_t)((o + 7) & ~7LL) + 8, 0);
+            kd.assign(kcj.size(), 0.0);
+            o = 0;
+            for (size_t b = 0; b < nb; ++b) {
+                o = (o + 7) & ~7LL;
+                const int first = blocks[8 * b + 2], n = blocks[8 * b + 4];
+                std::copy(c.h_col_jump.begin() + first, c.h_col_jump.begin() + first + n, kcj.begin() + o);
+                std::copy(c.h_data.begin() + first, c.h_data.begin() + first + n, kd.begin() + o);
+                blocks[8 * b + 2] = (int)o;
+                o += n;
+            }
+        }
         TRY(dalloc(&c.d_parts, parts.size()));
         TRY(dalloc(&c.d_blocks, blocks.size() + 8));
         TRY(dalloc(&c.row_jump, c.h_row_jump.size() + 8));
-        TRY(dalloc(&c.col_jump, c.h_col_jump.size() + 8));
-        TRY(dalloc(&c.data, c.h_data.size() + 4));
+        TRY(dalloc(&c.col_jump, kcj.size()));
+        TRY(dalloc(&c.data, kd.size()));
         CU(cudaMemcpyAsync(c.d_parts, parts.data(), sizeof(int) * parts.size(), cudaMemcpyHostToDevice, m->stream));
         if (!blocks.empty())
             CU(cudaMemcpyAsync(c.d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice,
@@ -138,12 +161,9 @@ int build_format(pwmgpu_matrix* m) {
         if (!c.h_row_jump.empty())
             CU(cudaMemcpyAsync(c.row_jump, c.h_row_jump.data(), sizeof(uint16_t) * c.h_row_jump.size(),
                                cudaMemcpyHostToDevice, m->stream));
-        if (!c.h_col_jump.empty())
-            CU(cudaMemcpyAsync(c.col_jump, c.h_col_jump.data(), sizeof(uint16_t) * c.h_col_jump.size(),
-                               cudaMemcpyHostToDevice, m->stream));
-        if (!c.h_data.empty())
-            CU(cudaMemcpyAsync(c.data, c.h_data.data(), sizeof(double) * c.h_data.size(), cudaMemcpyHostToDevice,
-                               m->stream));
+        CU(cudaMemcpyAsync(c.col_jump, kcj.data(), sizeof(uint16_t) * kcj.size(), cudaMemcpyHostToDevice,
+                           m->stream));
+        CU(cudaMemcpyAsync(c.data, kd.data(), sizeof(double) * kd.size(), cudaMemcpyHostToDevice, m->stream));
     }
     CU(cudaStreamSynchronize(m->stream));
     TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)2 * dot_grid(m->M.nor, m->sm_count) + 64));
@@ -1512,16 +1532,15 @@ int pwmgpu_get_coh(pwmgpu_matrix* m, int32_t* part_info, uint16_t* row_jump, uin
         if (dst && !v.empty()) std::memcpy(dst, v.data(), sizeof(v[0]) * v.size());
     };
     put(part_info, c.part_info);
-    // the device copies are the ones the kernel reads: return those
+    // the row jumps as the kernel reads them; the column jumps and values
+    // from the host copies (the device copy starts every block on a
+    // multiple of 8 elements)
     if (row_jump && !c.h_row_jump.empty())
         CU(cudaMemcpyAsync(row_jump, c.row_jump, sizeof(uint16_t) * c.h_row_jump.size(), cudaMemcpyDeviceToHost,
                            m->stream));
-    if (col_jump && !c.h_col_jump.empty())
-        CU(cudaMemcpyAsync(col_jump, c.col_jump, sizeof(uint16_t) * c.h_col_jump.size(), cudaMemcpyDeviceToHost,
-                           m->stream));
-    if (data && !c.h_data.empty())
-        CU(cudaMemcpyAsync(data, c.data, sizeof(double) * c.h_data.size(), cudaMemcpyDeviceToHost, m->stream));
     CU(cudaStreamSynchronize(m->stream));
+    put(col_jump, c.h_col_jump);
+    put(data, c.h_data);
     put(block_nnz, c.block_nnz);
     put(row_jump_block, c.row_jump_block);
     put(col_jump_block, c.col_jump_block);
