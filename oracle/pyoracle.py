@@ -303,9 +303,8 @@ def row_error_bound(A, x, u=2.0 ** -53):
     rl = np.diff(A.row_start).astype(np.float64)
     absx = np.abs(np.asarray(x, np.float64))
     prod = np.abs(A.data) * absx[A.col_ind]
-    s = np.zeros(A.nor, np.float64)
     rows = np.repeat(np.arange(A.nor), np.diff(A.row_start))
-    np.add.at(s, rows, prod)
+    s = np.bincount(rows, weights=prod, minlength=A.nor)
     return 2.0 * rl * u * s
 
 
