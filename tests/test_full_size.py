@@ -6,7 +6,8 @@ oracle's CRS::mv / powerIteration.  C2: the 4096^2 Poisson matrix (N =
 fillPoisson (Util/Poisson.hpp:32-83), the SpMV on a seeded uniform vector
 within the per-row bound, and size-independent properties -- x = 1 gives the
 exact row sums, A(2x) = 2(Ax) bit for bit (scaling by 2 is exact), 20 power
-iterations within 1e-10 of the oracle.  C3: the irregular lognormal-row
+iterations within 1e-10 of the oracle; the same matrix in the CSB and CO-H
+formats.  C3: the irregular lognormal-row
 matrix (N = 4,194,304): the device generator's arrays bit for bit against
 the oracle's restatement, the SpMV within the bound, and FP64 and mixed
 solves to 1e-10 relative eigen-residual whose eigenvalues agree to 1e-10
@@ -97,3 +98,20 @@ def test_c3_irregular_arrays_spmv_and_solves(pwm):
         assert res <= 1.01e-10 and abs(lam - info.lambda_) <= 1e-10 * abs(lam)
         lams[prec] = info.lambda_
     assert abs(lams[pwm.PREC_MIXED] - lams[pwm.PREC_F64]) <= 1e-10 * abs(lams[pwm.PREC_F64])
+
+
+@pytest.mark.parametrize("fmt", ["csb", "coh"])
+def test_c2_poisson4096_other_formats(pwm, fmt):
+    """The 4096^2 matrix in the CSB format (load-time variant choice) and
+    the CO-H format (24 partitions per SM, as the bench runs it): SpMV within
+    the row bound, and the exact row sums for x = 1."""
+    import ctypes as C
+    sm = C.c_int()
+    pwm.lib().pwmgpu_device_info(C.byref(sm), None, None)
+    A = O.fill_poisson(4096, 4096)
+    M = pwm.CSBCuda(1) if fmt == "csb" else pwm.COHCuda(24 * sm.value)
+    M.generatePoissonMatrix(4096, 4096, 1)
+    x = np.random.default_rng(SEED + 1).random(A.noc)
+    assert np.all(np.abs(_mv(M, x) - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
+    ones = np.ones(A.noc)
+    assert np.array_equal(_mv(M, ones), O.crs_mv(A, ones))
