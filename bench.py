@@ -1,7 +1,7 @@
 """Benchmark: FP64 merge-path SpMV and power method on the 4096x4096-grid
 2D Poisson matrix (N = 16,777,216, nnz = 83,869,696), GB300.
 
-One step = one SpMV y = A x over the whole matrix (the benchmark spec's plain FP64
+One step = one SpMV y = A x over the whole matrix (the plain FP64
 merge-path SpMV, reported as GB/s against the HBM roofline).  Inputs are
 larger than L2 (1.34 GB of matrix and vectors per pass), so no flush is
 needed between steps.

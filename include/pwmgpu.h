@@ -235,7 +235,7 @@ int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
 int pwmgpu_set_low_format(pwmgpu_matrix* m, int fmt);
 
 /* Power solve with an eigenvalue estimate, the eigen-residual and a stopping
- * test (not in the reference: the benchmark spec extension).  x (host, length nor)
+ * test (not in the reference: an extension of the power method).  x (host, length nor)
  * holds the start vector on entry and the normalised eigenvector estimate on
  * return.  Iterates until ||A u - lambda u|| / |lambda| <= tol or max_it
  * iterations (max_it >= 2; tol = 0 runs exactly max_it SpMVs).  precision:
