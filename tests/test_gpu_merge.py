@@ -1,7 +1,7 @@
 """GPU parity of the merge-path CRS path (K1 partition, K2 SpMV + fix-up,
 power method) against the oracle, through the C ABI.
 
-Tolerances (the benchmark spec): SpMV rows within 2*nnz_row*u*sum|a_ij*x_j| (u = 2^-53)
+Tolerances: SpMV rows within 2*nnz_row*u*sum|a_ij*x_j| (u = 2^-53)
 of the oracle's CRS::mv; builders and merge-path coordinates bit-exact; power
 iterates at equal iteration counts within 1e-10 relative (eigenvalue
 estimates likewise); the reference's own known answers at its tolerances.
