@@ -174,6 +174,11 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
     const bool bnd_l = (rl == first_row && cross_lo) || (rl == last_row && cross_hi);
     const bool part_f = nv > 0 && (joins || bnd_f || (one_row && next_joins));
     const bool part_l = nv > 0 && !one_row && (next_joins || bnd_l);
+    // the lane where a partial first row ends adds the row once; unless the
+    // row continues in another chunk it is the row's only writer, so it
+    // starts from the y-window value and stores the total (no extra add)
+    const bool add_f = part_f && (!one_row || !next_joins);
+    const bool own_f = add_f && !bnd_f;
     // accumulate: rows inside the lane start from ys, partial rows from zero
     double pf = 0.0, pl = 0.0, acc = 0.0;
     int cur = -1;
@@ -189,7 +194,7 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
                         ys[cur] = acc;
                 }
                 cur = r;
-                acc = (r == rf && part_f) || (r == rl && part_l) ? 0.0 : ys[r];
+                acc = (r == rf && part_f && !own_f) || (r == rl && part_l) ? 0.0 : ys[r];
             }
             const double xv = GX ? __ldg(xg + gcs[j]) : xw[ids[j] & (uint32_t)(S - 1)];
             acc = fma(vs[j], xv, acc);
@@ -205,7 +210,6 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
     }
     // chains: lane l's tail value is the partial of its last row
     const double t = one_row ? pf : pl;
-    const bool add_f = part_f && (!one_row || !next_joins);  // partial first row ends here
     // a chain of lanes starts at a lane that is not a one-row lane joining
     // its predecessor; len = the earlier lanes of this lane's chain
     const unsigned starts = __ballot_sync(kFull, !(one_row && joins));
@@ -236,7 +240,7 @@ __device__ __forceinline__ void dense_oct(const Oct<K>& q, int S, const double* 
         if (bnd_f)
             atomicAdd(&ys[rf], tot);
         else
-            ys[rf] += tot;
+            ys[rf] = tot;  // tot started from ys[rf] (own_f)
     }
     if (part_l && !next_joins) atomicAdd(&ys[rl], pl);  // the chunk's last row, continued by another warp
 }
