@@ -33,10 +33,11 @@
 // close together in shared memory).  A row that lies inside one lane starts
 // from its y-window value and takes one FMA per element (the FP64 pipe, about
 // 2 operations per clock per SM here, is the scarce unit); a row split
-// across lanes is summed from zero in each and added once by the lane where
-// it ends, which gathers the chain's partials with shuffles (a segmented scan
-// for long rows); only a row that continues past the warp's chunk (the
-// element just outside has the same row) is added atomically.  The host
+// across lanes is summed from zero in each lane but the one where it ends,
+// which starts from the y-window value, gathers the chain's partials with
+// shuffles (a segmented scan for long rows) and stores the total; only a
+// row that continues past the warp's chunk (the element just outside has the
+// same row) is summed from zero everywhere and added atomically.  The host
 // arrays (pwmgpu_get_csb) stay the reference's.  Per row, the summation
 // order is the column order inside each dense unit and the order the atomics
 // land in elsewhere (the per-row error bound holds for any order).
