@@ -1,9 +1,10 @@
 """Build recipe for the oracle (test infrastructure only).
 
 ``build_oracle()`` compiles oracle/oracle.c (the C restatement) into
-oracle/_build/liboracle.so with gcc; ``build_ref()`` compiles the unmodified
-reference headers into oracle/_ref/libpwmref.so when the reference tree is
-present (development container only; see build_ref.sh).
+oracle/_build/liboracle.so with gcc; ``build_ref()`` runs build_ref.sh, which
+compiles the unmodified reference headers into oracle/_ref/libpwmref.so when
+it finds the reference tree (development container only; on other machines it
+builds nothing).  ``reference_dir()`` is the tree the last build used.
 """
 import os
 import subprocess
@@ -13,7 +14,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpwmref.so")
 REF_STATS = os.path.join(HERE, "_ref", "calc_stats")
-REF_DIR = os.environ.get("PWM_REFERENCE_DIR", "/root/reference")
+REF_DIR_FILE = os.path.join(HERE, "_ref", "reference_dir.txt")
 
 
 def build_oracle(force=False):
@@ -32,9 +33,7 @@ def build_oracle(force=False):
 
 def build_ref(force=False):
     """Compile oracle/_ref from the reference tree; returns the path or None."""
-    if not os.path.isdir(os.path.join(REF_DIR, "Matrix")):
-        return None
-    if not force and os.path.exists(REF_LIB):
+    if not force and os.path.exists(REF_LIB) and reference_dir() is not None:
         srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(HERE, "ref_stats_main.cpp"),
                 os.path.join(HERE, "build_ref.sh")]
         outs = [REF_LIB, REF_STATS]
@@ -42,7 +41,18 @@ def build_ref(force=False):
                 min(os.path.getmtime(o) for o in outs) >= max(os.path.getmtime(p) for p in srcs):
             return REF_LIB
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
-    return REF_LIB
+    return REF_LIB if os.path.exists(REF_LIB) and reference_dir() is not None else None
+
+
+def reference_dir():
+    """The reference tree oracle/_ref was built from, or None when it was not
+    built or that tree is gone."""
+    try:
+        with open(REF_DIR_FILE) as f:
+            d = f.read().strip()
+    except OSError:
+        return None
+    return d if os.path.isdir(os.path.join(d, "Matrix")) else None
 
 
 if __name__ == "__main__":

@@ -170,5 +170,7 @@ if __name__ == "__main__":
     if "--stats" in sys.argv:
         make_stats()
     else:
-        main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PWM_REFERENCE_DIR", "/root/reference"))
+        if len(sys.argv) < 2 and not os.environ.get("PWM_REFERENCE_DIR"):
+            sys.exit("usage: make_golden.py REFERENCE_TREE (or set PWM_REFERENCE_DIR)")
+        main(sys.argv[1] if len(sys.argv) > 1 else os.environ["PWM_REFERENCE_DIR"])
         make_stats()

@@ -18,7 +18,6 @@ import pytest
 from conftest import ROOT
 from oracle import pyoracle as O
 
-REF = os.environ.get("PWM_REFERENCE_DIR", "/root/reference")
 CPP = os.path.join(ROOT, "tests", "cpp")
 
 
@@ -30,7 +29,10 @@ def _gxx():
 
 
 def test_header_compiles_against_reference_interface(tmp_path):
-    if not os.path.isdir(os.path.join(REF, "Matrix")):
+    from oracle.build import build_ref, reference_dir
+    build_ref()
+    REF = reference_dir()
+    if REF is None:
         pytest.skip("reference tree not present")
     cmd = [_gxx(), "-std=c++17", "-fsyntax-only", "-fopenmp", "-DNTBB", "-include", "cstring", "-include", "climits",
            "-I" + os.path.join(ROOT, "oracle", "ref_shim"), "-I" + REF, "-I" + os.path.join(ROOT, "include"),
@@ -58,12 +60,15 @@ def test_driver_builds_against_stand_in(tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("itype", ["u32", "int", "unsigned"])
 @pytest.mark.parametrize("method", [12, 13, 14, 15])
-def test_driver_runs_through_the_interface(tmp_path, method):
+def test_driver_runs_through_the_interface(tmp_path, method, itype):
+    """Every method with the index types the reference instantiates:
+    uint32_t (drivers), int and unsigned int (Tests/poisson.cpp:28,146)."""
     exe = _build_driver(tmp_path)
     m, n, it = 37, 23, 9
     out = str(tmp_path / "out.bin")
-    r = subprocess.run([exe, str(method), str(m), str(n), str(it), out], capture_output=True, text=True)
+    r = subprocess.run([exe, str(method), str(m), str(n), str(it), out, itype], capture_output=True, text=True)
     assert r.returncode == 0, (r.stdout, r.stderr)
     assert "threw=1" in r.stdout
     N = m * n
@@ -97,7 +102,8 @@ def test_driver_runs_through_the_interface(tmp_path, method):
     yb = np.frombuffer(raw, np.float64, R, off)
     assert np.all(np.abs(yb - O.crs_mv(B, xb)) <= O.row_error_bound(B, xb))
     off += 8 * R
-    srows = np.frombuffer(raw, np.uint32, nnz, off)
-    scols = np.frombuffer(raw, np.uint32, nnz, off + 4 * nnz)
+    idt = np.int32 if itype == "int" else np.uint32
+    srows = np.frombuffer(raw, idt, nnz, off)
+    scols = np.frombuffer(raw, idt, nnz, off + 4 * nnz)
     order = np.lexsort((np.array(cols), np.array(rows)))
     assert np.array_equal(srows, np.array(rows)[order]) and np.array_equal(scols, np.array(cols)[order])

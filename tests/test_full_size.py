@@ -115,3 +115,34 @@ def test_c2_poisson4096_other_formats(pwm, fmt):
     assert np.all(np.abs(_mv(M, x) - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
     ones = np.ones(A.noc)
     assert np.array_equal(_mv(M, ones), O.crs_mv(A, ones))
+
+
+@pytest.fixture(scope="module")
+def irregular():
+    """The irregular matrix's CRS arrays (oracle restatement of the device
+    generator) and a seeded start vector, shared by the format tests."""
+    B = O.random_crs(IRREGULAR["n"], IRREGULAR["seed"], IRREGULAR["length_dist"], IRREGULAR["mean_len"],
+                     IRREGULAR["sigma"], IRREGULAR["max_len"], IRREGULAR["band_permille"], IRREGULAR["band_half"])
+    x = np.random.default_rng(SEED + 2).random(B.noc)
+    return B, x, O.crs_mv(B, x), O.row_error_bound(B, x), O.power(B, x, 10)
+
+
+@pytest.mark.parametrize("fmt", ["csb", "coh"])
+def test_c3_irregular_other_formats(pwm, irregular, fmt):
+    """The irregular matrix (N = 4,194,304, lognormal row lengths up to 20,000,
+    70 % of the columns uniform over [0, N)) in the CSB format (the variant its
+    load-time tuner picks: flat units of sparse sub-squares with x gathered by
+    global column) and the CO-H format (24 partitions per SM): each SpMV row
+    within the bound of the oracle's CRS::mv, and 10 power iterations
+    (SOA_Implementations/CSB.hpp:651-663, BlockCOH.hpp:519-531) within 1e-10
+    of the oracle's CRS::powerIteration."""
+    import ctypes as C
+    B, x, ref, bound, (xr, yr) = irregular
+    sm = C.c_int()
+    pwm.lib().pwmgpu_device_info(C.byref(sm), None, None)
+    M = pwm.CSBCuda(1) if fmt == "csb" else pwm.COHCuda(24 * sm.value)
+    M.generateRandom(**IRREGULAR)
+    assert np.all(np.abs(_mv(M, x) - ref) <= bound)
+    xg, yg = x.copy(), np.zeros(B.nor)
+    M.powerIteration(xg, yg, 10)
+    np.testing.assert_allclose(xg, xr, rtol=1e-10, atol=1e-15)

@@ -101,9 +101,12 @@ __global__ void __launch_bounds__(256) k_noalloc_spmv(const int32_t* __restrict_
             double sum = acc;
             int u = lane + 1;
             for (; u < 32 && crow[u] == a; ++u) sum += cval[u];
+            // A row below rw1 ends inside this sub-tile, so some lane at or
+            // after the leader completes it and the run stops before lane 32;
+            // the u < 32 test keeps hval[u] inside this warp's slice anyway.
             if (a < rw1) {
                 const int b0u = kw0 + u * qm + (u < rem ? u : rem);
-                if (__ldg(row_start + a) < b0u) y[a] = hval[u] + sum;
+                if (u < 32 && __ldg(row_start + a) < b0u) y[a] = hval[u] + sum;
             } else if (a < nor) {
                 carries[s] = sum;
             }
@@ -114,6 +117,7 @@ __global__ void __launch_bounds__(256) k_noalloc_spmv(const int32_t* __restrict_
 
 std::mutex g_mu;
 void* g_scratch_addr[64] = {nullptr};  // per device ordinal
+int g_sm_count[64] = {0};              // SM count of that device, read with the address
 
 // Failures are reported through pwmgpu_last_error(), like every entry point.
 int nfail(int code, const char* fmt, ...) {
@@ -126,23 +130,30 @@ int nfail(int code, const char* fmt, ...) {
     return code;
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the array's name is only a host-side stand-in).
-int scratch_address(void** out) {
+// Device address of the scratch array on the current device and that
+// device's SM count, looked up once per device (the array's name is only a
+// host-side stand-in).
+int scratch_address(void** out, int* sms) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return nfail(PWMGPU_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= 64) return nfail(PWMGPU_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_scratch_addr[dev]) {
+        int count = 0;
+        e = cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || count < 1)
+            return nfail(PWMGPU_ERR_CUDA, "SM count of device %d: %s", dev, cudaGetErrorString(e));
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return nfail(PWMGPU_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
                          cudaGetErrorString(e));
+        g_sm_count[dev] = count;
         g_scratch_addr[dev] = p;
     }
     *out = g_scratch_addr[dev];
+    *sms = g_sm_count[dev];
     return PWMGPU_OK;
 }
 
@@ -165,7 +176,8 @@ extern "C" int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nn
     if (!row_start || !y || (nnz > 0 && (!col_ind || !vals || !x)))
         return nfail(PWMGPU_ERR_INVALID, "null device array");
     void* base = nullptr;
-    int rc = scratch_address(&base);
+    int sms = 1;
+    int rc = scratch_address(&base, &sms);
     if (rc != PWMGPU_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const long long total = (long long)nor + nnz;
@@ -176,9 +188,6 @@ extern "C" int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nn
     cudaError_t e = cudaMemsetAsync(carries, 0, sizeof(double) * (size_t)nsub, st);
     if (e == cudaSuccess) e = launch_merge_partition(row_start, nor, nnz, kNoAllocWM, nsub, subc, st);
     if (e == cudaSuccess) {
-        int dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         long long blocks = (nsub + 7) / 8;
         if (blocks > (long long)sms * 8) blocks = (long long)sms * 8;
         k_noalloc_spmv<<<(int)blocks, 256, 0, st>>>(row_start, col_ind, vals, subc, nsub, nor, x, y, carries);
@@ -190,9 +199,6 @@ extern "C" int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nn
         M.noc = noc;
         M.nnz = nnz;
         M.row_start = const_cast<int32_t*>(row_start);
-        int dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         e = launch_merge_fixup_f64(kModeSpmv, M, subc, nsub, y, carries, nullptr, fixup_grid(nsub, sms), st);
     }
     if (e != cudaSuccess) return nfail(PWMGPU_ERR_CUDA, "pwmgpu_mv_csr_device_noalloc: %s", cudaGetErrorString(e));
