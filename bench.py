@@ -197,12 +197,12 @@ def run_reference(args, world, rank):
 
 
 def coh_partitions(n, nnz, sm_count):
-    """CO-H partition count (the reference's thread count) for the GPU: a warp
-    per partition, 24 per SM.  More partitions make more, emptier blocks,
-    fewer leave warps idle (4096^2 stencil: 0.70 ms at 24 per SM, 0.85 at
-    32, 1.51 at 8; the irregular matrix prefers 8 per SM, 4.4 ms -- the
-    format autotuner times 8, 16, 24 and 32 per SM per matrix class); n and
-    nnz are unused."""
+    """CO-H partition count (the reference's thread count) for the GPU: 24
+    per SM.  The partitions split the rows by nonzero count as the
+    reference's threads do; the tile kernel runs their Hilbert-ordered blocks
+    window by window, so the count only moves partition boundaries (beta
+    depends on the column count for square matrices); n and nnz are
+    unused."""
     return 24 * sm_count
 
 
@@ -232,8 +232,7 @@ def autotune_report(pwm, torch, stream, load, load_same_class, x, y, B):
         if t["timed"]:
             rec["candidates_ms"] = {"merge": round(t["merge_ms"], 5),
                                     **{"csb_v%d" % v: round(t["csb_ms"][v], 5) for v in range(4)},
-                                    **{"coh_%d_per_sm" % p: round(t["coh_ms"][i], 5)
-                                       for i, p in enumerate((8, 16, 24, 32))}}
+                                    **{"coh_v%d" % v: round(t["coh_ms"][v], 5) for v in range(4)}}
         if tag == "first_of_class":
             for _ in range(3):
                 A.mv_device(x.data_ptr(), y.data_ptr())
@@ -360,10 +359,11 @@ def _stream_specs(rng, count):
     return specs
 
 
-def _submit(svc, kind, kw, precision, max_it, tol):
+def _submit(svc, kind, kw, precision, max_it, tol, keep=False):
     if kind == "poisson":
-        return svc.submit_poisson(kw["m"], kw["n"], max_it=max_it, tol=tol, precision=precision, x0_seed=11)
-    return svc.submit_random(max_it=max_it, tol=tol, precision=precision, x0_seed=11, **kw)
+        return svc.submit_poisson(kw["m"], kw["n"], max_it=max_it, tol=tol, precision=precision, x0_seed=11,
+                                  keep_vector=keep)
+    return svc.submit_random(max_it=max_it, tol=tol, precision=precision, x0_seed=11, keep_vector=keep, **kw)
 
 
 def seeded_uniform(n, seed):
@@ -379,13 +379,70 @@ def seeded_uniform(n, seed):
 
 
 def _one_at_a_time(pwm, kind, kw, max_it, tol):
+    """The plain FP64 merge-path path on one request: a fresh handle, the
+    matrix built on the device, pwmgpu_solve.  Returns (SolveInfo,
+    eigenvector)."""
     M = pwm.CRSCuda(1)
     if kind == "poisson":
         M.generatePoissonMatrix(kw["m"], kw["n"], 1)
     else:
         M.generateRandom(**kw)
     x = seeded_uniform(M.dims()[0], 11)  # the service's start vector for x0_seed = 11
-    return M.solve(x, max_it, tol, pwm.PREC_F64)
+    return M.solve(x, max_it, tol, pwm.PREC_F64), x
+
+
+def _oracle_matrix(kind, kw):
+    from oracle import pyoracle as O
+    if kind == "poisson":
+        return O.fill_poisson(kw["m"], kw["n"])
+    return O.random_crs(kw["n"], kw["seed"], kw["length_dist"], kw["mean_len"], kw["sigma"], kw["max_len"],
+                        kw["band_permille"], kw["band_half"])
+
+
+def _oracle_checks(rows):
+    """The FP64 oracle's check of returned eigenpairs: for each (kind, kw,
+    lambda, residual, converged, u) the oracle's Rayleigh quotient of u
+    (CRS::mv and sequential FP64 dots) gives lambda_o and the relative
+    eigen-residual res_o.  Reports the largest |lambda - lambda_o| /
+    |lambda_o|, the largest res_o over converged solves (the stopping target
+    is 1e-10), and the largest gap |res - res_o| between the residual the
+    GPU reported and the oracle's (both are FP64 sums of rounded terms, so a
+    residual near 1e-13 agrees to a few digits only)."""
+    from oracle import pyoracle as O
+    lam_err, res_conv, res_gap, n_conv = 0.0, 0.0, 0.0, 0
+    for kind, kw, lam, res, conv, u in rows:
+        lo, ro = O.rayleigh(_oracle_matrix(kind, kw), u)
+        lam_err = max(lam_err, abs(lam - lo) / abs(lo))
+        res_gap = max(res_gap, abs(res - ro))
+        if conv:
+            n_conv += 1
+            res_conv = max(res_conv, ro)
+    return {"checked": len(rows), "checked_converged": n_conv, "max_lambda_rel_err_vs_oracle": lam_err,
+            "max_residual_vs_oracle_converged": res_conv if n_conv else None,
+            "max_residual_abs_diff_gpu_vs_oracle": res_gap}
+
+
+def _check_set(specs, per_class=3, max_n=400000):
+    """Indices of the requests whose eigenpairs the oracle checks: the first
+    `per_class` Poisson grids and random matrices with at most max_n rows."""
+    out, seen = [], {"poisson": 0, "random": 0}
+    for i, (k, kw) in enumerate(specs):
+        n = kw["m"] * kw["n"] if k == "poisson" else kw["n"]
+        if n <= max_n and seen[k] < per_class:
+            out.append(i)
+            seen[k] += 1
+    return set(out)
+
+
+def _class_counts(specs, conv, iters, max_it):
+    """Per matrix class: requests, converged to the tolerance, and stopped at
+    the iteration cap."""
+    out = {}
+    for cls in ("poisson", "random"):
+        idx = [i for i, (k, _) in enumerate(specs) if k == cls]
+        out[cls] = {"requests": len(idx), "converged": int(sum(bool(conv[i]) for i in idx)),
+                    "capped_at_max_it": int(sum((not conv[i]) and iters[i] >= max_it for i in idx))}
+    return out
 
 
 def _stream_run(submit_fn, arrivals, step_fn, idle_fn):
@@ -407,50 +464,106 @@ def _stream_run(submit_fn, arrivals, step_fn, idle_fn):
     return idle_fn(t0)
 
 
+def _service_batch(pwm, S, specs, prec, max_it, tol, check):
+    """All requests submitted at once to a fresh service, run until idle."""
+    svc = S.Service(hbm_budget_bytes=150 << 30, round_iterations=8)
+    t0 = time.perf_counter()
+    ids = [_submit(svc, k, kw, prec, max_it, tol, keep=i in check) for i, (k, kw) in enumerate(specs)]
+    svc.run_until_idle()
+    el = time.perf_counter() - t0
+    res = [svc.result(i) for i in ids]
+    vecs = {i: svc.result(ids[i], want_vector=True)[1] for i in check}
+    st = svc.stats()
+    svc.close()
+    return el, res, vecs, st
+
+
 def serving(pwm, args):
     """Batch (256 uneven matrices) and serving-stream workloads: the batched
     service in mixed precision and in FP64 (one launch per power step for all
     live solves, graph-captured rounds) against the plain FP64 merge-path
-    path solving one request at a time (pwmgpu_solve per matrix)."""
+    path solving one request at a time (pwmgpu_solve per matrix).  Every
+    figure is split by matrix class (Poisson grids, random matrices); solves
+    that reach the 1e-10 residual are counted apart from solves stopped at the
+    2,000-step cap; a seeded subset of the returned eigenpairs is checked by
+    the FP64 oracle's Rayleigh quotient (outside the timed runs)."""
     from thesis_spmv_gb300 import service as S
     tol, max_it = 1e-10, 2000
     out = {}
 
     # ---- the 256-matrix batch, all submitted at once ----
     specs = _batch_specs(np.random.default_rng(20261203), args.batch_count)
+    check = _check_set(specs)
     batch = {}
     arms = (("service_mixed", pwm.PREC_MIXED), ("service_fp64", pwm.PREC_F64))
     if args.batch_only:
         arms = (("service_fp64", pwm.PREC_F64),)
+    lam = {}
     for name, prec in arms:
-        svc = S.Service(hbm_budget_bytes=150 << 30, round_iterations=8)
-        t0 = time.perf_counter()
-        ids = [_submit(svc, k, kw, prec, max_it, tol) for k, kw in specs]
-        svc.run_until_idle()
-        el = time.perf_counter() - t0
-        res = [svc.result(i) for i in ids]
-        batch[name] = {"seconds": round(el, 3), "solves_per_s": round(len(ids) / el, 2),
-                       "converged": int(sum(r.converged for r in res)),
-                       "steps_total": int(sum(r.iterations for r in res)),
-                       "steps_low_precision": int(sum(r.iterations_low for r in res)),
-                       "rounds": int(svc.stats().rounds), "gpu_round_ms": round(svc.stats().gpu_round_ms, 1)}
-        if name == "service_mixed":
-            lam_mixed = [r.lambda_ for r in res]
-        else:
-            lam64 = [r.lambda_ for r in res]
-        svc.close()
+        el, res, vecs, st = _service_batch(pwm, S, specs, prec, max_it, tol, check)
+        conv = [r.converged for r in res]
+        rec = {"seconds": round(el, 3), "solves_per_s": round(len(res) / el, 2),
+               "converged": int(sum(conv)), "converged_solves_per_s": round(sum(conv) / el, 2),
+               "capped_at_max_it": int(sum((not r.converged) and r.iterations >= max_it for r in res)),
+               "steps_total": int(sum(r.iterations for r in res)),
+               "steps_low_precision": int(sum(r.iterations_low for r in res)),
+               "max_reported_residual_converged": max([r.residual for r in res if r.converged], default=None),
+               "rounds": int(st.rounds), "gpu_round_ms": round(st.gpu_round_ms, 1),
+               "by_class": _class_counts(specs, conv, [r.iterations for r in res], max_it)}
+        if not args.batch_only:
+            rec["oracle_check"] = _oracle_checks([(specs[i][0], specs[i][1], res[i].lambda_, res[i].residual,
+                                                   res[i].converged, vecs[i]) for i in sorted(check)])
+        lam[name] = [r.lambda_ for r in res]
+        batch[name] = rec
     if args.batch_only:
         return {"batch_256": batch}
+    # the plain FP64 path, one request at a time (sequential: each class's
+    # solves/s is its requests over the time its own solves took)
+    t_req, one, vecs = [], [], {}
     t0 = time.perf_counter()
-    one = [_one_at_a_time(pwm, k, kw, max_it, tol) for k, kw in specs]
+    for i, (k, kw) in enumerate(specs):
+        ts = time.perf_counter()
+        info, u = _one_at_a_time(pwm, k, kw, max_it, tol)
+        t_req.append(time.perf_counter() - ts)
+        one.append(info)
+        if i in check:
+            vecs[i] = u
     el = time.perf_counter() - t0
-    batch["one_at_a_time_fp64"] = {"seconds": round(el, 3), "solves_per_s": round(len(specs) / el, 2),
-                                   "converged": int(sum(r.converged for r in one)),
-                                   "steps_total": int(sum(r.iterations for r in one))}
-    diffs = [abs(a - b) / abs(b) for a, b in zip(lam_mixed, lam64)]
+    conv = [r.converged for r in one]
+    batch["one_at_a_time_fp64"] = {
+        "seconds": round(el, 3), "solves_per_s": round(len(specs) / el, 2), "converged": int(sum(conv)),
+        "converged_solves_per_s": round(sum(conv) / el, 2),
+        "capped_at_max_it": int(sum((not r.converged) and r.iterations >= max_it for r in one)),
+        "steps_total": int(sum(r.iterations for r in one)),
+        "by_class": _class_counts(specs, conv, [r.iterations for r in one], max_it),
+        "oracle_check": _oracle_checks([(specs[i][0], specs[i][1], one[i].lambda_, one[i].residual,
+                                         one[i].converged, vecs[i]) for i in sorted(check)])}
+    diffs = [abs(a - b) / abs(b) for a, b in zip(lam["service_mixed"], lam["service_fp64"])]
     batch["lambda_rel_diff_mixed_vs_fp64"] = {"max": max(diffs), "median": float(np.median(diffs))}
     batch["speedup_service_mixed_vs_one_at_a_time_fp64"] = round(
         batch["service_mixed"]["solves_per_s"] / batch["one_at_a_time_fp64"]["solves_per_s"], 3)
+    # per class: each class alone through the service arms; the one-at-a-time
+    # time of a class is the sum of its own solves' times
+    per_class = {}
+    for cls in ("poisson", "random"):
+        sub = [(k, kw) for k, kw in specs if k == cls]
+        row = {}
+        for name, prec in arms:
+            el, res, _, _ = _service_batch(pwm, S, sub, prec, max_it, tol, set())
+            row[name] = {"solves_per_s": round(len(sub) / el, 2),
+                         "converged": int(sum(r.converged for r in res)),
+                         "converged_solves_per_s": round(sum(r.converged for r in res) / el, 2)}
+        t_cls = sum(t for t, (k, _) in zip(t_req, specs) if k == cls)
+        n_conv = sum(bool(r.converged) for r, (k, _) in zip(one, specs) if k == cls)
+        row["one_at_a_time_fp64"] = {"solves_per_s": round(len(sub) / t_cls, 2), "converged": n_conv,
+                                     "converged_solves_per_s": round(n_conv / t_cls, 2)}
+        row["speedup_service_mixed_vs_one_at_a_time_fp64"] = round(
+            row["service_mixed"]["solves_per_s"] / row["one_at_a_time_fp64"]["solves_per_s"], 3)
+        row["speedup_service_mixed_vs_service_fp64"] = round(
+            row["service_mixed"]["solves_per_s"] / row["service_fp64"]["solves_per_s"], 3)
+        row["target_2x_vs_one_at_a_time_fp64_met"] = row["speedup_service_mixed_vs_one_at_a_time_fp64"] >= 2.0
+        per_class[cls] = row
+    batch["per_class"] = per_class
     out["batch_256"] = dict(workload="128 Poisson grids (side U[32,1024]) + 128 random (N log-uniform [1e3,1e6], "
                                      "Poisson(8) rows); tol 1e-10 or 2000 steps", **batch)
 
@@ -458,6 +571,21 @@ def serving(pwm, args):
     stream = {}
     R = args.stream_requests
     specs = _stream_specs(np.random.default_rng(7), R)
+    check = _check_set(specs, per_class=2, max_n=300000)
+    kinds = np.array([k for k, _ in specs])
+
+    def lat_stats(lat, conv, span):
+        rec = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
+               "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
+               "solves_per_s": round(R / span, 2), "converged": int(np.sum(conv)),
+               "converged_solves_per_s": round(float(np.sum(conv)) / span, 2)}
+        for cls in ("poisson", "random"):
+            sel = kinds == cls
+            rec[cls] = {"p50_ms": round(float(np.percentile(lat[sel], 50)) * 1e3, 2),
+                        "p99_ms": round(float(np.percentile(lat[sel], 99)) * 1e3, 2),
+                        "requests": int(sel.sum()), "converged": int(np.sum(conv[sel]))}
+        return rec
+
     for rate in args.stream_rates:
         arr = np.cumsum(np.random.default_rng(int(rate)).exponential(1.0 / rate, R))
         arr -= arr[0]
@@ -469,39 +597,48 @@ def serving(pwm, args):
 
             def submit_fn(i, t0, svc=svc, ids=ids, prec=prec):
                 k, kw = specs[i]
-                ids[i] = _submit(svc, k, kw, prec, max_it, tol)
+                ids[i] = _submit(svc, k, kw, prec, max_it, tol, keep=i in check)
 
             def step_fn(svc=svc):
                 live, queued, _ = svc.step()
                 return live > 0 or queued > 0
 
             def idle_fn(t0, svc=svc, ids=ids, arr=arr, t_create=t_create):
-                lat = []
+                lat = np.zeros(R)
                 for i, rid in ids.items():
                     r = svc.result(rid)
-                    lat.append(r.t_done + (t_create - t0) - arr[i])
-                return np.array(lat)
+                    lat[i] = r.t_done + (t_create - t0) - arr[i]
+                return lat
 
             lat = _stream_run(submit_fn, arr, step_fn, idle_fn)
-            row[name] = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
-                         "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
-                         "solves_per_s": round(R / max(float(np.max(lat + arr)), 1e-9), 2)}
+            res = [svc.result(ids[i]) for i in range(R)]
+            rec = lat_stats(lat, np.array([r.converged for r in res], bool), max(float(np.max(lat + arr)), 1e-9))
+            rec["oracle_check"] = _oracle_checks([(specs[i][0], specs[i][1], res[i].lambda_, res[i].residual,
+                                                   res[i].converged, svc.result(ids[i], want_vector=True)[1])
+                                                  for i in sorted(check)])
+            row[name] = rec
             svc.close()
         # plain FP64 path, one request at a time in arrival order
-        done_t = []
+        done_t, one, vecs = [], [], {}
         t0 = time.perf_counter()
         for i, (k, kw) in enumerate(specs):
             now = time.perf_counter() - t0
             if arr[i] > now:
                 time.sleep(arr[i] - now)
-            _one_at_a_time(pwm, k, kw, max_it, tol)
+            info, u = _one_at_a_time(pwm, k, kw, max_it, tol)
             done_t.append(time.perf_counter() - t0)
+            one.append(info)
+            if i in check:
+                vecs[i] = u
         lat = np.array(done_t) - arr
-        row["one_at_a_time_fp64"] = {"p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 2),
-                                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 2),
-                                     "solves_per_s": round(R / max(done_t[-1], 1e-9), 2)}
+        rec = lat_stats(lat, np.array([r.converged for r in one], bool), max(done_t[-1], 1e-9))
+        rec["oracle_check"] = _oracle_checks([(specs[i][0], specs[i][1], one[i].lambda_, one[i].residual,
+                                               one[i].converged, vecs[i]) for i in sorted(check)])
+        row["one_at_a_time_fp64"] = rec
+        row["speedup_service_mixed_vs_one_at_a_time_fp64"] = round(
+            row["service_mixed"]["solves_per_s"] / row["one_at_a_time_fp64"]["solves_per_s"], 3)
         stream["rate_%g_per_s" % rate] = row
-    out["serving_stream"] = dict(workload="%d requests, N log-uniform [1e4, 4e6], half Poisson grids, half "
+    out["serving_stream"] = dict(workload="%d requests per rate, N log-uniform [1e4, 4e6], half Poisson grids, half "
                                           "lognormal-row random; Poisson arrivals; tol 1e-10 or 2000 steps; HBM "
                                           "budget 150 GB" % R, **stream)
     return out
@@ -549,6 +686,55 @@ def triplet_load(pwm, torch, dev, M, N, cpu=True):
                                "sample": "%d shuffled triplets of the 1024x1024 Poisson matrix "
                                          "(TripletToCRS restated in oracle/oracle.c)" % r0.size}
     return out
+
+
+def run_case(args):
+    """--case: one kernel on one matrix, for profiling (a small launch count
+    before the timed ones): the irregular lognormal-row matrix with
+    --case-n rows or the Poisson grid --grid, in the format --case-format
+    (merge, csb, coh with 24 partitions per SM, or "power": --steps
+    iterations of the power method in one pwmgpu_power_device call, AUTO
+    mode).  Prints ms per SpMV / iteration and GB/s of CRS algorithmic
+    bytes."""
+    import torch
+    import thesis_spmv_gb300 as pwm
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fmt = args.case_format
+    cls = {"merge": pwm.CRSCuda, "power": pwm.CRSCuda, "csb": pwm.CSBCuda, "coh": pwm.COHCuda}[fmt]
+    M = cls(coh_partitions(0, 0, sm) if fmt == "coh" else 1)
+    stream = torch.cuda.Stream(device=dev)
+    M.set_stream(stream.cuda_stream)
+    if args.case == "irregular":
+        M.generateRandom(**dict(IRREGULAR, n=args.case_n))
+        workload = "lognormal_rows_n%d_mean16_sigma1.2_band30pct" % args.case_n
+    else:
+        M.generatePoissonMatrix(args.grid, args.grid, 1)
+        workload = "poisson2d_%dx%d" % (args.grid, args.grid)
+    N, _, nnz = M.dims()
+    B = algorithmic_bytes(N, nnz)
+    x = torch.rand(N, dtype=torch.float64, generator=torch.Generator().manual_seed(5)).to(dev)
+    y = torch.zeros_like(x)
+
+    if fmt == "power":
+        M.power_device(x.data_ptr(), y.data_ptr(), max(args.warmup, 1))
+    else:
+        for _ in range(args.warmup):
+            M.mv_device(x.data_ptr(), y.data_ptr())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    if fmt == "power":
+        M.power_device(x.data_ptr(), y.data_ptr(), args.steps)
+    else:
+        for _ in range(args.steps):
+            M.mv_device(x.data_ptr(), y.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"case": args.case, "format": fmt, "workload": workload, "N": N, "nnz": nnz,
+                      "ms_per_launch": round(ms, 5), "gb_s_crs_bytes": round(B / (ms * 1e-3) / 1e9, 2)}))
 
 
 def run_ours(args, world, rank, local):
@@ -698,10 +884,13 @@ def run_ours(args, world, rank, local):
         "power": {"iterations": p_it,
                   "fused": {"ms_per_iteration": round(power_ms["fused"] / p_it, 5),
                             "gb_s": round(B / (power_ms["fused"] / p_it * 1e-3) / 1e9, 2),
-                            "kernels": "k_power_persistent (1 launch for all iterations)"},
+                            "kernels": "k_power_persistent (1 launch for all iterations; SpMV pass, barrier, "
+                                       "fix-up pass, barrier per iteration)"},
                   "multi": {"ms_per_iteration": round(power_ms["multi"] / p_it, 5),
                             "gb_s": round(B / (power_ms["multi"] / p_it * 1e-3) / 1e9, 2),
-                            "kernels": "k_merge_spmv + k_fix_runs + k_power_norm per iteration"}},
+                            "kernels": "k_merge_spmv + k_fix_runs per iteration (the rescale from the "
+                                       "largest magnitude key; the last two iterations sum ||y||^2 in the "
+                                       "same two kernels)"}},
         "clocks": clk.summary(),
     }
     if formats:
@@ -739,9 +928,16 @@ def main():
                     help="Poisson grids and random matrices in the batch (128 each)")
     ap.add_argument("--batch-only", action="store_true",
                     help="only the 256-matrix batch through the FP64 service (a profiling case)")
-    ap.add_argument("--stream-requests", type=int, default=48)
+    ap.add_argument("--stream-requests", type=int, default=300)
     ap.add_argument("--stream-rates", type=float, nargs="+", default=[50.0, 100.0, 200.0, 500.0, 1000.0, 2000.0])
+    ap.add_argument("--case", choices=["irregular", "poisson"],
+                    help="profiling case: one kernel on one matrix (see run_case)")
+    ap.add_argument("--case-n", type=int, default=1 << 21, help="rows of the irregular matrix of --case irregular")
+    ap.add_argument("--case-format", default="merge", choices=["merge", "csb", "coh", "power"])
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -152,7 +152,8 @@ int pwmgpu_stats(pwmgpu_matrix* m, pwmgpu_matrix_stats* out);
  * (the merge tuner's threshold) run merge. */
 typedef struct {
     int32_t format;          /* PWMGPU_FMT_MERGE / _CSB / _COH: the FP64 SpMV in use */
-    int32_t csb_variant;     /* CSB kernel variant: bit 0 = 8 elements per lane, bit 1 = 256 threads */
+    int32_t csb_variant;     /* tile kernel variant of a CSB or CO-H choice: bit 0 = 8 elements per lane,
+                                bit 1 = 256 threads */
     int32_t merge_variant;   /* merge launch variant (pwmgpu_launch_config) */
     int32_t cache_hit;       /* 1: taken from the class table without timing */
     int32_t timed;           /* 1: candidates were timed for this matrix */
@@ -160,7 +161,7 @@ typedef struct {
     int32_t coh_partitions;  /* CO-H partitions when CO-H is the format */
     float merge_ms;          /* ms per SpMV of the best merge variant (0 if not timed) */
     float csb_ms[4];         /* per CSB variant */
-    float coh_ms[4];         /* per CO-H partition count: 8, 16, 24, 32 per SM */
+    float coh_ms[4];         /* per tile kernel variant on the CO-H tiles (24 partitions per SM) */
     double tune_seconds;     /* wall time of the tuning (builds and timings) */
 } pwmgpu_tuning;
 int pwmgpu_tuning_info(const pwmgpu_matrix* m, pwmgpu_tuning* out);
@@ -172,7 +173,8 @@ int pwmgpu_tuner_reset(void);
 /* Number of classes recorded. */
 int pwmgpu_tuner_size(void);
 /* Record a class choice (to carry tunings between processes): format
- * PWMGPU_FMT_MERGE / _CSB / _COH, csb_variant 0..3, merge_variant one of
+ * PWMGPU_FMT_MERGE / _CSB / _COH, csb_variant 0..3 (the tile kernel variant
+ * of CSB and CO-H), merge_variant one of
  * the merge launch variants (0, 1, 4, 5), coh_parts_per_sm 1..64 (CO-H
  * partitions per SM; 0: 24). */
 int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_variant, int32_t merge_variant,
@@ -181,9 +183,10 @@ int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_varian
  * {format, csb_variant, merge_variant, coh_parts_per_sm}; returns the number
  * copied (or a negative status). */
 int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices);
-/* CSB kernel variant of a PWMGPU_FMT_CSB handle (0..3, as csb_variant
- * above).  Loading a matrix large enough to time (the merge tuner's
- * threshold) picks the fastest of the four; smaller ones get 0. */
+/* Tile kernel variant of a PWMGPU_FMT_CSB or PWMGPU_FMT_COH handle (both
+ * formats run as tiles of one kernel; 0..3, as csb_variant above).  Loading
+ * a matrix large enough to time (the merge tuner's threshold) picks the
+ * fastest of the four; smaller ones get 0. */
 int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant);
 int pwmgpu_get_csb_variant(const pwmgpu_matrix* m, int32_t* variant);
 
@@ -218,6 +221,16 @@ int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
 #define PWMGPU_POWER_FUSED 1
 #define PWMGPU_POWER_MULTI 2
 int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode);
+
+/* Failure-path testing hook (not in the reference): the grid barriers of the
+ * persistent power kernel wait at most `cycles` clock64 cycles (the default is
+ * about 2 s, 4e9 cycles) and open once every CTA of the grid plus `extra`
+ * more have arrived (extra = 0 normally).  With extra = 1 no barrier can
+ * open: every CTA gives up after `cycles`, lets its copies in flight land,
+ * records PWMGPU_ERR_TIMEOUT and returns, and the call reports that status;
+ * the handle stays usable.  cycles in [1e4, 4e9], extra 0 or 1; pass
+ * (0, 0) to restore the default. */
+int pwmgpu_test_grid_wait(pwmgpu_matrix* m, int64_t cycles, int32_t extra);
 
 /* Storage the FP32 / BF16 iterations (pwmgpu_solve's low-precision phase,
  * pwmgpu_mv_device_f32) stream (not in the reference).  AUTO (default): a
@@ -280,6 +293,40 @@ int pwmgpu_merge_partition(pwmgpu_matrix* m, int32_t parts, int32_t* coords);
 int pwmgpu_mv_csr_device_noalloc(int32_t nor, int32_t noc, int32_t nnz, const int32_t* row_start,
                                  const int32_t* col_ind, const double* vals, const double* x, double* y,
                                  void* stream);
+
+/* ---- Row-sharded power method (one rank per GPU) ----
+ * The reference's distributed power method (MPI_driver_poisson.cpp:38-63)
+ * gives each rank a block of consecutive rows: y_loc = A_loc x, the sum of
+ * squares of y_loc, an allreduce of those sums (:50), y_loc /= ||y||, and
+ * an allgather of the blocks into x (:61).  These entry points are the
+ * per-rank device work; the host mirror (thesis_spmv_gb300/sharded.py) runs
+ * the two collectives with torch.distributed between them.
+ *
+ * Row blocks of the reference's 1D split (Util/TripletToCRS.hpp:318-327,
+ * MPI_driver_poisson.cpp:84-89): nor / parts rows per block (integer
+ * division), the last block takes the rest.  Host only; parts >= 1. */
+int pwmgpu_row_blocks(int32_t nor, int32_t parts, int32_t* first_rows, int32_t* thread_rows);
+/* Rows [first_row, last_row) of the mx x ny Poisson matrix as a
+ * (last_row - first_row) x (mx * ny) matrix with global columns: the
+ * reference's fillPoisson with first_row / last_row (Util/Poisson.hpp:33-83),
+ * built on the device. */
+int pwmgpu_generate_poisson_rows(pwmgpu_matrix* m, int32_t mx, int32_t ny, int32_t first_row, int32_t last_row);
+/* Rows [first_row, last_row) of an nor x noc triplet matrix as a
+ * (last_row - first_row) x noc CRS matrix with global columns: one block of
+ * the reference's TripletToMultipleCRS (Util/TripletToCRS.hpp:309-385),
+ * sorted on the device like pwmgpu_load_triplets.  Every row index must lie
+ * in [0, nor); the caller's arrays are left unchanged (the reference sorts
+ * the whole triplet by row in place). */
+int pwmgpu_load_triplets_rows(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* rows,
+                              const int32_t* cols, const double* vals, int32_t first_row, int32_t last_row);
+/* A rank's part of one step (MPI_driver_poisson.cpp:41-47): dy_loc = A_loc
+ * dx_full (dx_full: all noc entries), and *dnsq_loc = sum of dy_loc[i]^2 in a
+ * fixed order (a device double).  Asynchronous on the handle's stream. */
+int pwmgpu_rows_step_device(pwmgpu_matrix* m, const double* dx_full, double* dy_loc, double* dnsq_loc);
+/* dy_loc[i] *= 1 / sqrt(*dnsq_total) for the handle's rows (the reference
+ * divides by the norm, MPI_driver_poisson.cpp:53-57; the reciprocal is within
+ * one ulp of the quotient).  Asynchronous on the handle's stream. */
+int pwmgpu_rows_normalize_device(pwmgpu_matrix* m, double* dy_loc, const double* dnsq_total);
 
 /* The CSB arrays of a PWMGPU_FMT_CSB handle, as CSB.hpp:464-567 builds them
  * (for checks against the reference): beta, block bits, horizontal and

@@ -129,6 +129,104 @@ void orc_triplet_to_crs(int32_t nnz, int32_t nor, int32_t* rows, int32_t* cols, 
     }
 }
 
+void orc_row_blocks(int32_t nor, int32_t parts, int32_t* first_rows, int32_t* thread_rows) {
+    /* Util/TripletToCRS.hpp:318-327: am_rows = round(nor / partitions) on
+     * integers (the division already truncates), first_rows[i] = previous
+     * last row, the last partition ends at nor. */
+    const int32_t am = nor / parts;
+    int32_t last = 0;
+    for (int32_t i = 0; i < parts; ++i) {
+        first_rows[i] = last;
+        last = (i == parts - 1) ? nor : first_rows[i] + am;
+        thread_rows[i] = last - first_rows[i];
+    }
+}
+
+void orc_triplet_to_multi_crs(int32_t nnz, int32_t nor, int32_t parts, int32_t* rows, int32_t* cols, double* vals,
+                              int32_t* first_rows, int32_t* thread_rows, int32_t* row_start_all, int32_t* col_all,
+                              double* data_all) {
+    /* Util/TripletToCRS.hpp:309-385: sort on rows (columns follow), then per
+     * partition copy its entries, fill the local row starts (empty rows
+     * repeat the index, trailing rows get the partition's count) and sort
+     * each row's columns.  Sorting the whole triplet by (row, column) first
+     * gives the same arrays for unique coordinates. */
+    sort_row_col(nnz, rows, cols, vals);
+    orc_row_blocks(nor, parts, first_rows, thread_rows);
+    int32_t k = 0, base = 0;
+    for (int32_t p = 0; p < parts; ++p) {
+        int32_t* rs = row_start_all + base;
+        const int32_t last = first_rows[p] + thread_rows[p];
+        const int32_t k0 = k;
+        int32_t row_index = 0;
+        rs[0] = 0;
+        while (k < nnz && rows[k] < last) {
+            col_all[k] = cols[k];
+            data_all[k] = vals[k];
+            while (rows[k] != row_index + first_rows[p]) {
+                row_index++;
+                rs[row_index] = k - k0;
+            }
+            ++k;
+        }
+        while (row_index < thread_rows[p]) {
+            row_index++;
+            rs[row_index] = k - k0;
+        }
+        base += thread_rows[p] + 1;
+    }
+}
+
+void orc_fill_poisson_rows(int32_t m, int32_t n, int32_t first_row, int32_t last_row, int32_t* row_start,
+                           int32_t* col_ind, double* data) {
+    /* Util/Poisson.hpp:33-83 with a row range: the same per-row entries as
+     * orc_fill_poisson, row starts counted from the block's first row. */
+    int32_t k = 0;
+    row_start[0] = 0;
+    for (int32_t row = first_row; row < last_row; ++row) {
+        if (row >= m) { data[k] = -1; col_ind[k] = row - m; ++k; }
+        if (row % m != 0) { data[k] = -1; col_ind[k] = row - 1; ++k; }
+        data[k] = 4; col_ind[k] = row; ++k;
+        if (row % m != m - 1) { data[k] = -1; col_ind[k] = row + 1; ++k; }
+        if (row < m * n - m) { data[k] = -1; col_ind[k] = m + row; ++k; }
+        row_start[row - first_row + 1] = k;
+    }
+}
+
+void orc_power_rows(int32_t nor, int32_t parts, const int32_t* rs_all, const int32_t* ci, const double* d, double* x,
+                    int32_t it) {
+    /* MPI_driver_poisson.cpp:38-63, every rank in turn */
+    int32_t* first = (int32_t*)malloc(sizeof(int32_t) * (size_t)parts);
+    int32_t* nrow = (int32_t*)malloc(sizeof(int32_t) * (size_t)parts);
+    double* part = (double*)malloc(sizeof(double) * (size_t)parts);
+    double* y = (double*)malloc(sizeof(double) * (size_t)(nor > 0 ? nor : 1));
+    orc_row_blocks(nor, parts, first, nrow);
+    for (int32_t i = 0; i < it; ++i) {
+        int32_t base = 0, k0 = 0;
+        for (int32_t p = 0; p < parts; ++p) {
+            const int32_t* rs = rs_all + base;
+            double* yp = y + first[p];
+            for (int32_t l = 0; l < nrow[p]; ++l) {  /* mv, :24-35 */
+                double sum = 0;
+                for (int32_t k = rs[l]; k < rs[l + 1]; ++k) sum += d[k0 + k] * x[ci[k0 + k]];
+                yp[l] = sum;
+            }
+            double np = 0;  /* :44-47 */
+            for (int32_t l = 0; l < nrow[p]; ++l) np += yp[l] * yp[l];
+            part[p] = np;
+            k0 += rs[nrow[p]];
+            base += nrow[p] + 1;
+        }
+        double norm = 0;  /* :50, rank order */
+        for (int32_t p = 0; p < parts; ++p) norm += part[p];
+        norm = sqrt(norm);
+        for (int32_t r = 0; r < nor; ++r) x[r] = y[r] / norm;  /* :53-61 */
+    }
+    free(first);
+    free(nrow);
+    free(part);
+    free(y);
+}
+
 /* ------------------------------------------------------------------ */
 /* CRS mv                                                               */
 /* ------------------------------------------------------------------ */

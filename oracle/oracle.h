@@ -36,6 +36,33 @@ void orc_triplet_poisson(int32_t m, int32_t n, int32_t* rows, int32_t* cols, dou
 void orc_triplet_to_crs(int32_t nnz, int32_t nor, int32_t* rows, int32_t* cols, double* vals,
                         int32_t* row_start, int32_t* col_ind, double* crs_data);
 
+/* Row blocks of the reference's 1D split (Util/TripletToCRS.hpp:318-327,
+ * MPI_driver_poisson.cpp:84-89): am = nor / parts rows per block (integer
+ * division), the last block takes the rest. */
+void orc_row_blocks(int32_t nor, int32_t parts, int32_t* first_rows, int32_t* thread_rows);
+/* Util/TripletToCRS.hpp:309-385 (TripletToMultipleCRS): the triplet sorted
+ * in place like TripletToCRS, then one CRS per row block with local row
+ * starts and global columns.  Outputs are concatenated: block p's row starts
+ * (thread_rows[p] + 1 entries) follow block p-1's; columns and values of the
+ * blocks are consecutive (nnz in total).  A block without nonzeros gets all
+ * row starts 0 (the reference reads into the next block there). */
+void orc_triplet_to_multi_crs(int32_t nnz, int32_t nor, int32_t parts, int32_t* rows, int32_t* cols, double* vals,
+                              int32_t* first_rows, int32_t* thread_rows, int32_t* row_start_all, int32_t* col_all,
+                              double* data_all);
+/* Util/Poisson.hpp:33-83 with first_row / last_row: rows [first_row,
+ * last_row) of the m x n Poisson matrix, local row starts, global columns. */
+void orc_fill_poisson_rows(int32_t m, int32_t n, int32_t first_row, int32_t last_row, int32_t* row_start,
+                           int32_t* col_ind, double* data);
+/* MPI_driver_poisson.cpp:38-63 (powerIteration over `parts` ranks), in one
+ * process: per iteration every block's mv (:24-35, a row sum from 0), every
+ * block's sum of squares in row order (:44-47), the blocks' sums added in
+ * rank order (the MPI_Allreduce of :50), norm = sqrt, y /= norm per element
+ * (:53-57) and the full x assembled from the blocks (MPI_Allgatherv, :61).
+ * rs_all / ci / d: the blocks as orc_triplet_to_multi_crs writes them; x:
+ * all nor entries in, the normalised iterate after `it` iterations out. */
+void orc_power_rows(int32_t nor, int32_t parts, const int32_t* rs_all, const int32_t* ci, const double* d, double* x,
+                    int32_t it);
+
 /* Matrix/CRS.hpp:99-109 (sequential CRS::mv). */
 void orc_crs_mv(int32_t nor, const int32_t* row_start, const int32_t* col_ind, const double* data,
                 const double* x, double* y);

@@ -30,6 +30,11 @@ def lib():
         L.orc_triplet_poisson.argtypes = [C.c_int32, C.c_int32, I32P, I32P, F64P]
         L.orc_triplet_to_crs.argtypes = [C.c_int32, C.c_int32, I32P, I32P, F64P, I32P, I32P, F64P]
         L.orc_crs_mv.argtypes = [C.c_int32, I32P, I32P, F64P, F64P, F64P]
+        L.orc_row_blocks.argtypes = [C.c_int32, C.c_int32, I32P, I32P]
+        L.orc_triplet_to_multi_crs.argtypes = [C.c_int32, C.c_int32, C.c_int32, I32P, I32P, F64P, I32P, I32P, I32P,
+                                               I32P, F64P]
+        L.orc_fill_poisson_rows.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, I32P, I32P, F64P]
+        L.orc_power_rows.argtypes = [C.c_int32, C.c_int32, I32P, I32P, F64P, F64P, C.c_int32]
         L.orc_crs_omp_mv.argtypes = [C.c_int32, I32P, I32P, F64P, F64P, F64P, C.c_int]
         L.orc_merge_search.argtypes = [C.c_int32, C.c_int32, C.c_int32, I32P, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int32)]
@@ -114,6 +119,61 @@ def triplet_to_crs(nor, noc, rows, cols, vals):
     if nnz:
         lib().orc_triplet_to_crs(nnz, nor, rows, cols, vals, rs, ci, d)
     return CRSArrays(nor, noc, rs, ci[:nnz], d[:nnz])
+
+
+def row_blocks(nor, parts):
+    """(first_rows, thread_rows) of the reference's 1D row split."""
+    f = np.zeros(parts, np.int32)
+    t = np.zeros(parts, np.int32)
+    lib().orc_row_blocks(int(nor), int(parts), f, t)
+    return f, t
+
+
+def triplet_to_multi_crs(nor, noc, rows, cols, vals, parts):
+    """TripletToMultipleCRS: list of CRSArrays (local rows, global columns),
+    one per row block, and the blocks' first rows; the triplet arrays are
+    sorted in place."""
+    nnz = rows.size
+    f = np.zeros(parts, np.int32)
+    t = np.zeros(parts, np.int32)
+    rs = np.zeros(nor + parts, np.int32)
+    ci = np.zeros(max(nnz, 1), np.int32)
+    d = np.zeros(max(nnz, 1), np.float64)
+    lib().orc_triplet_to_multi_crs(nnz, nor, parts, _nz(rows, np.int32), _nz(cols, np.int32), _nz(vals), f, t, rs,
+                                   ci, d)
+    out, base, k0 = [], 0, 0
+    for p in range(parts):
+        r = rs[base:base + t[p] + 1].copy()
+        n = int(r[-1])
+        out.append(CRSArrays(t[p], noc, r, ci[k0:k0 + n].copy(), d[k0:k0 + n].copy()))
+        base += t[p] + 1
+        k0 += n
+    return out, f
+
+
+def fill_poisson_rows(m, n, first_row, last_row):
+    """Rows [first_row, last_row) of the m x n Poisson matrix (local row
+    starts, global columns): CRSArrays."""
+    rows = last_row - first_row
+    rs = np.zeros(rows + 1, np.int32)
+    ci = np.zeros(max(5 * rows, 1), np.int32)
+    d = np.zeros(max(5 * rows, 1), np.float64)
+    lib().orc_fill_poisson_rows(m, n, first_row, last_row, rs, ci, d)
+    k = int(rs[-1])
+    return CRSArrays(rows, m * n, rs, ci[:k], d[:k])
+
+
+def power_rows(blocks, x, it):
+    """MPI_driver_poisson.cpp's row-sharded power method over the blocks (a
+    list of CRSArrays in rank order, as triplet_to_multi_crs returns them):
+    the normalised full iterate after `it` iterations."""
+    nor = sum(b.nor for b in blocks)
+    rs = np.concatenate([b.row_start for b in blocks]).astype(np.int32)
+    ci = np.concatenate([b.col_ind for b in blocks] + [np.zeros(1, np.int32)]).astype(np.int32)
+    d = np.concatenate([b.data for b in blocks] + [np.zeros(1)])
+    x = np.array(x, dtype=np.float64, copy=True)
+    lib().orc_power_rows(nor, len(blocks), rs, ci, d, x, int(it))
+    return x
 
 
 def crs_mv(A, x):

@@ -70,6 +70,8 @@ def lib():
         L.ref_hilbert.restype = C.c_int
         L.ref_hilbert.argtypes = [C.c_int, C.c_int, C.c_int]
         L.ref_set_threads.argtypes = [C.c_int]
+        L.ref_multi_crs.argtypes = [C.c_int, C.c_int, C.c_int, I32P, I32P, F64P, I32P, I32P, I32P, I32P, F64P]
+        L.ref_fill_poisson_rows.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, I32P, I32P, F64P]
         L.ref_max_threads.restype = C.c_int
         L.ref_srand.argtypes = [C.c_uint]
         _lib = L
@@ -239,3 +241,30 @@ def calc_stats(nor, noc, rows, cols, vals):
             d["balanced"] = 0 if "unbalanced" in line else 1
     d["size"], d["nnz"] = int(d["size"]), int(d["nnz"])
     return d
+
+
+def multi_crs(nor, rows, cols, vals, parts):
+    """The reference's TripletToMultipleCRS on copies of the triplet arrays:
+    (first_rows, thread_rows, concatenated row starts, columns, values)."""
+    L = lib()
+    r = np.ascontiguousarray(rows, np.int32).copy()
+    c = np.ascontiguousarray(cols, np.int32).copy()
+    v = np.ascontiguousarray(vals, np.float64).copy()
+    f = np.zeros(parts, np.int32)
+    t = np.zeros(parts, np.int32)
+    rs = np.zeros(nor + parts, np.int32)
+    ci = np.zeros(max(r.size, 1), np.int32)
+    d = np.zeros(max(r.size, 1), np.float64)
+    L.ref_multi_crs(nor, r.size, parts, r, c, v, f, t, rs, ci, d)
+    return f, t, rs, ci[:r.size], d[:r.size]
+
+
+def fill_poisson_rows(m, n, first_row, last_row):
+    """The reference's fillPoisson over rows [first_row, last_row)."""
+    L = lib()
+    rows = last_row - first_row
+    rs = np.zeros(rows + 1, np.int32)
+    ci = np.zeros(max(5 * rows, 1), np.int32)
+    d = np.zeros(max(5 * rows, 1), np.float64)
+    L.ref_fill_poisson_rows(m, n, first_row, last_row, rs, ci, d)
+    return rs, ci[:rs[-1]], d[:rs[-1]]

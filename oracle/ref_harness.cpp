@@ -180,6 +180,33 @@ int ref_hilbert(int size, int row, int col) {
     return r;
 }
 
+// ---- Util/TripletToCRS.hpp:309-385 (TripletToMultipleCRS): the blocks'
+// arrays concatenated as orc_triplet_to_multi_crs writes them; the triplet
+// arrays are sorted in place as the reference sorts them ----
+void ref_multi_crs(int nor, int nnz, int parts, int* r, int* c, double* v, int* first_rows, int* thread_rows,
+                   int* rs_all, int* ci_all, double* d_all) {
+    std::vector<int*> rs(parts), ci(parts);
+    std::vector<double*> d(parts);
+    pwm::TripletToMultipleCRS<double, int>(r, c, v, rs.data(), ci.data(), d.data(), parts, thread_rows, first_rows,
+                                           nnz, nor);
+    int base = 0, k0 = 0;
+    for (int p = 0; p < parts; ++p) {
+        const int n = rs[p][thread_rows[p]];
+        std::copy(rs[p], rs[p] + thread_rows[p] + 1, rs_all + base);
+        std::copy(ci[p], ci[p] + n, ci_all + k0);
+        std::copy(d[p], d[p] + n, d_all + k0);
+        base += thread_rows[p] + 1;
+        k0 += n;
+        delete[] rs[p];
+        delete[] ci[p];
+        delete[] d[p];
+    }
+}
+// ---- Util/Poisson.hpp:33-83 with first_row / last_row ----
+void ref_fill_poisson_rows(int m, int n, int first_row, int last_row, int* rs, int* ci, double* d) {
+    pwm::fillPoisson<double, int>(d, rs, ci, m, n, first_row, last_row);
+}
+
 void ref_set_threads(int t) { omp_set_num_threads(t); }
 int ref_max_threads() { return omp_get_max_threads(); }
 void ref_srand(unsigned s) { srand(s); }

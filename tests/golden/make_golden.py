@@ -17,6 +17,8 @@ Writes
                            merge-path coordinates, CSB and CO-H arrays, mv and
                            power results.  These let the GPU-box tests pin the
                            oracle without the reference tree.
+  ref_multi_crs.npz     -- the reference's TripletToMultipleCRS blocks and its
+                           row-range fillPoisson (--multi: only these).
 """
 import json
 import os
@@ -166,11 +168,41 @@ def make_stats():
     print("stats cases:", len(res))
 
 
+def make_multi(ref_dir):
+    """ref_multi_crs.npz: the reference's TripletToMultipleCRS
+    (Util/TripletToCRS.hpp:309-385) on three triplets for 1, 2, 3 and 5 row
+    blocks, and its fillPoisson over row ranges (Util/Poisson.hpp:33-83)."""
+    from oracle import pyref as R
+    assert R.available(), "oracle/_ref could not be built"
+    out = {}
+    sets = [("poisson40x24",) + R.Triplet().poisson(40, 24).get()]
+    for fn, hd, sym in [("gre_1107.mtx", True, False), ("G38.mtx", False, True)]:
+        sets.append((fn.split(".")[0],) + R.Triplet().load_mm(os.path.join(ref_dir, "Test_input", fn), hd, sym).get())
+    for name, nor, noc, r, c, v in sets:
+        out["trip_%s_rows" % name], out["trip_%s_cols" % name], out["trip_%s_vals" % name] = r, c, v
+        out["trip_%s_dims" % name] = np.array([nor, noc], np.int32)
+        for parts in (1, 2, 3, 5):
+            f, t, rs, ci, d = R.multi_crs(nor, r, c, v, parts)
+            pre = "multi%d_%s_" % (parts, name)
+            out[pre + "first"], out[pre + "rows"], out[pre + "row_start"] = f, t, rs
+            out[pre + "col_ind"], out[pre + "data"] = ci, d
+    # (last_row = 0 means "every row" to the reference, so an empty range is not asked for)
+    for (m, n, a, b) in [(7, 5, 0, 35), (7, 5, 3, 20), (10, 10, 50, 100), (33, 17, 100, 101), (33, 17, 560, 561)]:
+        rs, ci, d = R.fill_poisson_rows(m, n, a, b)
+        pre = "poisson_rows_%d_%d_%d_%d_" % (m, n, a, b)
+        out[pre + "row_start"], out[pre + "col_ind"], out[pre + "data"] = rs, ci, d
+    np.savez_compressed(os.path.join(HERE, "ref_multi_crs.npz"), **out)
+    print("ref_multi_crs keys:", len(out))
+
+
 if __name__ == "__main__":
     if "--stats" in sys.argv:
         make_stats()
+    elif "--multi" in sys.argv:
+        make_multi(os.environ["PWM_REFERENCE_DIR"] if len(sys.argv) < 3 else sys.argv[-1])
     else:
         if len(sys.argv) < 2 and not os.environ.get("PWM_REFERENCE_DIR"):
             sys.exit("usage: make_golden.py REFERENCE_TREE (or set PWM_REFERENCE_DIR)")
         main(sys.argv[1] if len(sys.argv) > 1 else os.environ["PWM_REFERENCE_DIR"])
         make_stats()
+        make_multi(sys.argv[1] if len(sys.argv) > 1 else os.environ["PWM_REFERENCE_DIR"])

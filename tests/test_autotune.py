@@ -105,7 +105,8 @@ def test_auto_times_then_reuses_class(pwm, poisson):
     assert t["format"] in ("merge", "csb", "coh")
     assert t["merge_ms"] > 0 and all(v > 0 for v in t["coh_ms"]) and all(v > 0 for v in t["csb_ms"])
     best = min([t["merge_ms"]] + t["coh_ms"] + t["csb_ms"])
-    chosen = {"merge": t["merge_ms"], "coh": min(t["coh_ms"]), "csb": t["csb_ms"][t["csb_variant"]]}[t["format"]]
+    chosen = {"merge": t["merge_ms"], "coh": t["coh_ms"][t["csb_variant"]],
+              "csb": t["csb_ms"][t["csb_variant"]]}[t["format"]]
     assert chosen == best
     assert pwm.tuner_size() == 1
     _check_mv(M, poisson, 3)
@@ -125,7 +126,7 @@ def test_auto_times_then_reuses_class(pwm, poisson):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fmt,variant,pps", [("csb", 0, 0), ("csb", 3, 0), ("coh", 0, 0), ("coh", 0, 8),
+@pytest.mark.parametrize("fmt,variant,pps", [("csb", 0, 0), ("csb", 3, 0), ("coh", 0, 0), ("coh", 2, 8),
                                              ("merge", 0, 0)])
 def test_auto_recorded_choice_runs_that_format(pwm, poisson, fmt, variant, pps):
     """A recorded class choice (as a tuning carried from another process)
@@ -142,7 +143,7 @@ def test_auto_recorded_choice_runs_that_format(pwm, poisson, fmt, variant, pps):
     M = pwm.AutoCuda(1)
     M.generatePoissonMatrix(GRID, GRID, 1)
     t = M.tuning()
-    assert t["cache_hit"] and (t["format"], t["csb_variant"]) == (fmt, variant if fmt == "csb" else 0)
+    assert t["cache_hit"] and (t["format"], t["csb_variant"]) == (fmt, variant if fmt != "merge" else 0)
     assert t["coh_partitions"] == ((pps or 24) * sm.value if fmt == "coh" else 0)
     _check_mv(M, poisson, 6)
     x0 = np.random.default_rng(7).random(poisson.noc)

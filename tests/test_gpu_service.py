@@ -199,3 +199,46 @@ def test_service_triplet_source_equals_csr(svc_mod):
     bad = svc.submit_triplets(4, np.array([0, 1, 9]), np.array([0, 1, 2]), np.ones(3), max_it=10)
     svc.run_until_idle()
     assert svc.result(bad).state == S.FAILED
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_service_batch_classes_confirmed_by_oracle(svc_mod, precision):
+    """A seeded sub-batch shaped like the benchmark's 256-matrix batch and
+    serving stream (Poisson grids; random matrices with Poisson(8) rows and
+    uniform columns; lognormal-row matrices with a band), solved together to
+    1e-10 or 2,000 steps: every returned eigenpair is checked by the FP64
+    oracle's Rayleigh quotient -- lambda within 1e-10 relative, the oracle's
+    residual within 2 tol for converged solves and equal to the reported one
+    within 1e-12 absolute for the capped ones."""
+    t, S = svc_mod
+    prec = t.PREC_F64 if precision == "f64" else t.PREC_MIXED
+    specs = [("poisson", dict(m=37, n=41)), ("poisson", dict(m=64, n=64)),
+             ("random", dict(n=3000, seed=1001, length_dist=1, mean_len=8.0, sigma=0.0, max_len=64,
+                             band_permille=0, band_half=0)),
+             ("random", dict(n=40000, seed=1002, length_dist=1, mean_len=8.0, sigma=0.0, max_len=64,
+                             band_permille=0, band_half=0)),
+             ("random", dict(n=20000, seed=5001, length_dist=0, mean_len=16.0, sigma=1.2, max_len=20000,
+                             band_permille=300, band_half=4096))]
+    svc = S.Service(round_iterations=8)
+    ids = []
+    for kind, kw in specs:
+        if kind == "poisson":
+            ids.append(svc.submit_poisson(kw["m"], kw["n"], max_it=2000, tol=1e-10, precision=prec, x0_seed=11,
+                                          keep_vector=True))
+        else:
+            ids.append(svc.submit_random(max_it=2000, tol=1e-10, precision=prec, x0_seed=11, keep_vector=True, **kw))
+    svc.run_until_idle()
+    for (kind, kw), rid in zip(specs, ids):
+        r, u = svc.result(rid, want_vector=True)
+        assert r.state == S.DONE
+        A = O.fill_poisson(kw["m"], kw["n"]) if kind == "poisson" else O.random_crs(
+            kw["n"], kw["seed"], kw["length_dist"], kw["mean_len"], kw["sigma"], kw["max_len"], kw["band_permille"],
+            kw["band_half"])
+        lam_o, res_o = O.rayleigh(A, u)
+        assert abs(r.lambda_ - lam_o) <= 1e-10 * abs(lam_o), (kind, kw)
+        if r.converged:
+            assert res_o <= 2e-10, (kind, kw, res_o)
+        else:
+            assert r.iterations >= 2000 and abs(r.residual - res_o) <= 1e-12, (kind, kw, r.residual, res_o)
+    assert svc.result(ids[2]).converged and svc.result(ids[4]).converged  # the random classes converge
+    svc.close()

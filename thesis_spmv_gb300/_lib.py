@@ -83,6 +83,12 @@ SIGNATURES = {
     "pwmgpu_power": (C.c_int, [vp, vp, vp, i32]),
     "pwmgpu_power_device": (C.c_int, [vp, vp, vp, i32]),
     "pwmgpu_set_power_mode": (C.c_int, [vp, C.c_int]),
+    "pwmgpu_test_grid_wait": (C.c_int, [vp, i64, i32]),
+    "pwmgpu_row_blocks": (C.c_int, [i32, i32, vp, vp]),
+    "pwmgpu_generate_poisson_rows": (C.c_int, [vp, i32, i32, i32, i32]),
+    "pwmgpu_load_triplets_rows": (C.c_int, [vp, i32, i32, i32, vp, vp, vp, i32, i32]),
+    "pwmgpu_rows_step_device": (C.c_int, [vp, vp, vp, vp]),
+    "pwmgpu_rows_normalize_device": (C.c_int, [vp, vp, vp]),
     "pwmgpu_set_low_format": (C.c_int, [vp, C.c_int]),
     "pwmgpu_solve": (C.c_int, [vp, vp, i32, C.c_double, C.c_int, C.POINTER(SolveInfo)]),
     "pwmgpu_merge_partition": (C.c_int, [vp, i32, vp]),

@@ -8,28 +8,25 @@
 // 16-bit column jumps that overflow by +beta at a row change, 16-bit row
 // jumps; between blocks BICRS (:404-445): int16 column jumps that overflow by
 // +hb at a block-row change, int16 block-row jumps.  Built on the host here,
-// bit for bit the reference's arrays.  The device copy of the column jumps
-// and values starts every block on a multiple of 8 elements (zeros between
-// blocks, never read as elements) so a lane loads its 8 elements with wide
-// loads; the block table holds the padded offsets.
+// bit for bit the reference's arrays (pwmgpu_get_coh returns them).
 //
-// The GPU kernel (k_coh_spmv) gives each partition to one warp (a partition
-// owns its rows, as a thread does in BlockCOH::mv :479-510).  The warp walks
-// the partition's blocks in Hilbert order (block positions decoded once at
-// build time) and each block's elements in chunks of 32 x 8: lane l takes 8
-// consecutive elements and decodes them with a warp prefix sum of the column
-// jumps (running position S: column = S mod beta, row changes = S / beta;
-// rows from a warp prefix sum of the row jumps, staged in shared memory).  A
-// lane accumulates its runs of equal rows with one FMA per nonzero; a run
-// that crosses lanes is summed by the lane where it starts (lane order) and
-// one crossing the chunk end is carried.  A partition adds into its own rows
-// of y (zeroed first; the read-modify-writes stay in L2).  The walk is
-// latency-bound, so residency is what counts: 8 CTAs of 4 warps per SM
-// (64 registers); an earlier shared-memory y window of 2048 rows per warp
-// capped residency at 3 CTAs per SM and was 1.66x slower on the 4096^2
-// stencil.  Rows are written by one lane at a time and blocks in order: no
-// atomics, a fixed summation order (per row, Hilbert block order, as in the
-// reference).
+// The device executes the same blocks as tiles of the tile kernel
+// (k_csb_spmv, csb.cu): rows are cut into windows of S rows (S <= 1024, a
+// y window in shared memory per CTA), each CO-H block into the tiles its
+// elements form in a window and an S-column x window; a window's tiles are
+// taken partition by partition in the partition's Hilbert block order, a
+// block's tiles by column window.  A tile of at least kTileDenseUnit
+// elements stages its x window in shared memory with a TMA bulk copy and is
+// read row-major (one FMA per element inside a lane's rows); the window's
+// sparse tiles -- the blocks of a random matrix hold a handful of elements --
+// are merged into one row-major unit that gathers x through L1 / L2.  The
+// first GPU kernel walked a partition's blocks with one warp, decoding the
+// jumps with warp prefix sums and adding into y in global memory: a chain of
+// dependent loads per 256-element chunk that was latency-bound at 0.66 ms on
+// the 4096^2 Poisson matrix (2021 GB/s of CRS bytes) and 5.7 ms on the
+// 4.19M-row irregular matrix (156 GB/s).  Per row, the tile kernel adds the
+// merged sparse unit first, then the dense tiles in the window's order; the
+// per-row error bound holds for any order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,6 +34,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -45,11 +43,6 @@
 namespace pwmgpu {
 
 namespace {
-
-constexpr int kCohK = 8;           // elements per lane per chunk (one 16-byte load of jumps)
-static_assert(kCohK == 8, "a lane loads its column jumps as one uint4");
-constexpr int kCohWarps = 4;       // warps per CTA
-constexpr int kCohOcc = 8;         // resident CTAs per SM (64 registers): 32 warps
 
 // BlockCOH.hpp:79-114 rowColToHilbert: index of cell (row, col) on the
 // Hilbert curve over a size x size grid.
@@ -68,194 +61,6 @@ int hilbert_index(int size, int row, int col) {
         }
     }
     return index;
-}
-
-__global__ void __launch_bounds__(32 * kCohWarps, kCohOcc) k_coh_spmv(const int4* __restrict__ parts, int nparts,
-                                                             const int4* __restrict__ blocks,
-                                                             const uint16_t* __restrict__ row_jump,
-                                                             const uint16_t* __restrict__ col_jump,
-                                                             const double* __restrict__ data,
-                                                             const double* __restrict__ x, double* __restrict__ y,
-                                                             const double* nsq_in) {
-    constexpr int K = kCohK;
-    constexpr int CH = 32 * K;
-    __shared__ int rbuf_s[kCohWarps][CH + 1];
-    __shared__ int frow_s[kCohWarps][32];
-    __shared__ int crow_s[kCohWarps][32];
-    __shared__ double hval_s[kCohWarps][32];
-    __shared__ double cval_s[kCohWarps][32];
-    __shared__ int multi_s[kCohWarps][32];
-    __shared__ int carry_row_s[kCohWarps];
-    __shared__ double carry_s[kCohWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int* rbuf = rbuf_s[w];
-    int* frow = frow_s[w];
-    int* crow = crow_s[w];
-    double* hval = hval_s[w];
-    double* cval = cval_s[w];
-    int* multi = multi_s[w];
-    const int e = nsq_in ? pow2_rescale_exponent(*nsq_in, 256) : 0;
-    if (lane == 0) carry_row_s[w] = -1;
-    __syncwarp();
-    for (int p = blockIdx.x * kCohWarps + w; p < nparts; p += gridDim.x * kCohWarps) {
-        // parts[2p] = {first row, rows, block bits, first block}, parts[2p+1].x = blocks
-        const int4 pa = __ldg(parts + 2 * p);
-        const int nb = __ldg(&parts[2 * p + 1].x);
-        const int trs = pa.x, nrows = pa.y, bits = pa.z, b0 = pa.w;
-        const int beta = 1 << bits;
-        double* yp = y + trs;  // the partition's rows (no other warp writes them)
-        for (int r = lane; r < nrows; r += 32) yp[r] = 0.0;
-        __syncwarp();
-        for (int b = b0; b < b0 + nb; ++b) {
-            // blocks[2b] = {block row, block col, first element, first row jump}, blocks[2b+1].x = nnz
-            const int4 ba = __ldg(blocks + 2 * b);
-            const int n = __ldg(&blocks[2 * b + 1].x);
-            double* yb = yp + (long long)ba.x * beta;
-            const double* xb = x + (long long)ba.y * beta;
-            const long long eb = ba.z;
-            const uint16_t* rj = row_jump + ba.w;
-            int s_base = 0;          // position of the previous chunk's last element
-            int ch_base = 0;         // its row-change count
-            int r_base = __ldg(rj);  // its row (block-local)
-            int carry_row = -1;      // run open across the chunk boundary
-            double carry = 0.0;
-            for (int cs = 0; cs < n; cs += CH) {
-                // ---- positions: warp prefix sum of the column jumps
-                const int i0 = cs + lane * K;
-                int pos[K];
-                double dv[K];
-                int tot = 0;
-                // the block starts on a multiple of 8 elements in the device
-                // copy, padded past its end: one 16-byte load of jumps, four
-                // of values
-                uint4 cj = make_uint4(0u, 0u, 0u, 0u);
-                double2 dd[K / 2];
-#pragma unroll
-                for (int t = 0; t < K / 2; ++t) dd[t] = make_double2(0.0, 0.0);
-                if (i0 < n) {
-                    cj = __ldg(reinterpret_cast<const uint4*>(col_jump + eb + i0));
-#pragma unroll
-                    for (int t = 0; t < K / 2; ++t) dd[t] = __ldg(reinterpret_cast<const double2*>(data + eb + i0) + t);
-                }
-                const uint32_t cw[4] = {cj.x, cj.y, cj.z, cj.w};
-#pragma unroll
-                for (int t = 0; t < K; ++t) {
-                    const bool v = i0 + t < n;
-                    const int jump = (int)((t & 1) ? (cw[t >> 1] >> 16) : (cw[t >> 1] & 0xFFFFu));
-                    tot += v ? jump : 0;
-                    dv[t] = v ? ((t & 1) ? dd[t >> 1].y : dd[t >> 1].x) : 0.0;
-                    pos[t] = tot;
-                }
-                int incl = tot;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int u = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += u;
-                }
-                const int excl = s_base + incl - tot;
-                const int s_last = s_base + __shfl_sync(0xffffffffu, incl, 31);
-                // ---- rows reached in this chunk: R[ch_base + j] = rbuf[j]
-                const int ch_last = s_last >> bits;
-                const int nchg = ch_last - ch_base;
-                int run = r_base;
-                for (int c0 = 0; c0 < nchg; c0 += 32) {
-                    const int c = c0 + lane;
-                    int v = c < nchg ? (int)__ldg(rj + ch_base + 1 + c) : 0;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int u = __shfl_up_sync(0xffffffffu, v, o);
-                        if (lane >= o) v += u;
-                    }
-                    if (c < nchg) rbuf[c + 1] = run + v;
-                    run += __shfl_sync(0xffffffffu, v, 31);
-                }
-                if (lane == 0) rbuf[0] = r_base;
-                __syncwarp();
-                // ---- the lane's runs: middle runs are complete and written here
-                const bool has = i0 < n;
-                int first = INT_MAX, cur = INT_MAX;
-                double acc = 0.0, head = 0.0;
-                bool is_multi = false;
-#pragma unroll
-                for (int t = 0; t < K; ++t) {
-                    if (i0 + t < n) {
-                        const int S = excl + pos[t];
-                        const int row = rbuf[(S >> bits) - ch_base];
-                        const double xv = __ldg(xb + (S & (beta - 1)));
-                        if (t == 0) {
-                            first = cur = row;
-                        } else if (row != cur) {
-                            if (!is_multi) {
-                                head = acc;
-                                is_multi = true;
-                            } else {
-                                yb[cur] = yb[cur] + (e != 0 ? scale_pow2(acc, e) : acc);
-                            }
-                            acc = 0.0;
-                            cur = row;
-                        }
-                        acc = fma(dv[t], xv, acc);
-                    }
-                }
-                if (!is_multi) head = acc;
-                // the run carried from the previous chunk continues in lane 0, or is complete
-                if (lane == 0 && carry_row >= 0) {
-                    if (has && first == carry_row) {
-                        head += carry;
-                        if (!is_multi) acc += carry;
-                    } else {
-                        yb[carry_row] = yb[carry_row] + (e != 0 ? scale_pow2(carry, e) : carry);
-                    }
-                }
-                frow[lane] = has ? first : INT_MAX;
-                crow[lane] = has ? cur : INT_MAX;
-                hval[lane] = head;
-                cval[lane] = acc;
-                multi[lane] = is_multi ? 1 : 0;
-                __syncwarp();
-                if (has) {
-                    const bool cont_in = lane > 0 && frow[lane] == crow[lane - 1];
-                    // a first run that is not also the last run, starting here: complete
-                    if (is_multi && !cont_in) yb[first] = yb[first] + (e != 0 ? scale_pow2(head, e) : head);
-                    // the last run starts here (or the lane is one run not continuing): lead its chain
-                    if (is_multi || !cont_in) {
-                        double sum = acc;
-                        int u = lane + 1;
-                        bool ended = false;
-                        while (u < 32 && frow[u] == cur) {
-                            if (multi[u]) {
-                                sum += hval[u];
-                                ended = true;
-                                break;
-                            }
-                            sum += cval[u];
-                            ++u;
-                        }
-                        if (!ended && u == 32) {  // runs into the next chunk
-                            carry_row_s[w] = cur;
-                            carry_s[w] = sum;
-                        } else {
-                            yb[cur] = yb[cur] + (e != 0 ? scale_pow2(sum, e) : sum);
-                        }
-                    }
-                }
-                __syncwarp();
-                // the carry for the next chunk: set by the chain that reached lane 31
-                // (or -1); the block's last chunk flushes it below
-                carry_row = carry_row_s[w];
-                carry = carry_s[w];
-                s_base = s_last;
-                ch_base = ch_last;
-                r_base = rbuf[nchg];
-                __syncwarp();
-                if (lane == 0) carry_row_s[w] = -1;
-                __syncwarp();
-            }
-            if (lane == 0 && carry_row >= 0) yb[carry_row] = yb[carry_row] + (e != 0 ? scale_pow2(carry, e) : carry);
-            __syncwarp();
-        }
-        __syncwarp();
-    }
 }
 
 }  // namespace
@@ -423,16 +228,90 @@ int coh_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
     return T;
 }
 
-cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, const uint16_t* row_jump,
-                            const uint16_t* col_jump, const double* data, const double* x, double* y,
-                            const double* nsq_in, int sm_count, cudaStream_t st) {
-    if (nparts <= 0) return cudaSuccess;
-    long long grid = (nparts + kCohWarps - 1) / kCohWarps;
-    if (grid > (long long)sm_count * kCohOcc) grid = (long long)sm_count * kCohOcc;
-    k_coh_spmv<<<(int)grid, 32 * kCohWarps, 0, st>>>(reinterpret_cast<const int4*>(parts), nparts,
-                                                    reinterpret_cast<const int4*>(blocks), row_jump, col_jump, data,
-                                                    x, y, nsq_in);
-    return cudaGetLastError();
+// The CO-H matrix as tile-kernel units (see the header comment).
+void coh_tile_units(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,
+                    const std::vector<int>& parts, int S, std::vector<uint32_t>& ind, std::vector<double>& data,
+                    std::vector<int>& win_ptr, std::vector<int>& unit_data) {
+    struct Tile {
+        int lo, hi, c0;
+    };
+    const int T = (int)(parts.size() / 8);
+    const int nwin = (nor + S - 1) / S;
+    ind.resize((size_t)nnz);
+    data.resize((size_t)nnz);
+    std::vector<std::vector<Tile>> tiles((size_t)nwin);
+    std::vector<int> first((size_t)T), bits((size_t)T), hgrid((size_t)T);
+    for (int p = 0; p < T; ++p) {
+        first[(size_t)p] = parts[(size_t)8 * p];
+        bits[(size_t)p] = parts[(size_t)8 * p + 2];
+        const int rows_p = parts[(size_t)8 * p + 1];
+        const int mx = std::max(std::max(rows_p, noc), 1);
+        const int hsize = (int)std::pow(2.0, std::ceil(std::log2((double)mx)));  // as coh_build_host
+        hgrid[(size_t)p] = std::max(hsize >> bits[(size_t)p], 1);
+    }
+    auto work = [&](int w0, int w1) {
+        // (partition << 40 | Hilbert index of the block, column window,
+        //  local row << 32 | column, CRS position)
+        std::vector<std::tuple<uint64_t, uint32_t, uint64_t, int64_t>> key;
+        for (int w = w0; w < w1; ++w) {
+            const int r0 = w * S, r1 = std::min(nor, r0 + S);
+            const int64_t e0 = row_start[r0];
+            key.clear();
+            int p = (int)(std::upper_bound(first.begin(), first.end(), r0) - first.begin()) - 1;
+            for (int r = r0; r < r1; ++r) {
+                while (p + 1 < T && first[(size_t)p + 1] <= r) ++p;
+                const int b = bits[(size_t)p];
+                const uint32_t br = (uint32_t)(r - first[(size_t)p]) >> b;
+                for (int64_t k = row_start[r]; k < row_start[r + 1]; ++k) {
+                    const uint32_t bc = (uint32_t)col[k] >> b;
+                    const uint64_t h = (uint64_t)(uint32_t)hilbert_index(hgrid[(size_t)p], (int)br, (int)bc);
+                    key.emplace_back(((uint64_t)p << 40) | h, (uint32_t)col[k] / (uint32_t)S,
+                                     ((uint64_t)(r - r0) << 32) | (uint64_t)(uint32_t)col[k], k);
+                }
+            }
+            std::sort(key.begin(), key.end());
+            std::vector<Tile>& tl = tiles[(size_t)w];
+            uint64_t cur_blk = ~0ull;
+            uint32_t cur_c = ~0u;
+            for (size_t q = 0; q < key.size(); ++q) {
+                const int64_t k = std::get<3>(key[q]);
+                const uint32_t cwin = std::get<1>(key[q]);
+                const uint32_t lr = (uint32_t)(std::get<2>(key[q]) >> 32);
+                const int dst = (int)(e0 + (int64_t)q);
+                const int c0 = (int)cwin * S;
+                ind[(size_t)dst] = (lr << 16) | (uint32_t)(col[k] - c0);
+                data[(size_t)dst] = val[k];
+                if (std::get<0>(key[q]) != cur_blk || cwin != cur_c) {
+                    tl.push_back(Tile{dst, dst + 1, c0});
+                    cur_blk = std::get<0>(key[q]);
+                    cur_c = cwin;
+                } else {
+                    tl.back().hi = dst + 1;
+                }
+            }
+        }
+    };
+    const int nt = std::max(1, std::min<int>(nwin, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back(work, (int)((long long)nwin * t / nt), (int)((long long)nwin * (t + 1) / nt));
+    for (auto& t : th) t.join();
+    // per window: sparse tiles first, then dense ones (win_ptr holds both starts)
+    win_ptr.assign(2 * (size_t)nwin + 1, 0);
+    unit_data.clear();
+    int o = 0;
+    for (int w = 0; w < nwin; ++w) {
+        win_ptr[2 * (size_t)w] = o;
+        for (int dense = 0; dense < 2; ++dense) {
+            if (dense) win_ptr[2 * (size_t)w + 1] = o;
+            for (const Tile& u : tiles[(size_t)w]) {
+                if ((u.hi - u.lo >= kTileDenseUnit) != (dense == 1)) continue;
+                unit_data.insert(unit_data.end(), {u.lo, u.hi, u.c0, 0});
+                ++o;
+            }
+        }
+    }
+    win_ptr[2 * (size_t)nwin] = o;
 }
 
 }  // namespace pwmgpu

@@ -13,13 +13,10 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include "internal.h"
 #include "pwmgpu.h"
 
 namespace pwmgpu {
-
-// Largest clock64 interval any spin-wait may take before it reports
-// PWMGPU_ERR_TIMEOUT (about 2 s at the 2.07 GHz maximum SM clock).
-constexpr long long kWaitCycles = 4000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -172,6 +169,35 @@ __host__ __device__ __forceinline__ int pow2_rescale_exponent(double nsq, int wi
 template <typename XT>
 __host__ __device__ __forceinline__ int rescale_window() {
     return sizeof(XT) == 4 ? 32 : 256;
+}
+
+// Magnitude key of a vector element: the sign-cleared top 32 bits of its
+// IEEE-754 pattern (FP64: sign, exponent and 20 mantissa bits; FP32: the whole
+// word).  For finite values the key orders like |v|, so the largest key of a
+// vector (an integer max: no FP64 pipe) gives the exponent of its largest
+// element.
+__device__ __forceinline__ unsigned mag_key(double v) {
+    return (unsigned)((unsigned long long)__double_as_longlong(v) >> 32) & 0x7FFFFFFFu;
+}
+__device__ __forceinline__ unsigned mag_key(float v) { return __float_as_uint(v) & 0x7FFFFFFFu; }
+
+// Exponent e of the exact 2^e rescale from the largest magnitude key of a
+// vector (instead of its squared norm): no rescale while the largest element
+// 2^E satisfies 2E in [-window, window) -- then ||v||^2 lies within
+// 2^[-window, window + 2 + log2 n), far from the range ends -- else e = -E,
+// which brings the largest element into [1, 2).  A zero vector or a
+// non-finite key gives 0; a subnormal largest element is scaled by 2^900.
+template <typename XT>
+__host__ __device__ __forceinline__ int pow2_rescale_exponent_key(unsigned key) {
+    constexpr int kShift = sizeof(XT) == 4 ? 23 : 20;
+    constexpr int kBias = sizeof(XT) == 4 ? 127 : 1023;
+    constexpr unsigned kInf = sizeof(XT) == 4 ? 0x7F800000u : 0x7FF00000u;
+    if (key == 0u || key >= kInf) return 0;
+    const int field = (int)(key >> kShift);
+    if (field == 0) return sizeof(XT) == 4 ? 100 : 900;
+    const int ex = field - kBias;
+    if (2 * ex >= -rescale_window<XT>() && 2 * ex < rescale_window<XT>()) return 0;
+    return -ex;
 }
 
 // ---- value conversions ---------------------------------------------------

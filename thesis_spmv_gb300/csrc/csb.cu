@@ -65,7 +65,7 @@ namespace {
 // the format autotuner times all four.
 constexpr int kCsbThreadsPerSM = 1024;
 constexpr int kCsbMaxS = 1024;
-constexpr int kDenseUnit = 256;  // elements from which a unit's x window is staged
+constexpr int kDenseUnit = kTileDenseUnit;  // elements from which a unit's x window is staged
 
 // Spread the low 16 bits of v to the even bit positions.
 inline uint64_t spread16(uint64_t v) {

@@ -20,7 +20,13 @@ struct DevMatrix {
     double* val = nullptr;
 };
 
-enum { kModeSpmv = 0, kModePower = 1 };
+// Merge kernel modes (merge.cuh MergeMode): plain SpMV; a power step with its
+// squared norm; a power step tracking only the largest magnitude key.
+enum { kModeSpmv = 0, kModePower = 1, kModeScale = 2 };
+
+// Largest clock64 interval any spin-wait may take before it reports
+// PWMGPU_ERR_TIMEOUT (about 2 s at the 2.07 GHz maximum SM clock).
+constexpr long long kWaitCycles = 4000000000LL;
 
 // merge.cu
 // Items per lane of a merge-path sub-tile (a sub-tile is 32 * kMliIpt merge
@@ -98,10 +104,20 @@ int power_persistent_grid(int cfg, int nsub, int sm_count, int l1 = 0);
 // = ||v_k||^2 (nsq[k0] read when k0 > 0), result (5 doubles, or null):
 // {lambda, residual^2, ||v_k||^2, v_k.v_{k+1}, e_k} of the last iteration.
 // partials: 2 doubles per CTA; barrier: 2 words (zeroed here).
+// wait: the grid barrier's budget (clock64 cycles) before it records
+// PWMGPU_ERR_TIMEOUT, and extra arrivals it waits for beyond the grid (0;
+// pwmgpu_test_grid_wait sets 1 to make every barrier run out of budget).
+struct GridWait {
+    long long cycles;
+    unsigned int extra;
+};
+// mxk: k0 + nk + 1 zeroed words (or null): iterations before the last two
+// of the launch track only the iterate's largest magnitude key (mxk[k+1]) for
+// the rescale instead of summing ||v||^2 (nsq[k+1] is then not written).
 cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                                     void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
                                     double* partials, unsigned int* barrier, int* status, cudaStream_t st,
-                                    int l1 = 0);
+                                    int l1, GridWait wait, unsigned int* mxk = nullptr);
 cudaError_t launch_merge_partition(const int32_t* row_start, int nor, long long nnz, long long ipt, int parts,
                                    int2* out, cudaStream_t st);
 cudaError_t launch_mli_plan(const int32_t* row_start, const int32_t* col, const double* val, const MliPlan& P,
@@ -126,15 +142,26 @@ cudaError_t launch_fix_runs_f32(int mode, const MliPlan& P, int k0, int k1, floa
 // total to *nsq_out.  npart holds power_norm_parts(P, spmv_grid) doubles;
 // counter is zero between launches.
 int power_norm_parts(const MliPlan& P, int spmv_grid);
+// mx_in (optional): the step's rescale from its input's largest magnitude key
+// instead of nsq_in.
 cudaError_t launch_fix_runs_norm(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
                                  double* npart, int spmv_grid, unsigned int* counter, double* nsq_out,
-                                 cudaStream_t st);
+                                 cudaStream_t st, const unsigned int* mx_in = nullptr);
+// The fix-up of a MODE_SCALE step: carries times 2^e (e from *mx_in, else
+// from *nsq_in, else 0 -- the same source as the step's SpMV), and atomicMax
+// of the fixed rows' magnitude keys into *mx_out.
+cudaError_t launch_fix_runs_scale(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
+                                  const unsigned int* mx_in, unsigned int* mx_out, cudaStream_t st);
 cudaError_t launch_mli_colspan(const MliPlan& P, int* cbase, int* flag, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_col16(const MliPlan& P, const int* cbase, int sm_count, cudaStream_t st);
 cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, int sm_count, cudaStream_t st);
+// mode kModeScale: mx_in (or nsq_in, or neither: e = 0) sets the rescale,
+// the stored rows' magnitude keys go to atomicMax(*mx_out); kModePower may
+// take its rescale from mx_in as well.
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st, int l1 = 0, double* npart = nullptr);
+                              cudaStream_t st, int l1 = 0, double* npart = nullptr,
+                              const unsigned int* mx_in = nullptr, unsigned int* mx_out = nullptr);
 // Carries of the merge SpMV into y (MODE_POWER: times the rescale factor of
 // nsq_in).
 cudaError_t launch_merge_fixup_f64(int mode, const DevMatrix& M, const int2* tiles, int num_tiles, double* y,
@@ -147,8 +174,10 @@ cudaError_t launch_power_norm_f64(const double* y, const double* x, int n, doubl
                                   double* out, int grid, cudaStream_t st);
 cudaError_t launch_power_finalize_f64(double* last, const double* nsq_last, double* prev, const double* nsq_prev,
                                       int n, int sm_count, cudaStream_t st);
+// Rows [first_row, last_row) of the Poisson matrix (last_row < 0: all m*n).
 cudaError_t launch_poisson_crs(int m, int n, int32_t* row_start, int32_t* col, double* val, int sm_count,
-                               cudaStream_t st);
+                               cudaStream_t st, int first_row = 0, int last_row = -1);
+long long poisson_rows_nnz(int m, int n, int first_row, int last_row);
 cudaError_t launch_dot2_f64(const double* a, const double* b, int n, double* partials, unsigned int* counter,
                             double* out, int grid, cudaStream_t st);
 cudaError_t launch_dot2_f32(const float* a, const float* b, int n, double* partials, unsigned int* counter,
@@ -216,6 +245,12 @@ cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_c
 cudaError_t launch_tile_slots(const BatchTable* T, int nslots, cudaStream_t st);
 cudaError_t launch_fill_uniform(double* x, int n, uint64_t seed, int sm_count, cudaStream_t st);
 
+// The tile kernel (k_csb_spmv) runs both blocked formats: rows in windows of
+// S, each window's tiles ("units", elements of one block in an S-column
+// window) from a list; tiles of at least kTileDenseUnit elements stage their
+// x window in shared memory, the rest are merged into one gathered unit.
+constexpr int kTileDenseUnit = 256;
+
 // csb.cu: CSB (CSB.hpp) parameters, host build and SpMV
 void csb_params(int nor, int noc, int* beta, int* bits);
 int csb_window(int nor, int beta, int sm_count);
@@ -236,9 +271,16 @@ int coh_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
                    std::vector<uint16_t>& col_jump, std::vector<double>& data, std::vector<int32_t>& block_nnz,
                    std::vector<int16_t>& row_jump_block, std::vector<int16_t>& col_jump_block,
                    std::vector<int>& parts, std::vector<int>& blocks);
-cudaError_t launch_coh_spmv(const int* parts, int nparts, const int* blocks, const uint16_t* row_jump,
-                            const uint16_t* col_jump, const double* data, const double* x, double* y,
-                            const double* nsq_in, int sm_count, cudaStream_t st);
+// The CO-H matrix as tiles for the tile kernel: per window of S rows, the
+// tiles of its rows' CO-H blocks -- partitions in row order, each
+// partition's blocks in its Hilbert order, a block's tiles by column window
+// -- with elements row-major inside a tile (columns ascending per row, as
+// in the block's ICRS order).  Outputs as csb_build_host's (ind = local row
+// << 16 | column - tile column, win_ptr: sparse tiles then dense ones).
+// parts: 8 ints per partition as coh_build_host writes them.
+void coh_tile_units(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col, const double* val,
+                    const std::vector<int>& parts, int S, std::vector<uint32_t>& ind, std::vector<double>& data,
+                    std::vector<int>& win_ptr, std::vector<int>& unit_data);
 
 // Pipelined host-array SpMV: chunk records (4 ints per chunk: first
 // sub-tile, its first row, row-split flag, largest column read), and the

@@ -77,6 +77,8 @@ struct pwmgpu_matrix {
     int l1 = 0;
     float tune_ms[2] = {0.f, 0.f};
     int power_mode = PWMGPU_POWER_AUTO;
+    // grid barrier budget of the persistent power kernel (pwmgpu_test_grid_wait)
+    pwmgpu::GridWait grid_wait{pwmgpu::kWaitCycles, 0u};
     // format autotuner (PWMGPU_FMT_AUTO handles, tuned on every load): the
     // format whose FP64 SpMV runs (-1: the handle's own), the CSB kernel
     // variant, and what the tuner saw
@@ -104,6 +106,8 @@ struct pwmgpu_matrix {
     unsigned int* counter = nullptr;
     double* nsq = nullptr;
     size_t nsq_cap = 0;
+    unsigned int* mxk = nullptr;  // mxk[k]: largest magnitude key of iterate k (power steps in MODE_SCALE)
+    size_t mxk_cap = 0;
     double* small = nullptr;  // 16 doubles of reduction outputs
     int* status = nullptr;
     unsigned int* barrier = nullptr;  // grid barrier words of the persistent kernel
@@ -122,15 +126,17 @@ struct pwmgpu_matrix {
         std::vector<double> h_data;
         std::vector<int32_t> h_blk_ptr;
     } csb;
-    // CO-H format (coh.cu): the reference's arrays plus partition / block tables
+    // CO-H format (coh.cu): the reference's arrays (host) and the tiles the
+    // tile kernel runs (device; same layout as the CSB handle's)
     struct {
         int parts = 0;
         long long nblocks = 0;
-        int* d_parts = nullptr;
-        int* d_blocks = nullptr;
-        uint16_t* row_jump = nullptr;
-        uint16_t* col_jump = nullptr;
+        int S = 0, nwin = 0;
+        uint32_t* ind = nullptr;
+        int32_t* kcol = nullptr;
         double* data = nullptr;
+        int* win_ptr = nullptr;
+        int* units = nullptr;
         std::vector<int32_t> part_info, block_nnz;
         std::vector<uint16_t> h_row_jump, h_col_jump;
         std::vector<double> h_data;
@@ -165,11 +171,11 @@ struct pwmgpu_matrix {
         csb = decltype(csb)();
     }
     void release_coh() {
-        pwmgpu::dfree(coh.d_parts);
-        pwmgpu::dfree(coh.d_blocks);
-        pwmgpu::dfree(coh.row_jump);
-        pwmgpu::dfree(coh.col_jump);
+        pwmgpu::dfree(coh.ind);
+        pwmgpu::dfree(coh.kcol);
         pwmgpu::dfree(coh.data);
+        pwmgpu::dfree(coh.win_ptr);
+        pwmgpu::dfree(coh.units);
         coh = decltype(coh)();
     }
     void release_matrix() {
@@ -216,6 +222,7 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(npart);
         pwmgpu::dfree(counter);
         pwmgpu::dfree(nsq);
+        pwmgpu::dfree(mxk);
         pwmgpu::dfree(small);
         pwmgpu::dfree(status);
         pwmgpu::dfree(barrier);
@@ -225,7 +232,7 @@ struct pwmgpu_matrix {
         pwmgpu::dfree(dy);
         pwmgpu::dfree(fx);
         pwmgpu::dfree(fy);
-        carries_cap = partials_cap = npart_cap = nsq_cap = vec_cap = fvec_cap = 0;
+        carries_cap = partials_cap = npart_cap = nsq_cap = mxk_cap = vec_cap = fvec_cap = 0;
     }
 };
 

@@ -182,7 +182,26 @@ struct MergeArgs {
     int tile0 = 0;  // the pass covers sub-tiles [tile0, tile0 + nsub)
     const uint16_t* colp16 = nullptr;  // C16 kernels: 16-bit column offsets (base in rec0.w)
     double* npart = nullptr;  // MODE_POWER: per-CTA sums of the squares of the rows the CTA completes, or null
+    // MODE_POWER / MODE_SCALE: the largest magnitude key of x (source of the
+    // 2^e rescale instead of nsq_in), or null
+    const unsigned int* mx_in = nullptr;
+    unsigned int* mx_out = nullptr;  // MODE_SCALE: atomicMax target for the keys of y
 };
+
+// The 2^e rescale of a power step from its input's largest magnitude key or
+// squared norm (neither: e = 0).
+template <int MODE, typename XT>
+__device__ __forceinline__ int step_exponent(const unsigned int* mx_in, const double* nsq_in) {
+    if (MODE == MODE_SPMV) return 0;
+    if (mx_in) return pow2_rescale_exponent_key<XT>(*mx_in);
+    return nsq_in ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
+}
+
+// Fold a warp's magnitude keys into the global max (one atomic per warp).
+__device__ __forceinline__ void warp_max_out(unsigned mx, unsigned int* out) {
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0 && mx != 0u) atomicMax(out, mx);
+}
 
 constexpr int kMliStages = 2;
 
@@ -193,10 +212,12 @@ constexpr int kMliStages = 2;
 // this warp's copies in flight have landed or a short bound ran out.
 template <int MODE, typename VT, typename XT, typename AT, int NT, int IPT, bool XCOH, bool C16, bool CG = false>
 // MODE_POWER: ss += the squares of the rows the warp completes (as stored;
-// rows that a fix-up completes are left to the fix-up).
+// rows that a fix-up completes are left to the fix-up); MODE_SCALE: mx max=
+// their magnitude keys.
 __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const XT* __restrict__ x,
                                           XT* __restrict__ y, unsigned char* stages, uint64_t* bars, int* crow,
-                                          AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol, double& ss) {
+                                          AT* cval, AT* hval, uint32_t& ticket, int e, uint64_t pol, double& ss,
+                                          unsigned& mx) {
     using S = WarpStage<VT, IPT, C16>;
     constexpr int NS = kMliStages;
     constexpr int W = NT / 32;
@@ -227,10 +248,10 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         constexpr bool NORM = MODE == MODE_POWER;
         if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
             finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
-                                                                   crow, cval, hval, ss);
+                                                                   crow, cval, hval, ss, &mx);
         else
             finish_subtile<MODE, false, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
-                                                                    crow, cval, hval, ss);
+                                                                    crow, cval, hval, ss, &mx);
         // every lane is done with this stage (finish_subtile ends with a warp
         // barrier): refill it with the warp's sub-tile i + NS
         if (lane == 0 && i + NS < n) {
@@ -279,13 +300,15 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     __syncwarp();
     // x, y, carries and ||x||^2 may belong to the kernel before on the stream
     pdl_wait();
-    const int e = (MODE == MODE_POWER && a.nsq_in) ? pow2_rescale_exponent(*a.nsq_in, rescale_window<XT>()) : 0;
+    const int e = step_exponent<MODE, XT>(a.mx_in, a.nsq_in);
     uint32_t ticket = 0;
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
     double ss = 0.0;
+    unsigned mx = 0u;
     warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16, CG>(a, a.x, a.y, stages, bars[w], crow + 32 * w,
                                                          cval + 32 * w, hval + 32 * w, ticket, e,
-                                                         policy_evict_first(), ss);
+                                                         policy_evict_first(), ss, mx);
+    if (MODE == MODE_SCALE && a.mx_out) warp_max_out(mx, a.mx_out);
     if (MODE == MODE_POWER && a.npart) {
         // this CTA's share of ||y||^2 (k_fix_runs adds the fixed-up rows and
         // sums the shares in a fixed order)
@@ -350,6 +373,8 @@ struct FixNorm {
     int nspmv = 0;
     unsigned int* counter = nullptr;  // zero between launches
     double* nsq_out = nullptr;
+    const unsigned int* mx_in = nullptr;  // the step's rescale from its input's largest key (else nsq_in)
+    unsigned int* mx_out = nullptr;       // MODE_SCALE: atomicMax target for the keys of the fixed rows
 };
 
 // One thread per run: y[r] += (carries[t] + ... + carries[n-1]) -- the sums of
@@ -361,16 +386,19 @@ __global__ void __launch_bounds__(256) k_fix_runs(const int4* __restrict__ runs,
     const int kk = k0 + blockIdx.x * blockDim.x + threadIdx.x;
     const int4 d0 = kk < k1 ? runs[kk] : make_int4(0, 0, 0, 0);  // plan data: before the wait
     pdl_wait();  // carries and y come from the SpMV before on the stream
-    const int e = (MODE == MODE_POWER && nsq_in) ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
+    const int e = step_exponent<MODE, XT>(nrm.mx_in, nsq_in);
     double ss = 0.0;
+    unsigned mx = 0u;
     for (int k = kk; k < k1; k += gridDim.x * blockDim.x) {
         const int4 d = k == kk ? d0 : runs[k];
         AT sum = __ldcg(carries + d.x);
         for (int j = d.x + 1; j < d.y; ++j) sum += __ldcg(carries + j);
-        const XT v = (XT)((AT)__ldcg(y + d.z) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+        const XT v = (XT)((AT)__ldcg(y + d.z) + (MODE != MODE_SPMV && e != 0 ? scale_pow2(sum, e) : sum));
         y[d.z] = v;
         if (MODE == MODE_POWER) ss = fma((double)v, (double)v, ss);
+        if (MODE == MODE_SCALE) mx = max(mx, mag_key(v));
     }
+    if (MODE == MODE_SCALE && nrm.mx_out) warp_max_out(mx, nrm.mx_out);
     if (MODE != MODE_POWER || !nrm.npart) return;
     __shared__ double red[8];
     __shared__ bool am_last;
@@ -435,8 +463,11 @@ __global__ void __launch_bounds__(256) k_power_norm(const XT* __restrict__ y, co
 
 // ---------------------------------------------------------------------------
 // Grid-wide barrier for a cooperative launch, with a bounded wait: after
-// kWaitCycles (or once another CTA has recorded a failure) it records
-// PWMGPU_ERR_TIMEOUT and returns false in every thread of the CTA.
+// `budget` clock64 cycles (kWaitCycles unless a test shortens it), or once
+// another CTA has recorded a failure, it records PWMGPU_ERR_TIMEOUT and
+// returns false in every thread of the CTA.  The barrier opens when
+// gridDim.x + extra CTAs have arrived (extra is 0 except in the timeout test,
+// whose barrier therefore never opens).
 // bar[0] counts arrivals, bar[1] is the generation; both start at zero.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
@@ -461,7 +492,7 @@ __device__ __forceinline__ void st_relaxed_gpu(unsigned int* p, unsigned int v) 
 // count and bumps the generation with a release; the others spin on the
 // generation with acquire loads.  After the final CTA barrier every thread's
 // ordinary loads see every CTA's writes from before the barrier.
-__device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
+__device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status, long long budget, unsigned int extra) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -469,7 +500,7 @@ __device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
         __threadfence();
         const unsigned int arrived = atom_add_acq_rel_gpu(bar, 1u) + 1u;
         int ok = 1;
-        if (arrived == gridDim.x) {
+        if (arrived == gridDim.x + extra) {
             st_relaxed_gpu(bar, 0u);
             red_add_release_gpu(bar + 1, 1u);
         } else {
@@ -478,7 +509,7 @@ __device__ __forceinline__ bool grid_sync(unsigned int* bar, int* status) {
             while (ld_acquire_gpu(bar + 1) == g) {
                 if ((++spins & 1023u) == 0u) {
                     if (*(volatile int*)status != PWMGPU_OK) { ok = 0; break; }
-                    if (clock64() - t0 > kWaitCycles) {
+                    if (clock64() - t0 > budget) {
                         atomicCAS(status, PWMGPU_OK, PWMGPU_ERR_TIMEOUT);
                         ok = 0;
                         break;
@@ -528,6 +559,10 @@ struct PowerArgs {
     double* result;    // null, or (k = k0+nk-1 >= 1): {lambda_k, residual^2, ||v_k||^2, v_k.v_{k+1}, e_k}
     double* partials;  // 2 per CTA
     unsigned int* barrier;
+    GridWait wait;     // grid barrier budget and extra arrivals
+    // mxk[k]: largest magnitude key of v_k, zeroed (or null: every iteration
+    // sums ||v||^2).  Iterations before the last two store only the keys.
+    unsigned int* mxk;
 };
 
 // Sum two per-CTA partials over the grid in a fixed order (every CTA gets the
@@ -578,23 +613,44 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
     double nsq_cur = p.k0 > 0 ? p.nsq[p.k0] : 0.0;
     double nsq_last = 0.0;
     int e = 0;
+    bool prev_keys = false;  // iteration k-1 stored only its magnitude keys (mxk[k])
     unsigned char* stages = smem_raw + (size_t)w * NS * S::BYTES;
     const int tid = blockIdx.x * NT + threadIdx.x, nthr = gridDim.x * NT;
     for (int k = p.k0; k < p.k0 + p.nk; ++k) {
         const XT* in = (k & 1) ? p.Y : p.X;
         XT* out = (k & 1) ? p.X : p.Y;
-        e = k > 0 ? pow2_rescale_exponent(nsq_cur, rescale_window<XT>()) : 0;
+        e = k == 0 ? 0
+            : prev_keys ? pow2_rescale_exponent_key<XT>(__ldcg(p.mxk + k))
+                        : pow2_rescale_exponent(nsq_cur, rescale_window<XT>());
+        if (p.mxk && k < p.k0 + p.nk - 2) {
+            // only the rescale needs this iterate's size: the largest key,
+            // folded into mxk[k+1] by every warp, read after the barrier
+            double no_ss = 0.0;
+            unsigned mx = 0u;
+            warp_pass<MODE_SCALE, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
+                                                                  cval + 32 * w, hval + 32 * w, ticket, e, pol,
+                                                                  no_ss, mx);
+            if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
+            fixup_pass<MODE_SCALE, XT, AT, false>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
+                                                  nthr, no_ss, &mx);
+            warp_max_out(mx, p.mxk + k + 1);
+            if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
+            prev_keys = true;
+            continue;
+        }
+        prev_keys = false;
         nsq_last = nsq_cur;
         const bool want_dot = p.result && k == p.k0 + p.nk - 1;
         double ss = 0.0, dd = 0.0;
+        unsigned mx = 0u;
         warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
-                                                              cval + 32 * w, hval + 32 * w, ticket, e, pol, ss);
-        if (!grid_sync(p.barrier, a.status)) return;
+                                                              cval + 32 * w, hval + 32 * w, ticket, e, pol, ss, mx);
+        if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
         fixup_pass<MODE_POWER, XT, AT, true>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
                                              nthr, ss);
         if (want_dot) {
             // the Rayleigh dot needs v_k: a row pass for both sums
-            if (!grid_sync(p.barrier, a.status)) return;
+            if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
             ss = 0.0;
             norm_rows<XT, true>(out, in, 0, a.nor, tid, nthr, ss, dd);
         }
@@ -604,7 +660,7 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
             p.partials[2 * blockIdx.x] = t_ss;
             p.partials[2 * blockIdx.x + 1] = t_dd;
         }
-        if (!grid_sync(p.barrier, a.status)) return;
+        if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
         grid_total2<NT>(p.partials, total);  // every CTA, same order
         nsq_cur = total[0];
         const double dot = total[1];
@@ -619,12 +675,12 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
                 rr = fma(d, d, rr);
             }
             const double t_rr = block_sum<NT>(rr, red);
-            if (!grid_sync(p.barrier, a.status)) return;  // everyone has read partials
+            if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;  // everyone has read partials
             if (threadIdx.x == 0) {
                 p.partials[2 * blockIdx.x] = t_rr;
                 p.partials[2 * blockIdx.x + 1] = 0.0;
             }
-            if (!grid_sync(p.barrier, a.status)) return;
+            if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
             grid_total2<NT>(p.partials, total);
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 p.result[0] = lam;
@@ -668,18 +724,21 @@ __host__ __device__ inline long long poisson_row_start(long long row, long long 
     return below + left + row + right + above;
 }
 
-__global__ void k_poisson_crs(int m, int n, int32_t* __restrict__ row_start, int32_t* __restrict__ col,
-                              double* __restrict__ val) {
+// Rows [r0, r1) of the m x n matrix (Poisson.hpp:33-83 with first_row /
+// last_row): row starts counted from row r0, global columns.
+__global__ void k_poisson_crs(int m, int n, int r0, int r1, int32_t* __restrict__ row_start,
+                              int32_t* __restrict__ col, double* __restrict__ val) {
     const int N = m * n;
-    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < N; row += gridDim.x * blockDim.x) {
-        long long k = poisson_row_start(row, m, n);
+    const long long k0 = poisson_row_start(r0, m, n);
+    for (int row = r0 + blockIdx.x * blockDim.x + threadIdx.x; row < r1; row += gridDim.x * blockDim.x) {
+        long long k = poisson_row_start(row, m, n) - k0;
         if (row >= m) { col[k] = row - m; val[k] = -1.0; ++k; }
         if (row % m != 0) { col[k] = row - 1; val[k] = -1.0; ++k; }
         col[k] = row; val[k] = 4.0; ++k;
         if (row % m != m - 1) { col[k] = row + 1; val[k] = -1.0; ++k; }
         if (row < N - m) { col[k] = row + m; val[k] = -1.0; ++k; }
-        row_start[row + 1] = (int32_t)k;
-        if (row == 0) row_start[0] = 0;
+        row_start[row - r0 + 1] = (int32_t)k;
+        if (row == r0) row_start[0] = 0;
     }
 }
 
@@ -860,8 +919,10 @@ struct MergeKernels {
     template <int L1, bool C16>
     static int setup_spmv() {
         setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
+        setup(k_merge_spmv<MODE_SCALE, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
         if constexpr (kHasCG) {
             setup(k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16, true>, L1, smem(C16));
+            setup(k_merge_spmv<MODE_SCALE, VT, XT, AT, NT, IPT, L1, C16, true>, L1, smem(C16));
             setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16, true>, L1, smem(C16));
         }
         return setup(k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16>, L1, smem(C16));
@@ -913,13 +974,14 @@ struct MergeKernels {
 
     static cudaError_t power(const DevMatrix& M, const void* valp, const MliPlan& P, int grid, void* X, void* Y,
                              void* carries, int k0, int nk, double* nsq, double* result, double* partials,
-                             unsigned int* barrier, int* status, cudaStream_t st, int v) {
+                             unsigned int* barrier, int* status, cudaStream_t st, int v, GridWait wait,
+                             unsigned int* mxk) {
         if (!P.colp16) v &= ~2;
         v &= 3;
         power_occ(v);
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
                                  nullptr, (AT*)carries, nullptr, status, 0, P.colp16},
-                                P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier};
+                                P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier, wait, mxk};
         cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned int), st);
         if (e != cudaSuccess) return e;
         void* args[] = {&p};
@@ -942,6 +1004,8 @@ struct MergeKernels {
         cfg.numAttrs = pdl ? 1 : 0;
         if (mode == MODE_POWER)
             cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_POWER, VT, XT, AT, NT, IPT, L1, C16, CG>, a);
+        else if (mode == MODE_SCALE)
+            cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_SCALE, VT, XT, AT, NT, IPT, L1, C16, CG>, a);
         else
             cudaLaunchKernelEx(&cfg, k_merge_spmv<MODE_SPMV, VT, XT, AT, NT, IPT, L1, C16, CG>, a);
     }
@@ -961,12 +1025,13 @@ struct MergeKernels {
     static cudaError_t spmv(int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                             const void* x, void* y, void* carries, const double* nsq_in, int* status,
                             cudaStream_t st, int v, int tile0 = 0, int nsub = -1, bool pdl = true,
-                            double* npart = nullptr) {
+                            double* npart = nullptr, const unsigned int* mx_in = nullptr,
+                            unsigned int* mx_out = nullptr) {
         if (!P.colp16) v &= ~2;
         geom(v);
         MergeArgs<VT, XT, AT> a{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor,
                                 nsub < 0 ? P.nsub : nsub, (const XT*)x, (XT*)y, (AT*)carries, nsq_in, status,
-                                tile0, P.colp16, npart};
+                                tile0, P.colp16, npart, mx_in, mx_out};
         const bool cg = (v >> 2) & 1;
         switch (v & 3) {
             case 1: launch_spmv_cg<1, false>(cg, mode, a, grid, st, pdl); break;
@@ -1018,18 +1083,19 @@ int power_persistent_grid(int cfg, int nsub, int sm_count, int l1) {
 
 cudaError_t launch_power_persistent(int cfg, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                                     void* X, void* Y, void* carries, int k0, int nk, double* nsq, double* result,
-                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st, int l1) {
+                                    double* partials, unsigned int* barrier, int* status, cudaStream_t st, int l1,
+                                    GridWait wait, unsigned int* mxk) {
     if (nk <= 0) return cudaSuccess;
     switch (cfg) {
         case kCfgF32:
             return CfgF32::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st,
-                                 l1);
+                                 l1, wait, mxk);
         case kCfgBF16:
             return CfgBF16::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status,
-                                  st, l1);
+                                  st, l1, wait, mxk);
         default:
             return CfgF64::power(M, valp, P, grid, X, Y, carries, k0, nk, nsq, result, partials, barrier, status, st,
-                                 l1);
+                                 l1, wait, mxk);
     }
 }
 
@@ -1087,15 +1153,19 @@ cudaError_t launch_mli_unpermute(const MliPlan& P, int32_t* col, double* val, in
 
 cudaError_t launch_merge_spmv(int cfg, int mode, const DevMatrix& M, const void* valp, const MliPlan& P, int grid,
                               const void* x, void* y, void* carries, const double* nsq_in, int* status,
-                              cudaStream_t st, int l1, double* npart) {
+                              cudaStream_t st, int l1, double* npart, const unsigned int* mx_in,
+                              unsigned int* mx_out) {
     if (P.nsub == 0) return cudaSuccess;
     switch (cfg) {
         case kCfgF32:
-            return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
+            return CfgF32::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart,
+                                mx_in, mx_out);
         case kCfgBF16:
-            return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
+            return CfgBF16::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart,
+                                 mx_in, mx_out);
         default:
-            return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart);
+            return CfgF64::spmv(mode, M, valp, P, grid, x, y, carries, nsq_in, status, st, l1, 0, -1, true, npart,
+                                mx_in, mx_out);
     }
 }
 
@@ -1259,7 +1329,7 @@ int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, 
 template <typename XT, typename AT>
 static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT* y, const AT* carries,
                                  const double* nsq_in, cudaStream_t st, const FixNorm& nrm = FixNorm{}) {
-    if (k1 <= k0 && !nrm.npart) return cudaSuccess;
+    if (k1 <= k0 && !nrm.npart) return cudaSuccess;  // (a MODE_SCALE step without runs has no keys to add)
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(k1 > k0 ? (k1 - k0 + 255) / 256 : 1);  // the norm's last CTA runs even without runs
     cfg.blockDim = dim3(256);
@@ -1272,6 +1342,8 @@ static cudaError_t fix_runs_impl(int mode, const MliPlan& P, int k0, int k1, XT*
     const int4* runs = P.runs;
     if (mode == MODE_POWER)
         cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_POWER, XT, AT>, runs, k0, k1, y, carries, nsq_in, nrm);
+    else if (mode == MODE_SCALE)
+        cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_SCALE, XT, AT>, runs, k0, k1, y, carries, nsq_in, nrm);
     else
         cudaLaunchKernelEx(&cfg, k_fix_runs<MODE_SPMV, XT, AT>, runs, k0, k1, y, carries, nsq_in, FixNorm{});
     return cudaGetLastError();
@@ -1291,14 +1363,27 @@ int power_norm_parts(const MliPlan& P, int spmv_grid) {
     return spmv_grid + (P.nruns > 0 ? (P.nruns + 255) / 256 : 1);
 }
 
+cudaError_t launch_fix_runs_scale(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
+                                  const unsigned int* mx_in, unsigned int* mx_out, cudaStream_t st) {
+    FixNorm nrm;
+    nrm.mx_in = mx_in;
+    nrm.mx_out = mx_out;
+    if (f32)
+        return fix_runs_impl<float, float>(MODE_SCALE, P, 0, P.nruns, (float*)y, (const float*)carries, nsq_in, st,
+                                           nrm);
+    return fix_runs_impl<double, double>(MODE_SCALE, P, 0, P.nruns, (double*)y, (const double*)carries, nsq_in, st,
+                                         nrm);
+}
+
 cudaError_t launch_fix_runs_norm(bool f32, const MliPlan& P, void* y, const void* carries, const double* nsq_in,
                                  double* npart, int spmv_grid, unsigned int* counter, double* nsq_out,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, const unsigned int* mx_in) {
     FixNorm nrm;
     nrm.npart = npart;
     nrm.nspmv = spmv_grid;
     nrm.counter = counter;
     nrm.nsq_out = nsq_out;
+    nrm.mx_in = mx_in;
     if (f32)
         return fix_runs_impl<float, float>(MODE_POWER, P, 0, P.nruns, (float*)y, (const float*)carries, nsq_in, st,
                                            nrm);
@@ -1322,13 +1407,18 @@ cudaError_t launch_power_finalize_f64(double* last, const double* nsq_last, doub
 }
 
 cudaError_t launch_poisson_crs(int m, int n, int32_t* row_start, int32_t* col, double* val, int sm_count,
-                               cudaStream_t st) {
-    long long N = (long long)m * n;
-    long long blocks = (N + 255) / 256;
+                               cudaStream_t st, int first_row, int last_row) {
+    if (last_row < 0) last_row = m * n;
+    long long rows = (long long)last_row - first_row;
+    long long blocks = (rows + 255) / 256;
     if (blocks > sm_count * 16) blocks = sm_count * 16;
     if (blocks < 1) blocks = 1;
-    k_poisson_crs<<<(int)blocks, 256, 0, st>>>(m, n, row_start, col, val);
+    k_poisson_crs<<<(int)blocks, 256, 0, st>>>(m, n, first_row, last_row, row_start, col, val);
     return cudaGetLastError();
+}
+
+long long poisson_rows_nnz(int m, int n, int first_row, int last_row) {
+    return poisson_row_start(last_row, m, n) - poisson_row_start(first_row, m, n);
 }
 
 int dot_grid(long long n, int sm_count) {

@@ -173,7 +173,12 @@ __device__ __forceinline__ void load_lane(const T* p, int qm, int cnt, int lane,
     }
 }
 
-enum MergeMode { MODE_SPMV = 0, MODE_POWER = 1 };
+// MODE_SPMV: y = A x.  MODE_POWER: y = 2^e A x with ||y||^2 summed (the power
+// method's steps whose norm is used).  MODE_SCALE: y = 2^e A x tracking only
+// the largest |y_i| (magnitude keys, integer max) -- the power method's
+// intermediate steps, whose norm serves only the exponent of the exact
+// power-of-two rescale.
+enum MergeMode { MODE_SPMV = 0, MODE_POWER = 1, MODE_SCALE = 2 };
 
 // One warp's shared-memory stage: the staged sub-tile's record, row-end
 // masks, lane-interleaved columns and values.  C16: the columns are stored as
@@ -259,6 +264,7 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 //             (as stored), except a row that began in an earlier sub-tile:
 //             its value here is a partial that the fix-up completes (and
 //             squares)
+//   mx        MODE_SCALE: max= the magnitude keys of the same rows
 // NORM, common path (no empty row in the sub-tile): the completed rows are
 // collected in the stage's column / value area -- free once every lane holds
 // its columns and values in registers; the rows [fr, rw1) are consecutive --
@@ -272,7 +278,7 @@ template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT
 __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const AT (&xv)[IPT],
                                                const int32_t* __restrict__ row_start, XT* __restrict__ y,
                                                AT* __restrict__ carries, int nor, int e, int* crow, AT* cval,
-                                               AT* hval, double& ss) {
+                                               AT* hval, double& ss, unsigned* mx = nullptr) {
     using S = WarpStage<VT, IPT, C16>;
     static_assert(S::COL_B + S::VAL_B >= S::WM * (int)sizeof(XT), "row buffer must fit the stage");
     const int lane = threadIdx.x & 31;
@@ -327,12 +333,13 @@ __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const A
             acc = fma((AT)vr[j], xv[j], acc);
             if ((mask >> j) & 1u) {
                 AT v = acc;
-                if (MODE == MODE_POWER && e != 0) v = scale_pow2(v, e);
+                if (MODE != MODE_SPMV && e != 0) v = scale_pow2(v, e);
                 if (to_head) {
                     hval[lane] = v;
                 } else if (!BUF) {
                     y[a] = (XT)v;
                     if (NORM && a != open_row) ss = fma((double)(XT)v, (double)(XT)v, ss);
+                    if (MODE == MODE_SCALE && a != open_row) *mx = max(*mx, mag_key((XT)v));
                 } else {
                     rbuf[a - fr] = (XT)v;
                 }
@@ -368,10 +375,11 @@ __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const A
             // Lane u completes row a.  If the row began before lane u, lane u
             // left its part in hval[u] and the total is written here.
             if (cu < 0) {
-                const XT t = (XT)(hval[u] + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+                const XT t = (XT)(hval[u] + (MODE != MODE_SPMV && e != 0 ? scale_pow2(sum, e) : sum));
                 if (!BUF) {
                     y[a] = t;
                     if (NORM && a != open_row) ss = fma((double)t, (double)t, ss);
+                    if (MODE == MODE_SCALE && a != open_row) *mx = max(*mx, mag_key(t));
                 } else {
                     rbuf[a - fr] = t;
                 }
@@ -403,11 +411,12 @@ __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const A
 // the carries times 2^e.  Threads take the first sub-tiles t = t0, t0 +
 // stride, ... < t_end (a run starting before t_end may extend past it).
 // ---------------------------------------------------------------------------
-// NORM: ss += the FP64 squares of the completed rows (as stored).
+// NORM: ss += the FP64 squares of the completed rows (as stored); MODE_SCALE:
+// mx max= their magnitude keys.
 template <int MODE, typename XT, typename AT, bool NORM = false>
 __device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start, const int2* __restrict__ tiles,
                                            int nor, int num_tiles, XT* __restrict__ y, const AT* __restrict__ carries,
-                                           int e, int t0, int t_end, int stride, double& ss) {
+                                           int e, int t0, int t_end, int stride, double& ss, unsigned* mx = nullptr) {
     for (int t = t0; t < t_end; t += stride) {
         const int r = tiles[t + 1].x;
         if (r >= nor) continue;
@@ -418,9 +427,10 @@ __device__ __forceinline__ void fixup_pass(const int32_t* __restrict__ row_start
         while (n < num_tiles && tiles[n + 1].x == r) sum += __ldcg(carries + n++);
         // sub-tile n starts at (r, tiles[n].y) and completes row r
         if (tiles[n].y > row_start[r]) {
-            const XT v = (XT)((AT)__ldcg(y + r) + (MODE == MODE_POWER && e != 0 ? scale_pow2(sum, e) : sum));
+            const XT v = (XT)((AT)__ldcg(y + r) + (MODE != MODE_SPMV && e != 0 ? scale_pow2(sum, e) : sum));
             y[r] = v;
             if (NORM) ss = fma((double)v, (double)v, ss);
+            if (MODE == MODE_SCALE) *mx = max(*mx, mag_key(v));
         }
     }
 }

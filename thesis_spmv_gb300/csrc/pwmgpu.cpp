@@ -126,44 +126,29 @@ int build_format(pwmgpu_matrix* m) {
                                  c.h_row_jump, c.h_col_jump, c.h_data, c.block_nnz, c.row_jump_block,
                                  c.col_jump_block, parts, blocks);
         c.nblocks = (long long)c.block_nnz.size();
-        // the kernel's copy of the column jumps and values: every block from a
-        // multiple of 8 elements (a lane's 8 elements are one 16-byte load of
-        // jumps and four of values); blocks[8 b + 2] = the block's first element
-        std::vector<uint16_t> kcj;
-        std::vector<double> kd;
-        {
-            long long o = 0;
-            const size_t nb = blocks.size() / 8;
-            for (size_t b = 0; b < nb; ++b) o = ((o + 7) & ~7LL) + blocks[8 * b + 4];
-            if (o + 16 > (long long)INT32_MAX)
-                return fail(PWMGPU_ERR_INVALID, "CO-H: the padded device copy exceeds 32-bit element offsets");
-            kcj.assign((size_t)((o + 7) & ~7LL) + 8, 0);
-            kd.assign(kcj.size(), 0.0);
-            o = 0;
-            for (size_t b = 0; b < nb; ++b) {
-                o = (o + 7) & ~7LL;
-                const int first = blocks[8 * b + 2], n = blocks[8 * b + 4];
-                std::copy(c.h_col_jump.begin() + first, c.h_col_jump.begin() + first + n, kcj.begin() + o);
-                std::copy(c.h_data.begin() + first, c.h_data.begin() + first + n, kd.begin() + o);
-                blocks[8 * b + 2] = (int)o;
-                o += n;
-            }
-        }
-        TRY(dalloc(&c.d_parts, parts.size()));
-        TRY(dalloc(&c.d_blocks, blocks.size() + 8));
-        TRY(dalloc(&c.row_jump, c.h_row_jump.size() + 8));
-        TRY(dalloc(&c.col_jump, kcj.size()));
-        TRY(dalloc(&c.data, kd.size()));
-        CU(cudaMemcpyAsync(c.d_parts, parts.data(), sizeof(int) * parts.size(), cudaMemcpyHostToDevice, m->stream));
-        if (!blocks.empty())
-            CU(cudaMemcpyAsync(c.d_blocks, blocks.data(), sizeof(int) * blocks.size(), cudaMemcpyHostToDevice,
-                               m->stream));
-        if (!c.h_row_jump.empty())
-            CU(cudaMemcpyAsync(c.row_jump, c.h_row_jump.data(), sizeof(uint16_t) * c.h_row_jump.size(),
-                               cudaMemcpyHostToDevice, m->stream));
-        CU(cudaMemcpyAsync(c.col_jump, kcj.data(), sizeof(uint16_t) * kcj.size(), cudaMemcpyHostToDevice,
+        // the kernel's copy: the blocks as tiles of the tile kernel (windows
+        // of S rows, Hilbert block order per partition; csb.cu / coh.cu)
+        c.S = csb_window(nor, 1024, m->sm_count);
+        c.nwin = (nor + c.S - 1) / c.S;
+        std::vector<uint32_t> tind, kind;
+        std::vector<double> tdata, kdata;
+        std::vector<int32_t> kcol;
+        std::vector<int> win_ptr, units;
+        coh_tile_units(nor, noc, nnz, rs.data(), ci.data(), va.data(), parts, c.S, tind, tdata, win_ptr, units);
+        if (!csb_kernel_layout(tind, tdata, c.S, win_ptr, units, kind, kdata, kcol))
+            return fail(PWMGPU_ERR_INVALID, "CO-H: the padded device copy exceeds 32-bit element offsets");
+        TRY(dalloc(&c.ind, kind.size()));
+        TRY(dalloc(&c.kcol, kcol.size()));
+        TRY(dalloc(&c.data, kdata.size()));
+        TRY(dalloc(&c.win_ptr, win_ptr.size()));
+        TRY(dalloc(&c.units, units.size() + 4));
+        CU(cudaMemcpyAsync(c.ind, kind.data(), sizeof(uint32_t) * kind.size(), cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(c.kcol, kcol.data(), sizeof(int32_t) * kcol.size(), cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(c.data, kdata.data(), sizeof(double) * kdata.size(), cudaMemcpyHostToDevice, m->stream));
+        CU(cudaMemcpyAsync(c.win_ptr, win_ptr.data(), sizeof(int) * win_ptr.size(), cudaMemcpyHostToDevice,
                            m->stream));
-        CU(cudaMemcpyAsync(c.data, kd.data(), sizeof(double) * kd.size(), cudaMemcpyHostToDevice, m->stream));
+        if (!units.empty())
+            CU(cudaMemcpyAsync(c.units, units.data(), sizeof(int) * units.size(), cudaMemcpyHostToDevice, m->stream));
     }
     CU(cudaStreamSynchronize(m->stream));
     TRY(ensure_cap(&m->partials, &m->partials_cap, (size_t)2 * dot_grid(m->M.nor, m->sm_count) + 64));
@@ -317,11 +302,10 @@ int tune_csb(pwmgpu_matrix* m);
 
 int build_plan(pwmgpu_matrix* m) {
     if (m->auto_fmt) return build_auto(m);
-    if (m->format == PWMGPU_FMT_CSB) {
+    if (m->format == PWMGPU_FMT_CSB || m->format == PWMGPU_FMT_COH) {
         TRY(build_format(m));
         return tune_csb(m);
     }
-    if (m->format != PWMGPU_FMT_MERGE) return build_format(m);
     return build_merge(m, true);
 }
 }  // namespace pwmgpu
@@ -344,6 +328,18 @@ int ensure_vectors(pwmgpu_matrix* m) {
 namespace {
 
 int ensure_nsq(pwmgpu_matrix* m, size_t need) { return ensure_cap(&m->nsq, &m->nsq_cap, need + 1); }
+
+// Magnitude keys of `need` iterates, zeroed (the steps atomicMax into them).
+int ensure_mxk(pwmgpu_matrix* m, size_t need) {
+    if (m->mxk_cap < need || !m->mxk) {
+        dfree(m->mxk);
+        m->mxk_cap = 0;
+        TRY(dalloc(&m->mxk, need));
+        m->mxk_cap = need;
+    }
+    CU(cudaMemsetAsync(m->mxk, 0, sizeof(unsigned int) * need, m->stream));
+    return PWMGPU_OK;
+}
 
 int alloc_matrix(pwmgpu_matrix* m, int32_t nor, int32_t noc, long long nnz) {
     m->release_matrix();
@@ -381,8 +377,8 @@ int spmv_format(pwmgpu_matrix* m, int fmt, const double* dx, double* dy, const d
                            m->status, m->sm_count, m->stream, m->csb_var));
     } else {
         const auto& c = m->coh;
-        CU(launch_coh_spmv(c.d_parts, c.parts, c.d_blocks, c.row_jump, c.col_jump, c.data, dx, dy, nsq_in,
-                           m->sm_count, m->stream));
+        CU(launch_csb_spmv(c.ind, c.kcol, c.data, c.win_ptr, c.units, c.nwin, c.S, m->M.nor, m->M.noc, dx, dy, nsq_in,
+                           m->status, m->sm_count, m->stream, m->csb_var));
     }
     return PWMGPU_OK;
 }
@@ -417,12 +413,13 @@ bool norm_in_step(const pwmgpu_matrix* m, int grid) {
 // fix-up), and nsq_out = ||out||^2 (deterministic): summed by the two kernels
 // from the rows they store, or a row pass where the plan has no run
 // descriptors.
-int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out) {
+int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, double* nsq_out,
+                   const unsigned int* mx_in = nullptr) {
     if (norm_in_step(m, m->grid)) {
         CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
-                             m->status, m->stream, m->l1, m->npart));
+                             m->status, m->stream, m->l1, m->npart, mx_in));
         CU(launch_fix_runs_norm(false, m->P, out, m->carries, nsq_in, m->npart, m->grid, m->counter + 1, nsq_out,
-                                m->stream));
+                                m->stream, mx_in));
         return PWMGPU_OK;
     }
     CU(launch_merge_spmv(kCfgF64, kModePower, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
@@ -434,6 +431,22 @@ int power_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double
                                   m->fix_grid, m->stream));
     CU(launch_power_norm_f64(out, nullptr, m->M.nor, m->partials, m->counter, nsq_out,
                              dot_grid(m->M.nor, m->sm_count), m->stream));
+    return PWMGPU_OK;
+}
+
+// A power step whose norm only decides the exact power-of-two rescale: out =
+// 2^e A in (e from the input's largest magnitude key *mx_in, or its squared
+// norm *nsq_in, or 0), and atomicMax(*mx_out) of out's magnitude keys (an
+// integer max on the stored rows -- no FP64 square per row, no norm shares).
+// Scaling by powers of two is exact, so an iterate differs from the one an
+// exact-norm step would give by a power of two only, which the final
+// normalisation (by the exact norms of the last two iterates) removes.
+// Needs the plan's run descriptors (norm_in_step).
+int scale_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double* nsq_in, const unsigned int* mx_in,
+                   unsigned int* mx_out) {
+    CU(launch_merge_spmv(kCfgF64, kModeScale, m->M, m->P.valp, m->P, m->grid, in, out, m->carries, nsq_in,
+                         m->status, m->stream, m->l1, nullptr, mx_in, mx_out));
+    CU(launch_fix_runs_scale(false, m->P, out, m->carries, nsq_in, mx_in, mx_out, m->stream));
     return PWMGPU_OK;
 }
 
@@ -471,14 +484,28 @@ int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
     if (m->power_mode == PWMGPU_POWER_FUSED && m->pgrid == 0)
         return fail(PWMGPU_ERR_UNSUPPORTED, "the fused power kernel cannot be made co-resident on this device");
     if (use_fused(m, m->pgrid)) {
-        // K5: all `it` iterations in one persistent launch
+        // K5: all `it` iterations in one persistent launch (the iterations
+        // before the last two track only the rescale's magnitude keys)
+        TRY(ensure_mxk(m, (size_t)it + 1));
         CU(launch_power_persistent(kCfgF64, m->M, m->P.valp, m->P, m->pgrid, dx, dy, m->carries, 0, it, m->nsq,
-                                   nullptr, m->partials, m->barrier, m->status, m->stream, m->l1));
+                                   nullptr, m->partials, m->barrier, m->status, m->stream, m->l1, m->grid_wait,
+                                   m->mxk));
     } else {
+        // The last two steps compute the exact norms the final normalisation
+        // uses; the steps before them only need the rescale exponent, from
+        // their input's largest magnitude key (MODE_SCALE).
+        const bool scale = norm_in_step(m, m->grid);
+        if (scale) TRY(ensure_mxk(m, (size_t)it + 1));
         for (int k = 0; k < it; ++k) {
             const double* in = (k % 2 == 0) ? dx : dy;
             double* out = (k % 2 == 0) ? dy : dx;
-            TRY(power_step_f64(m, in, out, k ? m->nsq + k : nullptr, m->nsq + k + 1));
+            const bool prev_scale = scale && k >= 1 && k - 1 < it - 2;  // step k-1 tracked keys only
+            const double* nsq_in = (k > 0 && !prev_scale) ? m->nsq + k : nullptr;
+            const unsigned int* mx_in = prev_scale ? m->mxk + k : nullptr;
+            if (scale && k < it - 2)
+                TRY(scale_step_f64(m, in, out, nsq_in, mx_in, m->mxk + k + 1));
+            else
+                TRY(power_step_f64(m, in, out, nsq_in, m->nsq + k + 1, mx_in));
         }
     }
     double* last = (it % 2 == 1) ? dy : dx;
@@ -609,22 +636,35 @@ int solve_chunk(pwmgpu_matrix* m, int cfg, const void* valp, int pgrid, void* X,
             }
         }
     } else if (use_fused(m, pgrid)) {
+        TRY(ensure_mxk(m, (size_t)(k0 + nk) + 1));
         CU(launch_power_persistent(cfg, m->M, valp, m->P, pgrid, X, Y, m->carries, k0, nk, m->nsq, m->small,
-                                   m->partials, m->barrier, m->status, m->stream, m->l1));
+                                   m->partials, m->barrier, m->status, m->stream, m->l1, m->grid_wait, m->mxk));
     } else {
         const bool f32 = cfg != kCfgF64;
         const int grid = merge_grid(cfg, m->num_tiles, m->sm_count, m->l1);
         const int dg = dot_grid(m->M.nor, m->sm_count);
+        // steps before the chunk's last two track only the rescale's
+        // magnitude keys (scale_step_f64); the last two sum ||v||^2
+        const bool keys = norm_in_step(m, grid) && nk > 2;
+        if (keys) TRY(ensure_mxk(m, (size_t)(k0 + nk) + 1));
         for (int k = k0; k < k0 + nk; ++k) {
             void* in = (k & 1) ? Y : X;
             void* out = (k & 1) ? X : Y;
-            const double* nsq_in = k > 0 ? m->nsq + k : nullptr;
+            const bool prev_keys = keys && k > k0 && k - 1 < k0 + nk - 2;
+            const double* nsq_in = (k > 0 && !prev_keys) ? m->nsq + k : nullptr;
+            const unsigned int* mx_in = prev_keys ? m->mxk + k : nullptr;
             const bool last = k == k0 + nk - 1;
+            if (keys && k < k0 + nk - 2) {
+                CU(launch_merge_spmv(cfg, kModeScale, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
+                                     m->stream, m->l1, nullptr, mx_in, m->mxk + k + 1));
+                CU(launch_fix_runs_scale(f32, m->P, out, m->carries, nsq_in, mx_in, m->mxk + k + 1, m->stream));
+                continue;
+            }
             if (!last && norm_in_step(m, grid)) {
                 CU(launch_merge_spmv(cfg, kModePower, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
-                                     m->stream, m->l1, m->npart));
+                                     m->stream, m->l1, m->npart, mx_in));
                 CU(launch_fix_runs_norm(f32, m->P, out, m->carries, nsq_in, m->npart, grid, m->counter + 1,
-                                        m->nsq + k + 1, m->stream));
+                                        m->nsq + k + 1, m->stream, mx_in));
                 continue;
             }
             CU(launch_merge_spmv(cfg, kModePower, m->M, valp, m->P, grid, in, out, m->carries, nsq_in, m->status,
@@ -1467,6 +1507,118 @@ int pwmgpu_set_power_mode(pwmgpu_matrix* m, int mode) {
     return PWMGPU_OK;
 }
 
+int pwmgpu_row_blocks(int32_t nor, int32_t parts, int32_t* first_rows, int32_t* thread_rows) {
+    if (nor < 0 || parts < 1 || !first_rows || !thread_rows)
+        return fail(PWMGPU_ERR_INVALID, "row blocks: nor >= 0, parts >= 1 and non-null outputs");
+    // Util/TripletToCRS.hpp:318-327: round(nor / partitions) on integers
+    const int32_t am = nor / parts;
+    int32_t last = 0;
+    for (int32_t i = 0; i < parts; ++i) {
+        first_rows[i] = last;
+        last = (i == parts - 1) ? nor : first_rows[i] + am;
+        thread_rows[i] = last - first_rows[i];
+    }
+    return PWMGPU_OK;
+}
+
+int pwmgpu_generate_poisson_rows(pwmgpu_matrix* m, int32_t mx, int32_t ny, int32_t first_row, int32_t last_row) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (mx < 1 || ny < 1) return fail(PWMGPU_ERR_INVALID, "Poisson grid must be at least 1x1 (got %d x %d)", mx, ny);
+    const long long N = (long long)mx * ny;
+    TRY(check_sizes(N, N, (long long)ny * (mx + 2LL * (mx - 1)) + 2LL * (ny - 1) * mx));
+    if (first_row < 0 || last_row < first_row || last_row > N)
+        return fail(PWMGPU_ERR_INVALID, "row block [%d, %d) outside the %lld rows", first_row, last_row, N);
+    const long long nnz = poisson_rows_nnz(mx, ny, first_row, last_row);
+    TRY(alloc_matrix(m, last_row - first_row, (int32_t)N, nnz));
+    if (last_row > first_row)
+        CU(launch_poisson_crs(mx, ny, m->M.row_start, m->M.col, m->M.val, m->sm_count, m->stream, first_row,
+                              last_row));
+    else
+        CU(cudaMemsetAsync(m->M.row_start, 0, sizeof(int32_t), m->stream));
+    return build_plan(m);
+}
+
+int pwmgpu_load_triplets_rows(pwmgpu_matrix* m, int32_t nor, int32_t noc, int32_t nnz, const int32_t* rows,
+                              const int32_t* cols, const double* vals, int32_t first_row, int32_t last_row) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    TRY(check_sizes(nor, noc, nnz));
+    if (nnz > 0 && (!rows || !cols || !vals)) return fail(PWMGPU_ERR_INVALID, "null triplet array");
+    if (first_row < 0 || last_row < first_row || last_row > nor)
+        return fail(PWMGPU_ERR_INVALID, "row block [%d, %d) outside the %d rows", first_row, last_row, nor);
+    // the block's entries, rows counted from first_row (TripletToCRS.hpp:328-345)
+    std::vector<int32_t> r, c;
+    std::vector<double> v;
+    for (int32_t i = 0; i < nnz; ++i) {
+        if (rows[i] < 0 || rows[i] >= nor)
+            return fail(PWMGPU_ERR_INVALID, "triplet entry %d: row %d outside [0, %d)", i, rows[i], nor);
+        if (rows[i] >= first_row && rows[i] < last_row) {
+            r.push_back(rows[i] - first_row);
+            c.push_back(cols[i]);
+            v.push_back(vals[i]);
+        }
+    }
+    const int32_t bn = (int32_t)r.size();
+    TripletIn in;
+    int rc = PWMGPU_OK;
+    do {
+        if ((rc = dalloc(&in.rows, (size_t)bn)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&in.cols, (size_t)bn)) != PWMGPU_OK) break;
+        if ((rc = dalloc(&in.vals, (size_t)bn)) != PWMGPU_OK) break;
+        cudaError_t e = cudaSuccess;
+        if (bn > 0) {
+            e = cudaMemcpyAsync(in.rows, r.data(), sizeof(int32_t) * (size_t)bn, cudaMemcpyHostToDevice, m->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(in.cols, c.data(), sizeof(int32_t) * (size_t)bn, cudaMemcpyHostToDevice,
+                                    m->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(in.vals, v.data(), sizeof(double) * (size_t)bn, cudaMemcpyHostToDevice, m->stream);
+        }
+        if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "triplet upload: %s", cudaGetErrorString(e)); break; }
+        rc = load_triplets_dev(m, last_row - first_row, noc, bn, in.rows, in.cols, in.vals, nullptr, nullptr, nullptr);
+    } while (0);
+    in.release();
+    return rc;
+}
+
+int pwmgpu_rows_step_device(pwmgpu_matrix* m, const double* dx_full, double* dy_loc, double* dnsq_loc) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (!dnsq_loc || (m->M.nor > 0 && (!dx_full || !dy_loc))) return fail(PWMGPU_ERR_INVALID, "null vector");
+    if (m->M.nor == 0) {
+        CU(cudaMemsetAsync(dnsq_loc, 0, sizeof(double), m->stream));
+        return PWMGPU_OK;
+    }
+    if (fp64_format(m) != PWMGPU_FMT_MERGE || m->num_tiles == 0) {
+        TRY(spmv_f64(m, dx_full, dy_loc));
+        CU(launch_power_norm_f64(dy_loc, nullptr, m->M.nor, m->partials, m->counter, dnsq_loc,
+                                 dot_grid(m->M.nor, m->sm_count), m->stream));
+        return PWMGPU_OK;
+    }
+    return power_step_f64(m, dx_full, dy_loc, nullptr, dnsq_loc);
+}
+
+int pwmgpu_rows_normalize_device(pwmgpu_matrix* m, double* dy_loc, const double* dnsq_total) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
+    if (m->M.nor == 0) return PWMGPU_OK;
+    if (!dy_loc || !dnsq_total) return fail(PWMGPU_ERR_INVALID, "null vector");
+    CU(launch_power_finalize_f64(dy_loc, dnsq_total, nullptr, nullptr, m->M.nor, m->sm_count, m->stream));
+    return PWMGPU_OK;
+}
+
+int pwmgpu_test_grid_wait(pwmgpu_matrix* m, int64_t cycles, int32_t extra) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (cycles == 0 && extra == 0) {
+        m->grid_wait = GridWait{kWaitCycles, 0u};
+        return PWMGPU_OK;
+    }
+    if (cycles < 10000 || cycles > kWaitCycles || (extra != 0 && extra != 1))
+        return fail(PWMGPU_ERR_INVALID, "grid wait: cycles in [1e4, %lld] and extra 0 or 1 (got %lld, %d)",
+                    (long long)kWaitCycles, (long long)cycles, extra);
+    m->grid_wait = GridWait{(long long)cycles, (unsigned int)extra};
+    return PWMGPU_OK;
+}
+
 int pwmgpu_solve(pwmgpu_matrix* m, double* x, int32_t max_it, double tol, int precision, pwmgpu_solve_info* info) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
     if (!m->loaded) return fail(PWMGPU_ERR_STATE, "no matrix loaded");
@@ -1532,13 +1684,8 @@ int pwmgpu_get_coh(pwmgpu_matrix* m, int32_t* part_info, uint16_t* row_jump, uin
         if (dst && !v.empty()) std::memcpy(dst, v.data(), sizeof(v[0]) * v.size());
     };
     put(part_info, c.part_info);
-    // the row jumps as the kernel reads them; the column jumps and values
-    // from the host copies (the device copy starts every block on a
-    // multiple of 8 elements)
-    if (row_jump && !c.h_row_jump.empty())
-        CU(cudaMemcpyAsync(row_jump, c.row_jump, sizeof(uint16_t) * c.h_row_jump.size(), cudaMemcpyDeviceToHost,
-                           m->stream));
-    CU(cudaStreamSynchronize(m->stream));
+    // the reference's arrays, kept on the host (the device holds the tiles)
+    put(row_jump, c.h_row_jump);
     put(col_jump, c.h_col_jump);
     put(data, c.h_data);
     put(block_nnz, c.block_nnz);
@@ -1651,8 +1798,7 @@ int pwmgpu_plan_info(const pwmgpu_matrix* m, int32_t* column_bytes, int32_t* gat
 namespace pwmgpu {
 namespace {
 
-constexpr int kCohPartsPerSM[4] = {8, 16, 24, 32};  // CO-H candidates (partitions per SM)
-constexpr int kCohPartsDefault = 24;
+constexpr int kCohPartsDefault = 24;  // CO-H partitions per SM
 
 struct TuneChoice {
     int fmt = PWMGPU_FMT_MERGE;
@@ -1723,10 +1869,11 @@ int build_candidate(pwmgpu_matrix* m, int fmt, int coh_pps = kCohPartsDefault) {
 
 }  // namespace
 
-// Load-time variant tuner of a CSB handle: with enough work to measure (the
-// merge tuner's threshold), time the four kernel variants and keep the
-// fastest (pwmgpu_set_csb_variant overrides it).  4096^2 stencil: 4 elements
-// per lane, 128 threads; irregular matrix: 256 threads.
+// Load-time variant tuner of a CSB or CO-H handle (both run the tile
+// kernel): with enough work to measure (the merge tuner's threshold), time
+// the four kernel variants and keep the fastest (pwmgpu_set_csb_variant
+// overrides it).  4096^2 stencil: 4 elements per lane, 128 threads;
+// irregular matrix: 256 threads.
 int tune_csb(pwmgpu_matrix* m) {
     m->csb_var = 0;
     const MergeGeom g = merge_geometry(kCfgF64, 0);
@@ -1736,7 +1883,7 @@ int tune_csb(pwmgpu_matrix* m) {
     int best = 0;
     for (int v = 0; v < kCsbVariants; ++v) {
         m->csb_var = v;
-        TRY(time_format(m, PWMGPU_FMT_CSB, &ms[v]));
+        TRY(time_format(m, m->format, &ms[v]));
         if (ms[v] < 0.97f * ms[best]) best = v;  // another variant only for a clear (3 %) gain
     }
     m->csb_var = best;
@@ -1794,18 +1941,17 @@ int build_auto(pwmgpu_matrix* m) {
             TRY(time_format(m, PWMGPU_FMT_CSB, &T.csb_ms[v]));
         }
         m->loaded = false;
-        // CO-H at each partition count (the format's layout depends on it)
+        // CO-H (the default partition count): the tile kernel's four variants
+        // on its tiles
         int coh_best = 0;
-        for (int i = 0; i < 4; ++i) {
-            TRY(build_candidate(m, PWMGPU_FMT_COH, kCohPartsPerSM[i]));
-            m->loaded = true;
-            TRY(time_format(m, PWMGPU_FMT_COH, &T.coh_ms[i]));
-            m->loaded = false;
-            if (T.coh_ms[i] < T.coh_ms[coh_best]) coh_best = i;
+        TRY(build_candidate(m, PWMGPU_FMT_COH, kCohPartsDefault));
+        m->loaded = true;
+        for (int v = 0; v < kCsbVariants; ++v) {
+            m->csb_var = v;
+            TRY(time_format(m, PWMGPU_FMT_COH, &T.coh_ms[v]));
+            if (T.coh_ms[v] < T.coh_ms[coh_best]) coh_best = v;
         }
-        // keep the best CO-H arrays (built from the CRS arrays, which the
-        // merge plan below releases)
-        if (coh_best != 3) TRY(build_candidate(m, PWMGPU_FMT_COH, kCohPartsPerSM[coh_best]));
+        m->loaded = false;
         // merge: plan and launch-variant tuner, then the same timing
         TRY(build_merge(m, true));
         TRY(time_format(m, PWMGPU_FMT_MERGE, &T.merge_ms));
@@ -1820,9 +1966,9 @@ int build_auto(pwmgpu_matrix* m) {
         if (T.coh_ms[coh_best] < best) {
             best = T.coh_ms[coh_best];
             choice.fmt = PWMGPU_FMT_COH;
-            choice.csb_var = 0;
+            choice.csb_var = coh_best;
         }
-        choice.coh_pps = kCohPartsPerSM[coh_best];
+        choice.coh_pps = kCohPartsDefault;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune_table[key] = choice;
     }
@@ -1830,7 +1976,7 @@ int build_auto(pwmgpu_matrix* m) {
     if (choice.fmt != PWMGPU_FMT_CSB) m->release_csb();
     if (choice.fmt != PWMGPU_FMT_COH) m->release_coh();
     m->tuned_fmt = choice.fmt;
-    m->csb_var = choice.fmt == PWMGPU_FMT_CSB ? choice.csb_var : 0;
+    m->csb_var = choice.fmt == PWMGPU_FMT_MERGE ? 0 : choice.csb_var;
     T.format = choice.fmt;
     T.coh_partitions = choice.fmt == PWMGPU_FMT_COH ? choice.coh_pps * m->sm_count : 0;
     T.csb_variant = m->csb_var;
@@ -1885,7 +2031,7 @@ int pwmgpu_tuner_record(const int32_t key[7], int32_t format, int32_t csb_varian
     std::copy(key, key + 7, k.begin());
     pwmgpu::TuneChoice c;
     c.fmt = format;
-    c.csb_var = format == PWMGPU_FMT_CSB ? csb_variant : 0;
+    c.csb_var = format == PWMGPU_FMT_MERGE ? 0 : csb_variant;
     c.merge_var = merge_variant;
     c.coh_pps = coh_parts_per_sm ? coh_parts_per_sm : pwmgpu::kCohPartsDefault;
     std::lock_guard<std::mutex> lk(pwmgpu::g_tune_mu);
@@ -1912,7 +2058,8 @@ int pwmgpu_tuner_entries(int32_t max, int32_t* keys, int32_t* choices) {
 
 int pwmgpu_get_csb_variant(const pwmgpu_matrix* m, int32_t* variant) {
     if (!m || !variant) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null handle or output");
-    if (m->format != PWMGPU_FMT_CSB) return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB handle");
+    if (m->format != PWMGPU_FMT_CSB && m->format != PWMGPU_FMT_COH)
+        return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB or CO-H handle");
     *variant = m->csb_var;
     return PWMGPU_OK;
 }
@@ -1920,7 +2067,8 @@ int pwmgpu_get_csb_variant(const pwmgpu_matrix* m, int32_t* variant) {
 int pwmgpu_set_csb_variant(pwmgpu_matrix* m, int32_t variant) {
     if (!m) return pwmgpu::fail(PWMGPU_ERR_INVALID, "null handle");
     if (variant < 0 || variant >= pwmgpu::kCsbVariants) return pwmgpu::fail(PWMGPU_ERR_INVALID, "CSB variant 0..3");
-    if (m->format != PWMGPU_FMT_CSB) return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB handle");
+    if (m->format != PWMGPU_FMT_CSB && m->format != PWMGPU_FMT_COH)
+        return pwmgpu::fail(PWMGPU_ERR_STATE, "not a CSB or CO-H handle");
     m->csb_var = variant;
     return PWMGPU_OK;
 }
