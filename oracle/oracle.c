@@ -309,6 +309,35 @@ void orc_merge_mv(int32_t nor, int32_t nnz, const int32_t* row_start, const int3
     free(coords); free(carry_row); free(carry_val);
 }
 
+void orc_merge_omp_mv(int32_t nor, int32_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                      const double* data, const double* x, double* y, int32_t threads) {
+    /* CRS_Merge.hpp:95-141 as the reference runs it: one merge-path
+     * partition per OpenMP thread (schedule(static), :101), then the serial
+     * carry fix-up (:136-140).  Same arithmetic as orc_merge_mv. */
+    const int32_t* row_end = row_start + 1;
+    int32_t* coords = (int32_t*)malloc(sizeof(int32_t) * 2 * (threads + 1));
+    int32_t* carry_row = (int32_t*)malloc(sizeof(int32_t) * threads);
+    double* carry_val = (double*)malloc(sizeof(double) * threads);
+    orc_merge_partition(nor, nnz, row_start, threads, coords);
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (int32_t t = 0; t < threads; ++t) {
+        int32_t a = coords[2 * t], b = coords[2 * t + 1];
+        const int32_t a_end = coords[2 * t + 2], b_end = coords[2 * t + 3];
+        double running = 0.;
+        for (; a < a_end; ++a) {
+            for (; b < row_end[a]; ++b) running += data[b] * x[col_ind[b]];
+            y[a] = running;
+            running = 0.;
+        }
+        for (; b < b_end; ++b) running += data[b] * x[col_ind[b]];
+        carry_row[t] = a_end;
+        carry_val[t] = running;
+    }
+    for (int32_t t = 0; t < threads; ++t)
+        if (carry_row[t] < nor) y[carry_row[t]] += carry_val[t];
+    free(coords); free(carry_row); free(carry_val);
+}
+
 /* ------------------------------------------------------------------ */
 /* Vector utilities and the power method                                */
 /* ------------------------------------------------------------------ */

@@ -63,6 +63,11 @@ void orc_fill_poisson_rows(int32_t m, int32_t n, int32_t first_row, int32_t last
 void orc_power_rows(int32_t nor, int32_t parts, const int32_t* rs_all, const int32_t* ci, const double* d, double* x,
                     int32_t it);
 
+/* SOA_Implementations/CRS_Merge.hpp:95-141 with one merge-path partition per
+ * OpenMP thread, as the reference runs it (the CPU baseline's timing;
+ * orc_merge_mv is the same arithmetic, partitions in sequence). */
+void orc_merge_omp_mv(int32_t nor, int32_t nnz, const int32_t* row_start, const int32_t* col_ind,
+                      const double* data, const double* x, double* y, int32_t threads);
 /* Matrix/CRS.hpp:99-109 (sequential CRS::mv). */
 void orc_crs_mv(int32_t nor, const int32_t* row_start, const int32_t* col_ind, const double* data,
                 const double* x, double* y);

@@ -40,6 +40,7 @@ def lib():
                                        C.POINTER(C.c_int32)]
         L.orc_merge_partition.argtypes = [C.c_int32, C.c_int32, I32P, C.c_int32, I32P]
         L.orc_merge_mv.argtypes = [C.c_int32, C.c_int32, I32P, I32P, F64P, F64P, F64P, C.c_int32]
+        L.orc_merge_omp_mv.argtypes = [C.c_int32, C.c_int32, I32P, I32P, F64P, F64P, F64P, C.c_int32]
         L.orc_norm2.restype = C.c_double
         L.orc_norm2.argtypes = [F64P, C.c_int64]
         L.orc_normalize.argtypes = [F64P, C.c_int64]
@@ -205,6 +206,14 @@ def merge_mv(A, x, threads):
     y = np.zeros(A.nor, np.float64)
     lib().orc_merge_mv(A.nor, A.nnz, A.row_start, _nz(A.col_ind, np.int32), _nz(A.data),
                        np.ascontiguousarray(x, np.float64), y, threads)
+    return y
+
+
+def merge_omp_mv(A, x, threads):
+    """CRS_Merge::mv with one partition per OpenMP thread (timing path)."""
+    y = np.zeros(A.nor, np.float64)
+    lib().orc_merge_omp_mv(A.nor, A.nnz, A.row_start, _nz(A.col_ind, np.int32), _nz(A.data),
+                           np.ascontiguousarray(x, np.float64), y, threads)
     return y
 
 

@@ -128,3 +128,15 @@ def test_calc_stats_against_reference_outputs():
         names.add(name)
     assert names == set(ref)
     assert any(w["balanced"] == 0 for w in ref.values()) and any(w["balanced"] == 1 for w in ref.values())
+
+
+def test_merge_omp_matches_sequential_partitions():
+    """The OpenMP CRS_Merge restatement (the CPU baseline's timing path) gives
+    the sequential-partition restatement's bits, which the compiled reference
+    pins (ref_outputs.npz)."""
+    for mn in [(37, 29), (10, 5)]:
+        A = O.fill_poisson(*mn)
+        x = REF["poisson_%dx%d_x" % mn]
+        for T in (1, 3, 8, 31):
+            assert np.array_equal(O.merge_omp_mv(A, x, T), O.merge_mv(A, x, T))
+            assert np.array_equal(O.merge_omp_mv(A, x, T), REF["poisson_%dx%d_merge%d_mv" % (mn + (T,))])
