@@ -277,6 +277,43 @@ def autotune_report(pwm, torch, stream, load, load_same_class, x, y, B):
     return out
 
 
+def poisson512(pwm, torch, dev, stream):
+    """The 512 x 512-grid Poisson workload (N = 262,144, nnz = 1,308,672, the
+    reference's CPU-runnable case): 100 timed SpMVs after 10 warm-ups and a
+    100-iteration power method (reference powerIteration semantics).  Its
+    21 MB of matrix and vectors stay in the 129 MB L2 between SpMVs, so the
+    GB/s here are L2 figures, not HBM ones."""
+    M = pwm.CRSCuda(1)
+    M.set_stream(stream.cuda_stream)
+    M.generatePoissonMatrix(512, 512, 1)
+    N, _, nnz = M.dims()
+    B = algorithmic_bytes(N, nnz)
+    x = torch.rand(N, dtype=torch.float64, generator=torch.Generator().manual_seed(3)).to(dev)
+    y = torch.zeros_like(x)
+    for _ in range(10):
+        M.mv_device(x.data_ptr(), y.data_ptr())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(100):
+        M.mv_device(x.data_ptr(), y.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / 100
+    px = x.clone()
+    M.power_device(px.data_ptr(), y.data_ptr(), 10)
+    px.copy_(x)
+    e0.record(stream)
+    M.power_device(px.data_ptr(), y.data_ptr(), 100)
+    e1.record(stream)
+    e1.synchronize()
+    pms = e0.elapsed_time(e1)
+    return {"workload": "poisson2d_512x512_fp64", "N": N, "nnz": nnz, "spmv_ms": round(ms, 5),
+            "spmv_gb_s_l2_resident": round(B / (ms * 1e-3) / 1e9, 2),
+            "power_100_iterations_ms": round(pms, 4), "power_ms_per_iteration": round(pms / 100, 5),
+            "note": "21 MB of matrix and vectors: L2-resident between SpMVs"}
+
+
 def irregular_and_solves(pwm, torch, dev, stream, args):
     """The irregular lognormal-row matrix (N = 4,194,304, generated on the
     device): FP64 SpMV GB/s, then power solves to 1e-10 relative
@@ -460,14 +497,19 @@ def _check_set(specs, per_class=3, max_n=400000):
     return set(out)
 
 
-def _class_counts(specs, conv, iters, max_it):
-    """Per matrix class: requests, converged to the tolerance, and stopped at
-    the iteration cap."""
+def _class_counts(specs, conv, iters, max_it, low=None):
+    """Per matrix class: requests, converged to the tolerance, stopped at the
+    iteration cap, and (mixed precision) the share of steps run in FP32 /
+    BF16 -- the service's precision tuner's choice for the class."""
     out = {}
     for cls in ("poisson", "random"):
         idx = [i for i, (k, _) in enumerate(specs) if k == cls]
         out[cls] = {"requests": len(idx), "converged": int(sum(bool(conv[i]) for i in idx)),
                     "capped_at_max_it": int(sum((not conv[i]) and iters[i] >= max_it for i in idx))}
+        if low is not None:
+            steps = sum(iters[i] for i in idx)
+            out[cls]["low_precision_step_share"] = round(sum(low[i] for i in idx) / max(steps, 1), 4)
+            out[cls]["solves_kept_in_fp64"] = int(sum(low[i] == 0 for i in idx))
     return out
 
 
@@ -535,7 +577,8 @@ def serving(pwm, args):
                "steps_low_precision": int(sum(r.iterations_low for r in res)),
                "max_reported_residual_converged": max([r.residual for r in res if r.converged], default=None),
                "rounds": int(st.rounds), "gpu_round_ms": round(st.gpu_round_ms, 1),
-               "by_class": _class_counts(specs, conv, [r.iterations for r in res], max_it)}
+               "by_class": _class_counts(specs, conv, [r.iterations for r in res], max_it,
+                                         [r.iterations_low for r in res])}
         if not args.batch_only:
             rec["oracle_check"] = _oracle_checks([(specs[i][0], specs[i][1], res[i].lambda_, res[i].residual,
                                                    res[i].converged, vecs[i]) for i in sorted(check)])
@@ -880,6 +923,8 @@ def run_ours(args, world, rank, local):
     e2e_gbs = B * world / e2e_s / 1e9 if e2e_steps else None
 
     extra = None if args.no_extra else irregular_and_solves(pwm, torch, dev, stream, args)
+    if extra is not None:
+        extra["poisson512"] = poisson512(pwm, torch, dev, stream)
     if not args.no_serving and rank == 0:
         extra = dict(extra or {}, **serving(pwm, args))
 

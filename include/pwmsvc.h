@@ -10,9 +10,11 @@
  * sub-tiles form one list: the block-diagonal matrix of the live solves, cut
  * at the matrix boundaries), followed by a residual pass; with use_graph the
  * round is one CUDA graph.  Each solve keeps its matrix and iterates resident
- * in HBM until it retires.  Mixed precision runs the FP32 (BF16 values where
- * exact) phase as pwmgpu_solve does (to a residual of 2e-6, the FP32 floor,
- * or the FP64 reserve), then FP64.
+ * in HBM until it retires.  Mixed precision starts with one FP64 round
+ * (the precision tuner's probe): a matrix whose residual after it projects
+ * to tol within five rounds stays in FP64; the others run the FP32 (BF16
+ * values where exact) phase as pwmgpu_solve does (to a residual of 2e-6,
+ * the FP32 floor, or the FP64 reserve), then FP64.
  * Sums over a solve's rows run in a fixed order over its own sub-tiles, so a
  * solve gives the same bits alone and in any mix.
  *

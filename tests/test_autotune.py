@@ -217,3 +217,39 @@ def test_csb_handle_picks_variant_at_load(pwm, poisson):
     M.set_csb_variant(3)
     assert M.csb_variant() == 3
     _check_mv(M, poisson, 42)
+
+
+@pytest.mark.gpu
+def test_service_precision_tuner_per_matrix_class():
+    """The service's precision tuner: a mixed request runs one FP64 probe
+    round, then keeps matrices that would finish within a few rounds in FP64
+    (the random Poisson(8)-row class of the batch workload) and moves slowly
+    converging ones (Poisson grids) to the FP32 / BF16 bulk phase.  Every
+    result is confirmed by the oracle; the same requests in FP64 take the
+    same number of steps where the tuner kept FP64."""
+    from oracle import pyoracle as O
+    from thesis_spmv_gb300 import service as S
+    import thesis_spmv_gb300 as t
+    rand = [dict(n=n, seed=1000 + i, length_dist=1, mean_len=8.0, sigma=0.0, max_len=64, band_permille=0,
+                 band_half=0) for i, n in enumerate((3000, 40000, 200000))]
+    grids = [(40, 40), (96, 64)]
+    out = {}
+    for prec in (t.PREC_MIXED, t.PREC_F64):
+        svc = S.Service(round_iterations=8)
+        ids = [svc.submit_random(max_it=2000, tol=1e-10, precision=prec, x0_seed=11, keep_vector=True, **kw)
+               for kw in rand]
+        ids += [svc.submit_poisson(m, n, max_it=2000, tol=1e-10, precision=prec, x0_seed=11, keep_vector=True)
+                for m, n in grids]
+        svc.run_until_idle()
+        out[prec] = [svc.result(i, want_vector=True) for i in ids]
+        svc.close()
+    for j, kw in enumerate(rand):
+        (rm, um), (r64, _) = out[t.PREC_MIXED][j], out[t.PREC_F64][j]
+        assert rm.converged and rm.iterations_low == 0 and rm.iterations == r64.iterations
+        lam, res = O.rayleigh(O.random_crs(kw["n"], kw["seed"], 1, 8.0, 0.0, 64, 0, 0), um)
+        assert res <= 2e-10 and abs(lam - rm.lambda_) <= 1e-10 * abs(lam)
+    for j, (m, n) in enumerate(grids):
+        rm, um = out[t.PREC_MIXED][len(rand) + j]
+        assert rm.iterations_low > 0
+        lam, res = O.rayleigh(O.fill_poisson(m, n), um)
+        assert abs(lam - rm.lambda_) <= 1e-10 * abs(lam) and abs(res - rm.residual) <= 1e-12

@@ -306,9 +306,45 @@ __global__ void __launch_bounds__(NT, kCsbThreadsPerSM / NT) k_csb_spmv(const ui
             const int b = (u - u0) & 1;
             __syncthreads();  // buffer b^1 is free (its unit is done), ys zeroed
             if (u + 1 < u1) stage(u + 1, b ^ 1);
+            const int4 un = __ldg(units + u);
+            if (un.w == 2) {
+                // one element per row: element lo + i to lane i % 32 of warp
+                // (i / 32) % W, so a warp's loads, x-window reads and y-window
+                // updates are 32 consecutive rows (no bank conflicts), four
+                // elements per lane in flight (the first four while the x
+                // window lands); one FMA per element from the row's y-window
+                // value
+                uint32_t id[4];
+                double v[4];
+                int base = un.x + warp * 128;
+                auto load4 = [&](int bs) {
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int k = bs + 32 * t + lane;
+                        id[t] = k < un.y ? __ldg(ind + k) : 0u;
+                        v[t] = k < un.y ? __ldg(data + k) : 0.0;
+                    }
+                };
+                load4(base);
+                ok = mbar_wait_bounded(&bar[b], uses[b] & 1u, status);
+                uses[b]++;
+                if (!__syncthreads_and(ok)) break;
+                const double* xw = xs[b];
+                while (base < un.y) {
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        if (base + 32 * t + lane < un.y) {
+                            const int r = (int)(id[t] >> 16) & (S - 1);
+                            ys[r] = fma(v[t], xw[id[t] & (uint32_t)(S - 1)], ys[r]);
+                        }
+                    }
+                    base += (NT / 32) * 128;
+                    if (base < un.y) load4(base);
+                }
+                continue;
+            }
             // row-major unit: warp chunks of kChunk elements; the first
             // chunk's loads are in flight while the x window lands
-            const int4 un = __ldg(units + u);
             constexpr int kChunk = 32 * K;
             constexpr int kStep = (NT / 32) * kChunk;
             int k = un.x + warp * kChunk;
@@ -432,9 +468,10 @@ int csb_build_host(int nor, int noc, long long nnz, const int32_t* row_start, co
 // kcol (x is gathered from global memory there); then its dense units, each
 // row-major (a stable sort by ind = local row << 16 | local column).  Every
 // unit starts on a multiple of 4 elements; the gaps hold zeros and are never
-// read as elements.  win_ptr and units (4 ints per unit: {lo, hi, c0, 0},
-// c0 = -1 for a flat unit) are rewritten: a window has at most one unit
-// before its first dense unit.  Windows are independent: filled by a few
+// read as elements.  win_ptr and units (4 ints per unit: {lo, hi, c0, kind},
+// c0 = -1 for a flat unit; kind 2 for a dense unit whose rows hold one
+// element each, else 0) are rewritten: a window has at most one unit before
+// its first dense unit.  Windows are independent: filled by a few
 // host threads.  Returns false when the copy would not fit 32-bit element
 // offsets.
 bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<double>& data, int S,
@@ -495,12 +532,17 @@ bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<doubl
                 }
             }
             std::sort(key.begin(), key.end());  // position last: stable by construction
+            bool one_per_row = !flat;
             for (size_t q = 0; q < key.size(); ++q) {
                 const long long k = std::get<2>(key[q]);
                 kind[(size_t)dst + q] = ind[(size_t)k];
                 kdata[(size_t)dst + q] = data[(size_t)k];
                 if (flat) kcol[(size_t)dst + q] = (int32_t)std::get<1>(key[q]);
+                if (q > 0 && ((std::get<0>(key[q]) ^ std::get<0>(key[q - 1])) >> 16) == 0) one_per_row = false;
             }
+            // a dense unit whose rows hold one element each (a stencil's
+            // off-diagonal tiles): the kernel's element-per-lane path
+            if (one_per_row) new_units[4 * (size_t)v + 3] = 2;
         }
     };
     const int nt = std::max(1, std::min<int>(nnew / 64 + 1, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));

@@ -38,6 +38,18 @@ constexpr int kSides = kNumCls - 1;  // forked streams of a round (the F64 class
 // pwmgpu_solve).
 constexpr double kSvcSwitchRel = 2e-6;
 
+// Precision tuner of the mixed solves: a MIXED request runs its first round
+// in FP64 (the probe); from the residual r after those C steps it projects
+// the steps to tol at that rate, C ln(tol) / ln(r).  A matrix that would
+// finish within kProbeRounds rounds stays in FP64 -- a low-precision phase
+// there costs a phase switch and an extra round for the few steps it would
+// cheapen (the service's 128 random Poisson(8)-row matrices: 696 mixed vs
+// 861 FP64 solves/s with the phase, the batch-wide figure without the probe);
+// slower ones take the FP32 / BF16 bulk phase from the probe's iterate on.
+// The choice depends only on the solve's own residual, so a solve gives the
+// same bits alone and in any mix.
+constexpr int kProbeRounds = 5;
+
 struct Req {
     int64_t id = 0;
     pwmsvc_request spec{};
@@ -51,6 +63,8 @@ struct Req {
     int n = 0;
     int cls = kClsF64;
     bool low = false;
+    bool probe = false;  // MIXED: the first round runs in FP64 (the precision tuner's probe)
+    int low_cls = kClsF64;
     int slot = -1;
     const void* valp_low = nullptr;
     int iterations = 0, iterations_low = 0, rounds_in_phase = 0, converged = 0;
@@ -152,6 +166,25 @@ struct pwmsvc {
 
 namespace {
 
+// The FP32 / BF16 copies of a request's matrix (values, SELL-32 slices where
+// the matrix fits them) and vectors, made on its own stream when its solve
+// enters the low-precision phase.
+int prepare_low(Req* r) {
+    pwmgpu_matrix* m = r->m;
+    const pwmsvc_request& q = r->spec;
+    int cfg = kCfgF32, pg = 0;
+    TRY(ensure_low_values(m, q.precision == PWMGPU_PREC_MIXED, &cfg, &r->valp_low, &pg));
+    TRY(ensure_fvectors(m));
+    if (sell_for(m, cfg)) {
+        r->valp_low = cfg == kCfgBF16 ? m->sell.valbf : (const void*)m->sell.val32;
+        r->low_cls = cfg == kCfgBF16 ? kClsBF16Sell : kClsF32Sell;
+    } else {
+        r->low_cls = cfg == kCfgBF16 ? kClsBF16 : kClsF32;
+    }
+    CU(cudaStreamSynchronize(m->stream));
+    return PWMGPU_OK;
+}
+
 // Build the request's matrix and start vector on its own stream.
 int admit(pwmsvc* S, Req* r) {
     const pwmsvc_request& q = r->spec;
@@ -187,19 +220,16 @@ int admit(pwmsvc* S, Req* r) {
     } else {
         CU(launch_fill_uniform(m->dx, r->n, q.x0_seed, m->sm_count, m->stream));
     }
-    r->low = q.precision != PWMGPU_PREC_F64;
     r->cls = kClsF64;
-    if (r->low) {
-        int cfg = kCfgF32, pg = 0;
-        TRY(ensure_low_values(m, q.precision == PWMGPU_PREC_MIXED, &cfg, &r->valp_low, &pg));
-        TRY(ensure_fvectors(m));
+    r->low = false;
+    // MIXED: the probe round first, the low-precision copies only if the
+    // solve takes the low phase
+    r->probe = q.precision == PWMGPU_PREC_MIXED;
+    if (q.precision == PWMGPU_PREC_F32) {  // FP32 throughout: the low phase from the start
+        TRY(prepare_low(r));
         CU(launch_convert_f64_f32(m->dx, m->fx, r->n, m->sm_count, m->stream));
-        if (sell_for(m, cfg)) {
-            r->valp_low = cfg == kCfgBF16 ? m->sell.valbf : (const void*)m->sell.val32;
-            r->cls = cfg == kCfgBF16 ? kClsBF16Sell : kClsF32Sell;
-        } else {
-            r->cls = cfg == kCfgBF16 ? kClsBF16 : kClsF32;
-        }
+        r->low = true;
+        r->cls = r->low_cls;
     }
     CU(cudaStreamSynchronize(m->stream));
     r->bytes = solve_bytes(m->M.nor, m->M.nnz, q.precision);
@@ -384,6 +414,33 @@ int after_round(pwmsvc* S, int* finished) {
         }
         r->lambda = st.lambda;
         r->rel = std::sqrt(st.res2 / nsq) / std::fabs(st.lambda);
+        if (r->probe) {
+            r->probe = false;
+            // projected steps to tol at this round's rate (r starts near 1)
+            const bool fast = r->rel <= q.tol ||
+                              (r->rel < 1.0 && q.tol > 0.0 &&
+                               C * std::log(q.tol) / std::log(r->rel) <= (double)(kProbeRounds * C));
+            const int reserve = std::max(2, std::min(64, q.max_it / 4));
+            if (!fast && r->iterations < q.max_it - reserve) {
+                // the bulk in FP32 / BF16 from the newest FP64 iterate on,
+                // normalised first (an FP64 iterate may lie outside FP32's range)
+                TRY(prepare_low(r));
+                pwmgpu_matrix* m = r->m;
+                double* newest = (st.k & 1) ? m->dy : m->dx;
+                CU(launch_power_finalize_f64(newest, &S->d_states[r->slot].nsq, nullptr, nullptr, r->n, m->sm_count,
+                                             S->stream));
+                CU(launch_convert_f64_f32(newest, m->fx, r->n, m->sm_count, S->stream));
+                TRY(reset_state(S, r->slot));
+                r->exact_set = false;
+                r->low = true;
+                r->cls = r->low_cls;
+                r->rounds_in_phase = 0;
+                r->prev_rel = r->rel;
+                S->dirty = true;
+                keep.push_back(r);
+                continue;
+            }
+        }
         bool done = false;
         if (!r->low || q.precision == PWMGPU_PREC_F32) {
             if (r->rel <= q.tol) {
