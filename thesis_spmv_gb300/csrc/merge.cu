@@ -197,11 +197,6 @@ __device__ __forceinline__ int step_exponent(const unsigned int* mx_in, const do
     return nsq_in ? pow2_rescale_exponent(*nsq_in, rescale_window<XT>()) : 0;
 }
 
-// Fold a warp's magnitude keys into the global max (one atomic per warp).
-__device__ __forceinline__ void warp_max_out(unsigned mx, unsigned int* out) {
-    mx = __reduce_max_sync(0xffffffffu, mx);
-    if ((threadIdx.x & 31) == 0 && mx != 0u) atomicMax(out, mx);
-}
 
 constexpr int kMliStages = 2;
 
@@ -563,7 +558,28 @@ struct PowerArgs {
     // mxk[k]: largest magnitude key of v_k, zeroed (or null: every iteration
     // sums ||v||^2).  Iterations before the last two store only the keys.
     unsigned int* mxk;
+    // The plan's fix-up runs (null: the fix-up pass searches the sub-tiles).
+    const int4* runs;
+    int nruns;
 };
+
+// The fix-up pass over the plan's run list: thread t0, t0 + stride, ... adds
+// run k's carries to its row -- the sums of fixup_pass in the same order
+// (k_fix_runs' loop, for the persistent kernel).
+template <int MODE, typename XT, typename AT, bool NORM>
+__device__ __forceinline__ void fix_runs_pass(const int4* __restrict__ runs, int nruns, XT* __restrict__ y,
+                                              const AT* __restrict__ carries, int e, int t0, int stride, double& ss,
+                                              unsigned* mx) {
+    for (int k = t0; k < nruns; k += stride) {
+        const int4 d = __ldg(runs + k);
+        AT sum = __ldcg(carries + d.x);
+        for (int j = d.x + 1; j < d.y; ++j) sum += __ldcg(carries + j);
+        const XT v = (XT)((AT)__ldcg(y + d.z) + (e != 0 ? scale_pow2(sum, e) : sum));
+        y[d.z] = v;
+        if (NORM) ss = fma((double)v, (double)v, ss);
+        if (MODE == MODE_SCALE) *mx = max(*mx, mag_key(v));
+    }
+}
 
 // Sum two per-CTA partials over the grid in a fixed order (every CTA gets the
 // same totals); call after a grid barrier.
@@ -631,8 +647,11 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
                                                                   cval + 32 * w, hval + 32 * w, ticket, e, pol,
                                                                   no_ss, mx);
             if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
-            fixup_pass<MODE_SCALE, XT, AT, false>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
-                                                  nthr, no_ss, &mx);
+            if (p.runs)
+                fix_runs_pass<MODE_SCALE, XT, AT, false>(p.runs, p.nruns, out, a.carries, e, tid, nthr, no_ss, &mx);
+            else
+                fixup_pass<MODE_SCALE, XT, AT, false>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid,
+                                                      a.nsub, nthr, no_ss, &mx);
             warp_max_out(mx, p.mxk + k + 1);
             if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
             prev_keys = true;
@@ -646,8 +665,11 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
         warp_pass<MODE_POWER, VT, XT, AT, NT, IPT, true, C16>(a, in, out, stages, bars[w], crow + 32 * w,
                                                               cval + 32 * w, hval + 32 * w, ticket, e, pol, ss, mx);
         if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
-        fixup_pass<MODE_POWER, XT, AT, true>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
-                                             nthr, ss);
+        if (p.runs)
+            fix_runs_pass<MODE_POWER, XT, AT, true>(p.runs, p.nruns, out, a.carries, e, tid, nthr, ss, &mx);
+        else
+            fixup_pass<MODE_POWER, XT, AT, true>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid, a.nsub,
+                                                 nthr, ss);
         if (want_dot) {
             // the Rayleigh dot needs v_k: a row pass for both sums
             if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
@@ -981,7 +1003,8 @@ struct MergeKernels {
         power_occ(v);
         PowerArgs<VT, XT, AT> p{{M.row_start, P.colp, (const VT*)valp, P.rec, P.masks, M.nor, P.nsub, nullptr,
                                  nullptr, (AT*)carries, nullptr, status, 0, P.colp16},
-                                P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier, wait, mxk};
+                                P.subc, (XT*)X, (XT*)Y, k0, nk, nsq, result, partials, barrier, wait, mxk,
+                                P.runs, P.nruns};
         cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned int), st);
         if (e != cudaSuccess) return e;
         void* args[] = {&p};

@@ -173,6 +173,13 @@ __device__ __forceinline__ void load_lane(const T* p, int qm, int cnt, int lane,
     }
 }
 
+// Fold a warp's magnitude keys into a max in global memory (one atomic per
+// warp; call with the whole warp).
+__device__ __forceinline__ void warp_max_out(unsigned mx, unsigned int* out) {
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0 && mx != 0u) atomicMax(out, mx);
+}
+
 // MODE_SPMV: y = A x.  MODE_POWER: y = 2^e A x with ||y||^2 summed (the power
 // method's steps whose norm is used).  MODE_SCALE: y = 2^e A x tracking only
 // the largest |y_i| (magnitude keys, integer max) -- the power method's
