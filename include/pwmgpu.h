@@ -367,8 +367,13 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
  * (tuned_ms[2], ms per SpMV; 0 when the matrix was too small to tune). */
 int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* grid, int32_t* power_grid,
                          float* tuned_ms);
-/* Override the tuner's choice (prefer_l1 0 or 1) for later launches. */
-int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1);
+/* The merge kernels' full launch variant: bit 0 = the smaller shared-memory
+ * carveout, bit 1 = 16-bit columns, bit 2 = x gathers that bypass L1. */
+int pwmgpu_launch_variant(const pwmgpu_matrix* m, int32_t* variant);
+/* Override the tuner's choice for later launches: 0 or 1 (carveout), 4 or 5
+ * (the same with x gathers that bypass L1, on FP64 iterations).  16-bit
+ * columns are used wherever the plan has them. */
+int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t variant);
 /* Bytes per column index the merge kernels stream: 2 when every merge
  * sub-tile's columns span less than 2^16 (banded and stencil matrices: the
  * plan then keeps 16-bit offsets from a per-sub-tile base), else 4; and

@@ -247,10 +247,11 @@ def test_power_extreme_scales(pwm, scale, mode):
 
 @pytest.mark.parametrize("kind", ["poisson", "random"])
 def test_launch_tuner_variants_same_bits(pwm, kind):
-    """The load-time tuner times both launch variants of the merge kernels on
-    a matrix large enough to tune; both give the same SpMV bits (a sub-tile is
-    computed the same whichever warp takes it); the power method's norms are
-    summed in grid-dependent order, so its iterates agree to rounding."""
+    """The load-time tuner times the launch variants of the merge kernels on
+    a matrix large enough to tune; all give the same SpMV bits (a sub-tile is
+    computed the same whichever warp takes it and whichever cache path its x
+    gathers take); the power method's norms are summed in grid-dependent
+    order, so its iterates agree to rounding."""
     M = pwm.CRSCuda(1)
     if kind == "poisson":
         M.generatePoissonMatrix(2048, 2048, 1)
@@ -258,22 +259,28 @@ def test_launch_tuner_variants_same_bits(pwm, kind):
         M.generateRandom(1_500_000, 77, mean_len=16.0)
     l1, grid, pgrid, ms = M.launch_config()
     assert ms[0] > 0 and ms[1] > 0 and l1 in (0, 1) and grid > 0 and pgrid > 0
+    assert M.launch_variant() in range(8)
     n = M.dims()[0]
     x = np.random.default_rng(2).uniform(-1, 1, n)
-    ys = []
-    for v in (0, 1):
+    ys, ps = [], []
+    for v in (0, 1, 4, 5):
         M.set_launch_variant(v)
+        assert M.launch_variant() & ~2 == v
         y = np.zeros(n)
         M.mv(x, y)
         ys.append(y)
         xp, yp = x.copy(), np.zeros(n)
         M.powerIteration(xp, yp, 3)
-        ys.append(yp)
-    assert np.array_equal(ys[0], ys[2])
-    np.testing.assert_allclose(ys[1], ys[3], rtol=1e-13, atol=1e-15)
+        ps.append(yp)
+    for y in ys[1:]:
+        assert np.array_equal(ys[0], y)
+    for p in ps[1:]:
+        np.testing.assert_allclose(ps[0], p, rtol=1e-13, atol=1e-15)
     rs, ci, d = M.getCSR()
     A = O.CRSArrays(n, n, rs, ci, d)
     assert np.all(np.abs(ys[0] - O.crs_mv(A, x)) <= O.row_error_bound(A, x))
+    with pytest.raises(RuntimeError):
+        M.set_launch_variant(2)
 
 
 @pytest.mark.parametrize("offset", [0, 1])

@@ -102,6 +102,7 @@ SIGNATURES = {
     "pwmgpu_csb_params": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
     "pwmgpu_launch_config": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]),
     "pwmgpu_set_launch_variant": (C.c_int, [vp, i32]),
+    "pwmgpu_launch_variant": (C.c_int, [vp, C.POINTER(i32)]),
     "pwmgpu_plan_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32)]),
     "pwmgpu_csb_build_host": (C.c_int, [i32, i32, i64, vp, vp, vp, vp, vp, vp]),
     "pwmgpu_coh_build_host": (C.c_int, [i32, i32, i64, vp, vp, vp, i32, C.POINTER(i32), C.POINTER(i64),

@@ -10,7 +10,12 @@
 //   k_batch_norm    ||v_{k+1}||^2 (and v_k . v_{k+1} on a round's last step)
 //                   per slot, over fixed row chunks in a fixed order; the
 //                   slot's last CTA advances the slot state (k, ||v||^2)
-// and once per round
+// except on a round's steps before its last two ("key steps"), whose norms
+// only choose the next exact rescale: there the SpMV and the fix-up fold the
+// largest magnitude key of the rows they store into the slot (one atomic max
+// per warp and slot; integer work only) and k_batch_keys advances the state;
+// the iterates differ from the norm schedule by powers of two only, which the
+// final normalisation removes bit for bit.  Once per round
 //   k_batch_resid   lambda and ||A u - lambda u||^2 of u = v_{k-1}/||v_{k-1}||.
 // The SpMV keeps one FP64 FMA per nonzero and no other FP64 work (GB300's
 // FP64 pipe is 2 operations per clock per SM); the sums are row passes.
@@ -53,10 +58,19 @@ struct SlotRegs {
     const void* X;
     const void* Y;
     void* carries;
-    int nor, tile0, k;
-    double nsq;
+    unsigned int* mx_next;
+    int nor, tile0, k, e;
 };
 
+// Exponent of the exact 2^e rescale of step k -> k+1: from the largest key of
+// v_k after a key step, else from ||v_k||^2; none on the first step.
+template <typename XT>
+__device__ __forceinline__ int slot_exponent(const SlotState* st) {
+    if (st->k <= 0) return 0;
+    return st->keyed ? pow2_rescale_exponent_key<XT>(st->mx) : pow2_rescale_exponent(st->nsq, rescale_window<XT>());
+}
+
+template <typename XT>
 __device__ __forceinline__ void load_slot(const BatchTable& T, int j, SlotRegs& r) {
     const BatchSlot* d = T.slots + j;
     r.row_start = d->row_start;
@@ -65,9 +79,10 @@ __device__ __forceinline__ void load_slot(const BatchTable& T, int j, SlotRegs& 
     r.carries = d->carries;
     r.nor = d->nor;
     r.tile0 = d->tile0;
-    const SlotState* st = T.states + d->state;
+    SlotState* st = T.states + d->state;
     r.k = st->k;
-    r.nsq = st->nsq;
+    r.e = slot_exponent<XT>(st);
+    r.mx_next = &st->mx_next;
 }
 
 // Lane 0: the TMA copies of global sub-tile g (slot j, its record r1).
@@ -93,7 +108,9 @@ constexpr int batch_min_ctas() {
     return sizeof(VT) == 8 ? 5 : 8;
 }
 
-template <typename VT, typename XT, typename AT, int NT, int IPT>
+// KEYS: a key step (the largest magnitude key of the stored rows into the
+// slot's mx_next, one atomic max per warp and slot), else the rows only.
+template <typename VT, typename XT, typename AT, int NT, int IPT, bool KEYS = false>
 __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const BatchTable* __restrict__ Tp) {
     using S = WarpStage<VT, IPT>;
     constexpr int W = NT / 32;
@@ -129,6 +146,7 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
     int jc = __ldg(T.tile_slot + gw);
     int jcur = -1;  // slot whose fields are in `cur` (consecutive sub-tiles of a warp often share it)
     SlotRegs cur;
+    unsigned mx = 0u;  // KEYS: largest key of the rows stored for slot jcur
     int i = 0;
     for (; i < n; ++i) {
         const int k = i % NS;
@@ -137,13 +155,17 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
         // the slot's fields (when the slot changes) and the next sub-tile's
         // slot: loads in flight during the wait
         if (jc != jcur) {
-            load_slot(T, jc, cur);
+            if (KEYS && jcur >= 0) {
+                warp_max_out(mx, cur.mx_next);
+                mx = 0u;
+            }
+            load_slot<XT>(T, jc, cur);
             jcur = jc;
         }
         const int jn = i + 1 < n ? __ldg(T.tile_slot + g + tw) : 0;
         const bool ok = mbar_wait_bounded(&bars[w][k], (uint32_t)(i / NS) & 1u, T.status);
         if (!__all_sync(0xffffffffu, ok)) break;
-        const int e = cur.k > 0 ? pow2_rescale_exponent(cur.nsq, rescale_window<XT>()) : 0;
+        const int e = cur.e;
         const XT* in = static_cast<const XT*>((cur.k & 1) ? cur.Y : cur.X);
         XT* out = const_cast<XT*>(static_cast<const XT*>((cur.k & 1) ? cur.X : cur.Y));
         const int s = g - cur.tile0;
@@ -152,12 +174,13 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
         gather_subtile<VT, XT, AT, IPT>(st, in, xv);
         const bool general = reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral;
         double no_ss = 0.0;
+        constexpr int MODE = KEYS ? MODE_SCALE : MODE_POWER;
         if (general)
-            finish_subtile<MODE_POWER, true, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
-                                                              cval, hval, no_ss);
+            finish_subtile<MODE, true, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow, cval,
+                                                        hval, no_ss, &mx);
         else
-            finish_subtile<MODE_POWER, false, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow,
-                                                               cval, hval, no_ss);
+            finish_subtile<MODE, false, VT, XT, AT, IPT>(s, st, xv, cur.row_start, out, car, cur.nor, e, crow, cval,
+                                                         hval, no_ss, &mx);
         if (lane == 0) {
             if (i + NS < n) {
                 fence_proxy_async();
@@ -168,6 +191,7 @@ __global__ void __launch_bounds__(NT, batch_min_ctas<VT>()) k_batch_spmv(const B
         __syncwarp();
         jc = jn;
     }
+    if (KEYS && jcur >= 0) warp_max_out(mx, cur.mx_next);
     if (i < n) {  // timed out: let this warp's copies in flight land first
         if (lane == 0)
             for (int t = i; t < n && t < i + NS; ++t)
@@ -184,26 +208,34 @@ struct SellSlotRegs {
     const void* valp;
     const float* in;
     float* out;
+    unsigned int* mx_next;
     int nor, tile0, e;
 };
 
 __device__ __forceinline__ void load_sell_slot(const BatchTable& T, int j, SellSlotRegs& r) {
     const BatchSlot* d = T.slots + j;
-    const SlotState* st = T.states + d->state;
+    SlotState* st = T.states + d->state;
     const int k = st->k;
     r.soff = d->soff;
     r.col16 = d->col16;
     r.valp = d->valp;
     r.in = static_cast<const float*>((k & 1) ? d->Y : d->X);
     r.out = static_cast<float*>((k & 1) ? d->X : d->Y);
+    r.mx_next = &st->mx_next;
     r.nor = d->nor;
     r.tile0 = d->tile0;
-    r.e = k > 0 ? pow2_rescale_exponent(st->nsq, rescale_window<float>()) : 0;
+    r.e = slot_exponent<float>(st);
 }
 
+// What a SELL step sums besides the rows: nothing (a round's last step, whose
+// row pass follows), the squares per slice group (the step before it), or the
+// largest magnitude key per slot (the round's earlier steps).
+enum SellSum { kSellNone = 0, kSellSquares = 1, kSellKeys = 2 };
+
 // One power step of every live solve of a SELL-32 class: v_{k+1} =
-// 2^{e_k} A_j v_k, one lane per row; with NORM also the sums of squares of
-// ||v_{k+1}||^2 per slice group.  A slot's slices form groups of kSellGroup,
+// 2^{e_k} A_j v_k, one lane per row; with kSellSquares also the sums of
+// squares of ||v_{k+1}||^2 per slice group (with kSellKeys the slot's largest
+// magnitude key instead: one atomic max per warp and slot).  A slot's slices form groups of kSellGroup,
 // in the slot's own slice order; warp w takes the consecutive global groups
 // [w K, w K + K) (K = groups / warps, rounded up), two slices at a time, so
 // its slot advances by a comparison.  Per group the lanes' FP64 sums of
@@ -211,8 +243,10 @@ __device__ __forceinline__ void load_sell_slot(const BatchTable& T, int j, SellS
 // land in grp_part; k_batch_grp then sums a slot's groups in order.  Rows
 // are one lane's sums in CRS order and the grouping depends only on the
 // slot: the same bits in any mix.
-template <typename VT, bool NORM>
+template <typename VT, int SUM>
 __global__ void __launch_bounds__(256, sizeof(VT) == 2 ? 4 : 3) k_batch_sell(const BatchTable* __restrict__ Tp) {
+    constexpr bool NORM = SUM == kSellSquares;
+    constexpr bool KEYS = SUM == kSellKeys;
     const BatchTable T = *Tp;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, tw = (gridDim.x * blockDim.x) >> 5;
@@ -224,8 +258,13 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 2 ? 4 : 3) k_batch_sell(con
     SellSlotRegs A;
     load_sell_slot(T, j, A);
     int fix0 = __ldg(&T.slots[j].fix0), nfix = __ldg(&T.slots[j].nfix), nsub = __ldg(&T.slots[j].nsub);
+    unsigned mx = 0u;  // KEYS: largest key of the rows stored for slot j
     for (; q < q1; ++q) {
         while (q >= fix0 + nfix) {  // the next slot (slots own consecutive groups)
+            if (KEYS) {
+                warp_max_out(mx, A.mx_next);
+                mx = 0u;
+            }
             ++j;
             load_sell_slot(T, j, A);
             fix0 = __ldg(&T.slots[j].fix0);
@@ -255,6 +294,7 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 2 ? 4 : 3) k_batch_sell(con
                     const double wo = __any_sync(0xffffffffu, widen_special(out)) ? (double)out : widen_normal(out);
                     ss = fma(wo, wo, ss);
                 }
+                if (KEYS) mx = max(mx, mag_key(out));
             }
         }
         if (NORM) {
@@ -262,6 +302,7 @@ __global__ void __launch_bounds__(256, sizeof(VT) == 2 ? 4 : 3) k_batch_sell(con
             if (lane == 0) T.grp_part[q] = ss;
         }
     }
+    if (KEYS) warp_max_out(mx, A.mx_next);
 }
 
 // After a NORM step: per slot (one warp each) ||v_{k+1}||^2 = its groups'
@@ -279,8 +320,22 @@ __global__ void __launch_bounds__(256) k_batch_grp(const BatchTable* __restrict_
             SlotState* stt = T.states + d.state;
             stt->nsq_prev = stt->nsq;
             stt->nsq = s0;
+            stt->keyed = 0;
             stt->k = stt->k + 1;
         }
+    }
+}
+
+// After a key step: per slot, the step's largest key becomes v_{k+1}'s and
+// the state advances (||v||^2 is not known for v_{k+1}).
+__global__ void __launch_bounds__(256) k_batch_keys(const BatchTable* __restrict__ Tp) {
+    const BatchTable T = *Tp;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < T.nslots; j += gridDim.x * blockDim.x) {
+        SlotState* stt = T.states + T.slots[j].state;
+        stt->mx = stt->mx_next;
+        stt->mx_next = 0u;
+        stt->keyed = 1;
+        stt->k = stt->k + 1;
     }
 }
 
@@ -293,22 +348,25 @@ __global__ void k_tile_slots(const BatchTable* __restrict__ Tp) {
     }
 }
 
-template <typename XT, typename AT>
+// KEYS: a key step (the fixed rows' largest key into the slot's mx_next).
+template <typename XT, typename AT, bool KEYS = false>
 __global__ void __launch_bounds__(256) k_batch_fixup(const BatchTable* __restrict__ Tp) {
     const BatchTable T = *Tp;
     for (int c = blockIdx.x; c < T.nfix; c += gridDim.x) {
         const int j = find_slot<1>(T.slots, T.nslots, c);
         const BatchSlot& d = T.slots[j];
-        const SlotState* stt = T.states + d.state;
+        SlotState* stt = T.states + d.state;
         const int kit = stt->k;
-        const int e = kit > 0 ? pow2_rescale_exponent(stt->nsq, rescale_window<XT>()) : 0;
+        const int e = slot_exponent<XT>(stt);
         XT* out = static_cast<XT*>((kit & 1) ? d.X : d.Y);
         const int lo = (c - d.fix0) * kFixTiles;
         const int hi = min(d.nsub, lo + kFixTiles);
         const AT* car = static_cast<const AT*>(d.carries);
         double no_ss = 0.0;
-        fixup_pass<MODE_POWER, XT, AT>(d.row_start, d.subc, d.nor, d.nsub, out, car, e, lo + threadIdx.x, hi,
-                                       blockDim.x, no_ss);
+        unsigned mx = 0u;
+        fixup_pass<KEYS ? MODE_SCALE : MODE_POWER, XT, AT>(d.row_start, d.subc, d.nor, d.nsub, out, car, e,
+                                                           lo + threadIdx.x, hi, blockDim.x, no_ss, &mx);
+        if (KEYS) warp_max_out(mx, &stt->mx_next);
     }
 }
 
@@ -419,6 +477,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_norm(const BatchTable* __restr
                 stt->nsq_prev = stt->nsq;
                 stt->nsq = s0;
                 if (want_dot) stt->dot = s1;
+                stt->keyed = 0;
                 stt->k = kit + 1;
                 stt->norm_count = 0u;
             }
@@ -505,10 +564,11 @@ __global__ void k_fill_uniform(double* __restrict__ x, int n, uint64_t seed) {
 template <typename VT, typename XT, typename AT>
 struct BatchKernels {
     static constexpr int SMEM = (kBatchNT / 32) * kBatchStages * WarpStage<VT, kMliIpt>::BYTES;
+    template <bool KEYS>
     static int grid(int sm_count) {
         static int occ = -1;
         if (occ < 0) {
-            auto k = k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt>;
+            auto k = k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt, KEYS>;
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
             int o = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, kBatchNT, SMEM);
@@ -516,8 +576,17 @@ struct BatchKernels {
         }
         return occ * sm_count;
     }
-    static cudaError_t step(const BatchTable* T, int want_dot, int sm_count, cudaStream_t st) {
-        k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid(sm_count), kBatchNT, SMEM, st>>>(T);
+    // keys: a key step (SpMV and fix-up fold the largest key, k_batch_keys
+    // advances the state); else the norm row pass (with v_k . v_{k+1} when
+    // want_dot).
+    static cudaError_t step(const BatchTable* T, int want_dot, bool keys, int sm_count, cudaStream_t st) {
+        if (keys) {
+            k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt, true><<<grid<true>(sm_count), kBatchNT, SMEM, st>>>(T);
+            k_batch_fixup<XT, AT, true><<<8 * sm_count, 256, 0, st>>>(T);
+            k_batch_keys<<<sm_count, 256, 0, st>>>(T);
+            return cudaGetLastError();
+        }
+        k_batch_spmv<VT, XT, AT, kBatchNT, kMliIpt><<<grid<false>(sm_count), kBatchNT, SMEM, st>>>(T);
         k_batch_fixup<XT, AT><<<8 * sm_count, 256, 0, st>>>(T);
         k_batch_norm<XT><<<3 * sm_count, 256, 0, st>>>(T, want_dot);
         return cudaGetLastError();
@@ -528,56 +597,70 @@ struct BatchKernels {
 
 // Resident grid of a k_batch_sell instance: every warp's range of slice
 // groups starts at once (a second wave would double the step).
-template <typename VT, bool DOT>
+template <typename VT, int SUM>
 static int sell_batch_grid(int sm_count) {
     static int occ = 0;
     if (occ == 0) {
         int o = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_batch_sell<VT, DOT>, 256, 0) != cudaSuccess || o < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_batch_sell<VT, SUM>, 256, 0) != cudaSuccess || o < 1)
             o = 1;
         occ = o;
     }
     return occ * sm_count;
 }
 
-// A step of a SELL-32 class: the SpMV with the group sums and the per-slot
-// totals; the round's last step (which also needs v_k . v_{k+1}) takes the
-// row pass instead.
+// A step of a SELL-32 class: a key step (the slots' largest keys, then the
+// state advance), the step before a round's last (the group sums of squares
+// and the per-slot totals), or the round's last step (which also needs
+// v_k . v_{k+1}: the row pass).
 template <typename VT>
-static void launch_batch_sell(const BatchTable* T, bool dot, int sm_count, cudaStream_t st) {
-    if (dot) {
-        k_batch_sell<VT, false><<<sell_batch_grid<VT, false>(sm_count), 256, 0, st>>>(T);
-        k_batch_norm<float><<<3 * sm_count, 256, 0, st>>>(T, 1);
-    } else {
-        k_batch_sell<VT, true><<<sell_batch_grid<VT, true>(sm_count), 256, 0, st>>>(T);
+static void launch_batch_sell(const BatchTable* T, int sum, int sm_count, cudaStream_t st) {
+    if (sum == kSellKeys) {
+        k_batch_sell<VT, kSellKeys><<<sell_batch_grid<VT, kSellKeys>(sm_count), 256, 0, st>>>(T);
+        k_batch_keys<<<sm_count, 256, 0, st>>>(T);
+    } else if (sum == kSellSquares) {
+        k_batch_sell<VT, kSellSquares><<<sell_batch_grid<VT, kSellSquares>(sm_count), 256, 0, st>>>(T);
         k_batch_grp<<<sm_count, 256, 0, st>>>(T);
+    } else {
+        k_batch_sell<VT, kSellNone><<<sell_batch_grid<VT, kSellNone>(sm_count), 256, 0, st>>>(T);
+        k_batch_norm<float><<<3 * sm_count, 256, 0, st>>>(T, 1);
     }
 }
 
 void batch_prepare(int sm_count) {
-    BatchKernels<double, double, double>::grid(sm_count);
-    BatchKernels<float, float, float>::grid(sm_count);
-    BatchKernels<__nv_bfloat16, float, float>::grid(sm_count);
-    sell_batch_grid<float, false>(sm_count);
-    sell_batch_grid<float, true>(sm_count);
-    sell_batch_grid<__nv_bfloat16, false>(sm_count);
-    sell_batch_grid<__nv_bfloat16, true>(sm_count);
+    BatchKernels<double, double, double>::grid<false>(sm_count);
+    BatchKernels<double, double, double>::grid<true>(sm_count);
+    BatchKernels<float, float, float>::grid<false>(sm_count);
+    BatchKernels<float, float, float>::grid<true>(sm_count);
+    BatchKernels<__nv_bfloat16, float, float>::grid<false>(sm_count);
+    BatchKernels<__nv_bfloat16, float, float>::grid<true>(sm_count);
+    sell_batch_grid<float, kSellNone>(sm_count);
+    sell_batch_grid<float, kSellSquares>(sm_count);
+    sell_batch_grid<float, kSellKeys>(sm_count);
+    sell_batch_grid<__nv_bfloat16, kSellNone>(sm_count);
+    sell_batch_grid<__nv_bfloat16, kSellSquares>(sm_count);
+    sell_batch_grid<__nv_bfloat16, kSellKeys>(sm_count);
 }
 
+// A round of `steps` power steps: key steps, then the two steps whose norms
+// the round's Rayleigh quotient and residual use (||v_{k-1}||^2, then
+// ||v_k||^2 with v_{k-1} . v_k), then the residual.
 cudaError_t launch_batch_round(int cfg, const BatchTable* T, int steps, int sm_count, cudaStream_t st, bool sell) {
     for (int it = 0; it < steps; ++it) {
         const int want_dot = it == steps - 1;
+        const bool keys = it < steps - 2;
         cudaError_t e;
-        if (sell) {  // one kernel per step: SpMV and norm
-            if (cfg == kCfgBF16) launch_batch_sell<__nv_bfloat16>(T, want_dot, sm_count, st);
-            else launch_batch_sell<float>(T, want_dot, sm_count, st);
+        if (sell) {
+            const int sum = keys ? kSellKeys : want_dot ? kSellNone : kSellSquares;
+            if (cfg == kCfgBF16) launch_batch_sell<__nv_bfloat16>(T, sum, sm_count, st);
+            else launch_batch_sell<float>(T, sum, sm_count, st);
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             continue;
         }
         switch (cfg) {
-            case kCfgF32: e = BatchKernels<float, float, float>::step(T, want_dot, sm_count, st); break;
-            case kCfgBF16: e = BatchKernels<__nv_bfloat16, float, float>::step(T, want_dot, sm_count, st); break;
-            default: e = BatchKernels<double, double, double>::step(T, want_dot, sm_count, st); break;
+            case kCfgF32: e = BatchKernels<float, float, float>::step(T, want_dot, keys, sm_count, st); break;
+            case kCfgBF16: e = BatchKernels<__nv_bfloat16, float, float>::step(T, want_dot, keys, sm_count, st); break;
+            default: e = BatchKernels<double, double, double>::step(T, want_dot, keys, sm_count, st); break;
         }
         if (e != cudaSuccess) return e;
     }

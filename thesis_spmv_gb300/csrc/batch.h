@@ -52,6 +52,13 @@ struct SlotState {
     double lambda;      // Rayleigh quotient of u = v_{k-1} / ||v_{k-1}||
     double res2;        // ||A u - lambda u||^2 * ||v_{k-1}||^2
     unsigned int norm_count, res_count;  // last-CTA counters (zero between kernels)
+    // Key steps (a round's steps before its last two): only the exponent of
+    // the next exact 2^e rescale needs v_k's size, so those steps track the
+    // largest magnitude key of the stored rows instead of ||v||^2.
+    unsigned int mx;       // largest magnitude key of v_k (when keyed)
+    unsigned int mx_next;  // atomic-max target of a key step (zero between steps)
+    int keyed;             // v_k came from a key step: its rescale uses mx, nsq is stale
+    int pad;
 };
 
 struct BatchTable {

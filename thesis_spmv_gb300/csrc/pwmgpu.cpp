@@ -1770,12 +1770,20 @@ int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* gr
     return PWMGPU_OK;
 }
 
-int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t prefer_l1) {
+int pwmgpu_launch_variant(const pwmgpu_matrix* m, int32_t* variant) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
-    if (prefer_l1 != 0 && prefer_l1 != 1) return fail(PWMGPU_ERR_INVALID, "prefer_l1 must be 0 or 1");
+    if (!variant) return fail(PWMGPU_ERR_INVALID, "null output");
+    *variant = m->l1;
+    return PWMGPU_OK;
+}
+
+int pwmgpu_set_launch_variant(pwmgpu_matrix* m, int32_t variant) {
+    if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
+    if (variant != 0 && variant != 1 && variant != 4 && variant != 5)
+        return fail(PWMGPU_ERR_INVALID, "launch variant must be 0, 1, 4 or 5");
     if (!m->loaded || m->format != PWMGPU_FMT_MERGE) return fail(PWMGPU_ERR_STATE, "no merge-format matrix loaded");
     CU(cudaStreamSynchronize(m->stream));
-    m->l1 = prefer_l1 | (m->P.colp16 ? 2 : 0);
+    m->l1 = variant | (m->P.colp16 ? 2 : 0);
     m->grid = merge_grid(m->cfg, m->num_tiles, m->sm_count, m->l1);
     m->pgrid = power_persistent_grid(kCfgF64, m->num_tiles, m->sm_count, m->l1);
     m->pgrid32 = power_persistent_grid(kCfgF32, m->num_tiles, m->sm_count, m->l1);

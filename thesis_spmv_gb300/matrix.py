@@ -269,8 +269,16 @@ class CudaSparseMatrix:
         check(_lib.lib().pwmgpu_plan_info(self._h, C.byref(b), C.byref(g)), "pwmgpu_plan_info")
         return b.value, g.value
 
-    def set_launch_variant(self, prefer_l1):
-        check(_lib.lib().pwmgpu_set_launch_variant(self._h, int(prefer_l1)), "set_launch_variant")
+    def launch_variant(self):
+        """The merge kernels' launch variant bits (pwmgpu_launch_variant)."""
+        v = C.c_int32()
+        check(_lib.lib().pwmgpu_launch_variant(self._h, C.byref(v)), "pwmgpu_launch_variant")
+        return v.value
+
+    def set_launch_variant(self, variant):
+        """Override the load-time tuner: 0 / 1 (shared-memory carveout), 4 / 5
+        (the same, x gathers around L1)."""
+        check(_lib.lib().pwmgpu_set_launch_variant(self._h, int(variant)), "set_launch_variant")
 
     def tile_info(self):
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
