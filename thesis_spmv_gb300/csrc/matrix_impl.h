@@ -63,6 +63,9 @@ struct pwmgpu_matrix {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool loaded = false;
+    // No load-time launch tuning (the serving loop's matrices: its batched
+    // kernels do not use the handle's launch variant).
+    bool skip_tune = false;
 
     DevMatrix M;
 

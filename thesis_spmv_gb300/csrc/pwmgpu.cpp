@@ -306,7 +306,7 @@ int build_plan(pwmgpu_matrix* m) {
         TRY(build_format(m));
         return tune_csb(m);
     }
-    return build_merge(m, true);
+    return build_merge(m, !m->skip_tune);
 }
 }  // namespace pwmgpu
 namespace {

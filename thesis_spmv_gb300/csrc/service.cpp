@@ -129,6 +129,7 @@ struct pwmsvc {
     SlotState* h_states = nullptr;
     std::vector<int> free_states;
     int* d_status = nullptr;
+    int* h_status = nullptr;  // pinned: read back while the host admits requests
     ClassDev cls[kNumCls];
     bool dirty = true;
     cudaGraph_t graph = nullptr;
@@ -154,6 +155,7 @@ struct pwmsvc {
         dfree(d_states);
         dfree(d_status);
         if (h_states) cudaFreeHost(h_states);
+        if (h_status) cudaFreeHost(h_status);
         for (cudaEvent_t e : {fork_ev, ev0, ev1})
             if (e) cudaEventDestroy(e);
         for (cudaEvent_t e : join_ev)
@@ -190,6 +192,7 @@ int admit(pwmsvc* S, Req* r) {
     const pwmsvc_request& q = r->spec;
     TRY(pwmgpu_create(PWMGPU_FMT_MERGE, 1, &r->m));
     pwmgpu_matrix* m = r->m;
+    m->skip_tune = true;
     if (q.source == PWMSVC_SRC_POISSON) {
         TRY(pwmgpu_generate_poisson(m, q.grid_m, q.grid_n));
     } else if (q.source == PWMSVC_SRC_RANDOM) {
@@ -515,6 +518,9 @@ int pwmsvc_create(const pwmsvc_config* cfg, pwmsvc** out) {
         if ((rc = dalloc(&S->d_status, 4)) != PWMGPU_OK) break;
         e = cudaMallocHost((void**)&S->h_states, sizeof(SlotState) * (size_t)c.max_live);
         if (e != cudaSuccess) { S->h_states = nullptr; rc = fail(PWMGPU_ERR_NOMEM, "cudaMallocHost failed"); break; }
+        e = cudaMallocHost((void**)&S->h_status, sizeof(int));
+        if (e != cudaSuccess) { S->h_status = nullptr; rc = fail(PWMGPU_ERR_NOMEM, "cudaMallocHost failed"); break; }
+        *S->h_status = 0;
         for (auto& D : S->cls)
             if ((rc = dalloc(&D.dT, 1)) != PWMGPU_OK) break;
         if (rc != PWMGPU_OK) break;
@@ -606,10 +612,35 @@ int pwmsvc_submit(pwmsvc* s, const pwmsvc_request* q, int64_t* id) {
 int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
     if (!s) return fail(PWMGPU_ERR_INVALID, "null service");
     int fin = 0;
+    // the round of the solves already live goes to the GPU first; the queue's
+    // matrices are built while it runs (on their own streams) and join the
+    // next round
+    const bool ran = !s->live.empty();
+    if (ran) {
+        if (s->dirty) TRY(rebuild_tables(s));
+        // a solve's last possible round reports its residual from the row
+        // pass (earlier rounds may take it from the round's sums while it is
+        // large)
+        for (Req* r : s->live) {
+            const bool result_phase = !r->low || r->spec.precision == PWMGPU_PREC_F32;
+            if (result_phase && !r->exact_set && r->iterations + s->cfg.round_iterations >= r->spec.max_it) {
+                static const int one = 1;
+                CU(cudaMemcpyAsync(&s->d_states[r->slot].exact_res, &one, sizeof(int), cudaMemcpyHostToDevice,
+                                   s->stream));
+                r->exact_set = true;
+            }
+        }
+        TRY(run_round(s));
+        CU(cudaMemcpyAsync(s->h_states, s->d_states, sizeof(SlotState) * (size_t)s->cfg.max_live,
+                           cudaMemcpyDeviceToHost, s->stream));
+        CU(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    }
     // admission: FIFO while slots and the HBM budget allow
-    while (!s->queue.empty() && (int)s->live.size() < s->cfg.max_live && !s->free_states.empty()) {
+    std::vector<Req*> admitted;
+    while (!s->queue.empty() && (int)(s->live.size() + admitted.size()) < s->cfg.max_live &&
+           !s->free_states.empty()) {
         Req* r = s->queue.front();
-        if (!s->live.empty() && s->in_use + r->est > s->cfg.hbm_budget_bytes) break;
+        if (!(s->live.empty() && admitted.empty()) && s->in_use + r->est > s->cfg.hbm_budget_bytes) break;
         s->queue.pop_front();
         r->t_admit = s->now();
         r->slot = s->free_states.back();
@@ -630,35 +661,24 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
         }
         r->state = PWMSVC_RUNNING;
         s->in_use += r->bytes;
-        s->live.push_back(r);
-        s->dirty = true;
+        admitted.push_back(r);
     }
-    if (!s->live.empty()) {
-        if (s->dirty) TRY(rebuild_tables(s));
-        // a solve's last possible round reports its residual from the row
-        // pass (earlier rounds may take it from the round's sums while it is
-        // large)
-        for (Req* r : s->live) {
-            const bool result_phase = !r->low || r->spec.precision == PWMGPU_PREC_F32;
-            if (result_phase && !r->exact_set && r->iterations + s->cfg.round_iterations >= r->spec.max_it) {
-                static const int one = 1;
-                CU(cudaMemcpyAsync(&s->d_states[r->slot].exact_res, &one, sizeof(int), cudaMemcpyHostToDevice,
-                                   s->stream));
-                r->exact_set = true;
-            }
-        }
-        TRY(run_round(s));
-        CU(cudaMemcpyAsync(s->h_states, s->d_states, sizeof(SlotState) * (size_t)s->cfg.max_live,
-                           cudaMemcpyDeviceToHost, s->stream));
-        int status = 0;
-        CU(cudaMemcpyAsync(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    if (ran) {
         CU(cudaStreamSynchronize(s->stream));
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->gpu_ms += ms;
         ++s->rounds;
-        if (status != PWMGPU_OK) return fail(status, "a bounded device wait timed out in a service round");
+        const int status = *s->h_status;
+        if (status != PWMGPU_OK) {
+            for (Req* r : admitted) s->live.push_back(r);
+            if (!admitted.empty()) s->dirty = true;
+            return fail(status, "a bounded device wait timed out in a service round");
+        }
+        // the round's solves only: the new ones have no state yet
         TRY(after_round(s, &fin));
     }
+    for (Req* r : admitted) s->live.push_back(r);
+    if (!admitted.empty()) s->dirty = true;
     if (live) *live = (int32_t)s->live.size();
     if (queued) *queued = (int32_t)s->queue.size();
     if (finished) *finished = fin;
