@@ -12,8 +12,9 @@ Prints one JSON line (rank 0).  N > 1 runs independent replicas, one per GPU
 (the path does not shard on this single-GPU pool): value = all ranks' bytes /
 max time over ranks.
 
---impl reference times the reference's CPU path (CRSOMP::mv restated in the C
-oracle, OpenMP over all host cores) on the same workload.
+--impl reference times the reference's CPU path (CRSOMP::mv and
+CRS_Merge::mv restated in the C oracle, OpenMP over all host cores; the faster
+is the value) on the same workload.
 """
 import argparse
 import json
@@ -565,7 +566,8 @@ def serving(pwm, args):
     batch = {}
     arms = (("service_mixed", pwm.PREC_MIXED), ("service_fp64", pwm.PREC_F64))
     if args.batch_only:
-        arms = (("service_fp64", pwm.PREC_F64),)
+        arms = ((("service_mixed", pwm.PREC_MIXED),) if args.batch_precision == "mixed"
+                else (("service_fp64", pwm.PREC_F64),))
     lam = {}
     for name, prec in arms:
         el, res, vecs, st = _service_batch(pwm, S, specs, prec, max_it, tol, check)
@@ -1003,7 +1005,9 @@ def main():
     ap.add_argument("--batch-count", type=int, default=128,
                     help="Poisson grids and random matrices in the batch (128 each)")
     ap.add_argument("--batch-only", action="store_true",
-                    help="only the 256-matrix batch through the FP64 service (a profiling case)")
+                    help="only the 256-matrix batch through the service (a profiling case)")
+    ap.add_argument("--batch-precision", choices=["fp64", "mixed"], default="fp64",
+                    help="the service precision of --batch-only")
     ap.add_argument("--stream-requests", type=int, default=300)
     ap.add_argument("--stream-rates", type=float, nargs="+", default=[50.0, 100.0, 200.0, 500.0, 1000.0, 2000.0])
     ap.add_argument("--case", choices=["irregular", "poisson"],
