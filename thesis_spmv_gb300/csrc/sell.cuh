@@ -18,6 +18,9 @@ constexpr uint16_t kSellPad = 0xFFFF;
 // each row's products summed left to right in CRS order.  For J
 // elements of both rows the column and value loads are issued together,
 // then the x gathers, then the FMAs.  cp*, vp*: the lane's first element.
+// The columns and values are read once per step: streaming loads
+// (ld.global.cs, evict-first in L1 and L2), so the stream does not push the
+// x rows a stencil's slices read again (rows r - m and r + m) out of L2.
 template <typename VT, int J = kSellJ>
 __device__ __forceinline__ void sell_rows2(const uint16_t* __restrict__ cpa, const VT* __restrict__ vpa,
                                            const float* __restrict__ xa, int cba, int wa,
@@ -30,10 +33,10 @@ __device__ __forceinline__ void sell_rows2(const uint16_t* __restrict__ cpa, con
         float va[J], vb[J], ga[J], gb[J];
 #pragma unroll
         for (int u = 0; u < J; ++u) {
-            ca[u] = j + u < wa ? __ldg(cpa + 32 * (j + u)) : kSellPad;
-            cb[u] = j + u < wb ? __ldg(cpb + 32 * (j + u)) : kSellPad;
-            va[u] = j + u < wa ? to_f32(__ldg(vpa + 32 * (j + u))) : 0.0f;
-            vb[u] = j + u < wb ? to_f32(__ldg(vpb + 32 * (j + u))) : 0.0f;
+            ca[u] = j + u < wa ? __ldcs(cpa + 32 * (j + u)) : kSellPad;
+            cb[u] = j + u < wb ? __ldcs(cpb + 32 * (j + u)) : kSellPad;
+            va[u] = j + u < wa ? to_f32(__ldcs(vpa + 32 * (j + u))) : 0.0f;
+            vb[u] = j + u < wb ? to_f32(__ldcs(vpb + 32 * (j + u))) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < J; ++u) {
