@@ -116,13 +116,22 @@ __device__ __forceinline__ Oct<K> load_oct(const uint32_t* __restrict__ ind, con
     const uint4* ip = reinterpret_cast<const uint4*>(ind + k);
     const uint4* cp = reinterpret_cast<const uint4*>(kcol + k);
     const double2* dp = reinterpret_cast<const double2*>(data + k);
+    // a flat unit (GX: x gathered by global column through L2) streams its
+    // elements with evict-first loads, so they do not push x out of L2; a
+    // dense unit's x window is in shared memory and keeps plain loads
 #pragma unroll
     for (int i = 0; i < K / 4; ++i)
         if (4 * i < q.nv) {
-            q.id[i] = __ldg(ip + i);
-            if (GX) q.gc[i] = __ldg(cp + i);
-            q.d[2 * i] = __ldg(dp + 2 * i);
-            q.d[2 * i + 1] = __ldg(dp + 2 * i + 1);
+            if (GX) {
+                q.id[i] = __ldcs(ip + i);
+                q.gc[i] = __ldcs(cp + i);
+                q.d[2 * i] = __ldcs(dp + 2 * i);
+                q.d[2 * i + 1] = __ldcs(dp + 2 * i + 1);
+            } else {
+                q.id[i] = __ldg(ip + i);
+                q.d[2 * i] = __ldg(dp + 2 * i);
+                q.d[2 * i + 1] = __ldg(dp + 2 * i + 1);
+            }
         }
     q.rout = -1;
     if (k0 >= hi) return q;  // a warp past the unit's end
