@@ -210,13 +210,14 @@ int pwmgpu_power(pwmgpu_matrix* m, double* x, double* y, int32_t it);
 int pwmgpu_power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it);
 
 /* How pwmgpu_power / pwmgpu_power_device run the iterations:
- * FUSED uses one persistent cooperative kernel for all iterations (SpMV,
- * fix-up, norm and rescale; three grid barriers per iteration; fails with
- * PWMGPU_ERR_UNSUPPORTED where it cannot be co-resident); MULTI launches the
- * SpMV, fix-up and norm kernels per iteration; AUTO (default) takes FUSED
- * for matrices with fewer than two merge sub-tiles per resident warp (where
- * launches would dominate), MULTI otherwise.  Results are equal within the
- * power method's tolerance. */
+ * FUSED uses one persistent cooperative kernel for all iterations (SpMV pass,
+ * grid barrier, fix-up pass, grid barrier per iteration, the norms of the
+ * last two iterations folded in; fails with PWMGPU_ERR_UNSUPPORTED where it
+ * cannot be co-resident); MULTI launches the SpMV and fix-up kernels per
+ * iteration with programmatic dependent launch; AUTO (default) takes MULTI,
+ * which measured faster at every size on GB300 (256^2 to 4096^2 Poisson
+ * grids, the 4M-row irregular matrix).  Results are equal within the power
+ * method's tolerance. */
 #define PWMGPU_POWER_AUTO 0
 #define PWMGPU_POWER_FUSED 1
 #define PWMGPU_POWER_MULTI 2

@@ -450,17 +450,14 @@ int scale_step_f64(pwmgpu_matrix* m, const double* in, double* out, const double
     return PWMGPU_OK;
 }
 
-// POWER_AUTO: the persistent kernel saves three launches per iteration,
-// which pays while a pass is short; once every resident warp has a few
-// sub-tiles per pass, the two-kernel step is as fast or faster (its SpMV runs
-// the most resident CTAs and its kernel boundaries are cheaper than grid
-// barriers: 4096^2 Poisson 0.277 vs 0.29 ms per iteration, 1024^2 0.038 vs
-// 0.043, the irregular 4M matrix 0.418 vs 0.424).
+// POWER_AUTO runs the two-kernel step at every size: its kernel boundaries
+// (programmatic dependent launch) cost less than the persistent kernel's
+// grid barriers, and its SpMV keeps the most resident CTAs.  Per iteration,
+// Poisson grids: 256^2 6.5 vs 11.0 us, 512^2 10.7 vs 19.7 us, 1024^2 21.7 vs
+// 30.4 us, 2048^2 63.2 vs 72.3 us, 4096^2 0.223 vs 0.240 ms; the irregular 4M
+// matrix 0.393 vs 0.425 ms.  POWER_FUSED selects the persistent kernel.
 bool use_fused(const pwmgpu_matrix* m, int pgrid) {
-    if (m->power_mode == PWMGPU_POWER_MULTI || pgrid <= 0) return false;
-    if (m->power_mode == PWMGPU_POWER_FUSED) return true;
-    const MergeGeom g = merge_geometry(kCfgF64, m->l1);
-    return m->num_tiles < 2LL * g.occ * g.w * m->sm_count;
+    return m->power_mode == PWMGPU_POWER_FUSED && pgrid > 0;
 }
 
 int power_device(pwmgpu_matrix* m, double* dx, double* dy, int32_t it) {
