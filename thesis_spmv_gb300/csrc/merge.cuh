@@ -230,8 +230,14 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 // it is read with ordinary coherent loads (ld.global.ca: L1-cached, and
 // ordered after the grid barrier's acquire) instead of the read-only
 // non-coherent path.
-// CG: gathers that bypass L1 (ld.global.cg) -- faster where x is spread too
-// widely for L1 to hit (the launch tuner decides per matrix).
+// CG: gathers of columns far from the sub-tile's rows bypass L1
+// (ld.global.cg) -- where x is spread too widely for L1 to hit, they would
+// only evict useful lines -- while columns within kNearRows of its first row
+// (a band around the diagonal, which neighbouring sub-tiles of the same CTA
+// read again) go through L1 (ld.global.ca).  The launch tuner decides per
+// matrix between this and plain read-only gathers.
+constexpr int kNearRows = 4096;
+
 template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false, bool C16 = false, bool CG = false>
 __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT* __restrict__ x, AT (&xv)[IPT]) {
     using S = WarpStage<VT, IPT, C16>;
@@ -253,8 +259,12 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 #pragma unroll
         for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldca(x + cv[j]) : AT(0);
     } else if (CG) {
+        const int rw0 = reinterpret_cast<const int4*>(st)[0].x;
 #pragma unroll
-        for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldcg(x + cv[j]) : AT(0);
+        for (int j = 0; j < IPT; ++j) {
+            const bool near = (unsigned)(cv[j] - rw0 + kNearRows) < 2u * kNearRows;
+            xv[j] = (j < cnt) ? (near ? (AT)__ldca(x + cv[j]) : (AT)__ldcg(x + cv[j])) : AT(0);
+        }
     } else {
 #pragma unroll
         for (int j = 0; j < IPT; ++j) xv[j] = (j < cnt) ? (AT)__ldg(x + cv[j]) : AT(0);
