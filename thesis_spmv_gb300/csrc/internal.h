@@ -45,6 +45,16 @@ struct MergeGeom {
 
 // Per-matrix plan of the merge-path kernel: sub-tile boundaries, metadata,
 // row-end masks and the lane-interleaved column / FP64 value arrays.
+// Device frees.  cudaFree waits for all work on the device, so a build that
+// runs beside other kernels (the serving loop builds admitted matrices while
+// its round runs) would wait for them at every free.  defer_frees(&list)
+// makes this thread's dev_free calls append to `list` instead, until
+// defer_frees(nullptr); free_deferred(list) then frees them (after the caller
+// has synchronised the work that used them).
+void dev_free(void* p);
+void defer_frees(std::vector<void*>* list);
+void free_deferred(std::vector<void*>& list);
+
 struct MliPlan {
     int nsub = 0;
     int2* subc = nullptr;       // nsub + 1 merge coordinates (row, nonzero)

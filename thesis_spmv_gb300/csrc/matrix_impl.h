@@ -46,7 +46,7 @@ inline int dalloc(T** p, size_t count) {
 
 template <typename T>
 inline void dfree(T*& p) {
-    if (p) cudaFree((void*)p);
+    if (p) dev_free((void*)p);
     p = nullptr;
 }
 
@@ -201,7 +201,7 @@ struct pwmgpu_matrix {
         tuning = pwmgpu_tuning{};
         pipe.K = 0;
         pipe.rec.clear();
-        if (valbf) cudaFree(valbf);
+        if (valbf) pwmgpu::dev_free(valbf);
         valbf = nullptr;
         bf16_exact = -1;
         sell.release();

@@ -1336,12 +1336,12 @@ int build_fix_runs(MliPlan& P, const int32_t* row_start, int nor, int sm_count, 
         if (total > 0) k_run_compact<<<nb, 256, 0, st>>>(P.run_pre, desc, P.nsub, P.runs);
         if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = 1;
     } while (0);
-    if (desc) cudaFree(desc);
-    if (scan_scratch) cudaFree(scan_scratch);
+    if (desc) dev_free(desc);
+    if (scan_scratch) dev_free(scan_scratch);
     if (rc) {
         (void)cudaGetLastError();
-        if (P.runs) cudaFree(P.runs);
-        if (P.run_pre) cudaFree(P.run_pre);
+        if (P.runs) dev_free(P.runs);
+        if (P.run_pre) dev_free(P.run_pre);
         P.runs = nullptr;
         P.run_pre = nullptr;
         P.nruns = 0;

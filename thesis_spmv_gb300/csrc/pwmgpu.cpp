@@ -53,6 +53,23 @@ int ensure_cap(double** p, size_t* cap, size_t need) {
 
 }  // namespace
 namespace pwmgpu {
+namespace {
+thread_local std::vector<void*>* g_deferred_frees = nullptr;
+}
+
+void dev_free(void* p) {
+    if (!p) return;
+    if (g_deferred_frees) g_deferred_frees->push_back(p);
+    else cudaFree(p);
+}
+
+void defer_frees(std::vector<void*>* list) { g_deferred_frees = list; }
+
+void free_deferred(std::vector<void*>& list) {
+    for (void* p : list) cudaFree(p);
+    list.clear();
+}
+
 int check_status(pwmgpu_matrix* m) {
     int st = 0;
     CU(cudaMemcpyAsync(&st, m->status, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
@@ -1450,7 +1467,7 @@ int pwmgpu_merge_partition(pwmgpu_matrix* m, int32_t parts, int32_t* coords) {
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(coords, d, sizeof(int2) * ((size_t)parts + 1), cudaMemcpyDeviceToHost, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
-    cudaFree(d);
+    dev_free(d);
     if (e != cudaSuccess) return fail(PWMGPU_ERR_CUDA, "merge partition: %s", cudaGetErrorString(e));
     return PWMGPU_OK;
 }

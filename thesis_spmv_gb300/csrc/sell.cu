@@ -186,11 +186,11 @@ int sell_grid(int nslices, int sm_count) {
 }
 
 void SellPlan::release() {
-    cudaFree(soff);
-    cudaFree(col16);
-    cudaFree(val32);
-    cudaFree(valbf);
-    cudaFree(npart);
+    dev_free(soff);
+    dev_free(col16);
+    dev_free(val32);
+    dev_free(valbf);
+    dev_free(npart);
     soff = nullptr;
     col16 = nullptr;
     val32 = nullptr;
@@ -281,9 +281,9 @@ int sell_build(SellPlan& S, const int32_t* row_start, const int32_t* col, const 
         }
         S.state = 1;
     } while (0);
-    if (flag) cudaFree(flag);
-    if (scratch) cudaFree(scratch);
-    if (total) cudaFree(total);
+    if (flag) dev_free(flag);
+    if (scratch) dev_free(scratch);
+    if (total) dev_free(total);
     if (rc) {
         (void)cudaGetLastError();
         S.release();

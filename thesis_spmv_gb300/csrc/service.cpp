@@ -50,6 +50,12 @@ constexpr double kSvcSwitchRel = 2e-6;
 // same bits alone and in any mix.
 constexpr int kProbeRounds = 5;
 
+// Requests admitted per step.  A step admits while its round runs, so a
+// burst (a batch submitted at once) is built a slice at a time beside the
+// rounds of the solves already admitted, instead of all before the first
+// round.
+constexpr int kAdmitPerStep = 32;
+
 struct Req {
     int64_t id = 0;
     pwmsvc_request spec{};
@@ -130,6 +136,7 @@ struct pwmsvc {
     std::vector<int> free_states;
     int* d_status = nullptr;
     int* h_status = nullptr;  // pinned: read back while the host admits requests
+    std::vector<void*> deferred;  // device frees of the matrix builds, made after the round
     ClassDev cls[kNumCls];
     bool dirty = true;
     cudaGraph_t graph = nullptr;
@@ -140,6 +147,7 @@ struct pwmsvc {
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
     void release() {
+        free_deferred(deferred);
         for (auto& kv : all)
             if (kv.second->m) pwmgpu_destroy(kv.second->m);
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -635,10 +643,13 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
                            cudaMemcpyDeviceToHost, s->stream));
         CU(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     }
-    // admission: FIFO while slots and the HBM budget allow
+    // admission: FIFO while slots and the HBM budget allow; the builds'
+    // device frees wait until the round is done (a cudaFree now would wait
+    // for the round)
     std::vector<Req*> admitted;
+    defer_frees(&s->deferred);
     while (!s->queue.empty() && (int)(s->live.size() + admitted.size()) < s->cfg.max_live &&
-           !s->free_states.empty()) {
+           !s->free_states.empty() && (int)admitted.size() < kAdmitPerStep) {
         Req* r = s->queue.front();
         if (!(s->live.empty() && admitted.empty()) && s->in_use + r->est > s->cfg.hbm_budget_bytes) break;
         s->queue.pop_front();
@@ -663,8 +674,11 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
         s->in_use += r->bytes;
         admitted.push_back(r);
     }
+    defer_frees(nullptr);
     if (ran) {
-        CU(cudaStreamSynchronize(s->stream));
+        const cudaError_t se = cudaStreamSynchronize(s->stream);
+        free_deferred(s->deferred);
+        CU(se);
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) s->gpu_ms += ms;
         ++s->rounds;
@@ -679,6 +693,7 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
     }
     for (Req* r : admitted) s->live.push_back(r);
     if (!admitted.empty()) s->dirty = true;
+    free_deferred(s->deferred);
     if (live) *live = (int32_t)s->live.size();
     if (queued) *queued = (int32_t)s->queue.size();
     if (finished) *finished = fin;
