@@ -87,6 +87,9 @@ struct SellPlan {
     void release();
 };
 int sell_grid(int nslices, int sm_count);
+// Fill the launch-geometry caches (occupancies) of the merge and SELL kernels
+// once, so that matrix builds on several host threads only read them.
+void warm_launch_caches(int sm_count);
 // Build the slices (first call) and the value array of the requested type
 // from CRS arrays; 0 = built, 1 = the matrix does not fit (state -1), 2 = a
 // CUDA error or no memory (state 0).

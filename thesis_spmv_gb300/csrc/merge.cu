@@ -1081,6 +1081,15 @@ MergeGeom merge_geometry(int cfg, int l1) {
     }
 }
 
+void warm_launch_caches(int sm_count) {
+    for (int cfg : {kCfgF64, kCfgF32, kCfgBF16})
+        for (int v = 0; v < 4; ++v) {
+            (void)merge_geometry(cfg, v);
+            (void)power_persistent_grid(cfg, 1, sm_count, v);
+        }
+    (void)sell_grid(1, sm_count);
+}
+
 int merge_grid(int cfg, int nsub, int sm_count, int l1) {
     MergeGeom g = merge_geometry(cfg, l1);
     long long ctas = (nsub + g.w - 1) / g.w;

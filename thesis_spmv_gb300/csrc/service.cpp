@@ -10,12 +10,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "batch.h"
@@ -55,6 +57,10 @@ constexpr int kProbeRounds = 5;
 // rounds of the solves already admitted, instead of all before the first
 // round.
 constexpr int kAdmitPerStep = 32;
+// Host threads that build a step's admissions (each on its own stream: the
+// builds are chains of short kernels, allocations and stream syncs, so a
+// burst of small matrices is bound by their latency, not by the GPU).
+constexpr int kAdmitThreads = 8;
 
 struct Req {
     int64_t id = 0;
@@ -538,6 +544,7 @@ int pwmsvc_create(const pwmsvc_config* cfg, pwmsvc** out) {
         if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
         if (e != cudaSuccess) { rc = fail(PWMGPU_ERR_CUDA, "pwmsvc_create: %s", cudaGetErrorString(e)); break; }
         batch_prepare(S->sm_count);
+        warm_launch_caches(S->sm_count);  // before builds run on several threads
         if ((rc = rebuild_tables(S.get())) != PWMGPU_OK) break;
     } while (0);
     if (rc != PWMGPU_OK) {
@@ -643,20 +650,47 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
                            cudaMemcpyDeviceToHost, s->stream));
         CU(cudaMemcpyAsync(s->h_status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     }
-    // admission: FIFO while slots and the HBM budget allow; the builds'
+    // admission: FIFO while slots and the HBM budget allow (by the requests'
+    // estimates), the builds on up to kAdmitThreads host threads; their
     // device frees wait until the round is done (a cudaFree now would wait
     // for the round)
-    std::vector<Req*> admitted;
-    defer_frees(&s->deferred);
-    while (!s->queue.empty() && (int)(s->live.size() + admitted.size()) < s->cfg.max_live &&
-           !s->free_states.empty() && (int)admitted.size() < kAdmitPerStep) {
+    std::vector<Req*> batch;
+    size_t planned = s->in_use;
+    while (!s->queue.empty() && (int)(s->live.size() + batch.size()) < s->cfg.max_live &&
+           !s->free_states.empty() && (int)batch.size() < kAdmitPerStep) {
         Req* r = s->queue.front();
-        if (!(s->live.empty() && admitted.empty()) && s->in_use + r->est > s->cfg.hbm_budget_bytes) break;
+        if (!(s->live.empty() && batch.empty()) && planned + r->est > s->cfg.hbm_budget_bytes) break;
         s->queue.pop_front();
         r->t_admit = s->now();
         r->slot = s->free_states.back();
         s->free_states.pop_back();
-        int rc = admit(s, r);
+        planned += r->est;
+        batch.push_back(r);
+    }
+    std::vector<int> built(batch.size(), PWMGPU_OK);
+    const int nt = (int)std::min<size_t>((size_t)kAdmitThreads, batch.size());
+    if (nt <= 1) {
+        defer_frees(&s->deferred);
+        for (size_t i = 0; i < batch.size(); ++i) built[i] = admit(s, batch[i]);
+        defer_frees(nullptr);
+    } else {
+        std::vector<std::vector<void*>> frees((size_t)nt);
+        std::atomic<int> next{0};
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back([&, t] {
+                cudaSetDevice(s->device);
+                defer_frees(&frees[(size_t)t]);
+                for (int i; (i = next.fetch_add(1)) < (int)batch.size();) built[(size_t)i] = admit(s, batch[(size_t)i]);
+                defer_frees(nullptr);
+            });
+        for (auto& t : th) t.join();
+        for (auto& f : frees) s->deferred.insert(s->deferred.end(), f.begin(), f.end());
+    }
+    std::vector<Req*> admitted;
+    for (size_t i = 0; i < batch.size(); ++i) {
+        Req* r = batch[i];
+        int rc = built[i];
         if (rc == PWMGPU_OK) rc = reset_state(s, r->slot);
         if (rc != PWMGPU_OK) {
             r->error = rc;
@@ -674,7 +708,6 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
         s->in_use += r->bytes;
         admitted.push_back(r);
     }
-    defer_frees(nullptr);
     if (ran) {
         const cudaError_t se = cudaStreamSynchronize(s->stream);
         free_deferred(s->deferred);
