@@ -52,14 +52,15 @@ constexpr double kSvcSwitchRel = 2e-6;
 // same bits alone and in any mix.
 constexpr int kProbeRounds = 5;
 
-// Requests admitted per step.  A step admits while its round runs, so a
-// burst (a batch submitted at once) is built a slice at a time beside the
-// rounds of the solves already admitted, instead of all before the first
-// round.
+// Requests admitted per step while a round runs: a burst that arrives
+// while solves are live is built a slice at a time beside their rounds.
+// With nothing live (a batch submitted at once) the step admits all it can:
+// there is no round to overlap, and the solves started later would only
+// finish later.
 constexpr int kAdmitPerStep = 32;
-// Host threads that build a step's admissions (each on its own stream: the
-// builds are chains of short kernels, allocations and stream syncs, so a
-// burst of small matrices is bound by their latency, not by the GPU).
+// Host threads that build a step's admissions while its round runs (each on
+// its own stream: the builds are chains of short kernels, allocations and
+// stream syncs, bound by their latency, not by the GPU).
 constexpr int kAdmitThreads = 8;
 
 struct Req {
@@ -656,8 +657,9 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
     // for the round)
     std::vector<Req*> batch;
     size_t planned = s->in_use;
+    const int cap = ran ? kAdmitPerStep : s->cfg.max_live;
     while (!s->queue.empty() && (int)(s->live.size() + batch.size()) < s->cfg.max_live &&
-           !s->free_states.empty() && (int)batch.size() < kAdmitPerStep) {
+           !s->free_states.empty() && (int)batch.size() < cap) {
         Req* r = s->queue.front();
         if (!(s->live.empty() && batch.empty()) && planned + r->est > s->cfg.hbm_budget_bytes) break;
         s->queue.pop_front();
@@ -668,7 +670,10 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
         batch.push_back(r);
     }
     std::vector<int> built(batch.size(), PWMGPU_OK);
-    const int nt = (int)std::min<size_t>((size_t)kAdmitThreads, batch.size());
+    // several builders only beside a round: with the device idle (a batch
+    // submitted at once) one thread built the 256-matrix batch faster (178
+    // vs 170 solves/s; its 128 small random matrices 870 vs 760)
+    const int nt = ran ? (int)std::min<size_t>((size_t)kAdmitThreads, batch.size()) : 1;
     if (nt <= 1) {
         defer_frees(&s->deferred);
         for (size_t i = 0; i < batch.size(); ++i) built[i] = admit(s, batch[i]);
