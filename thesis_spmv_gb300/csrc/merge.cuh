@@ -231,11 +231,12 @@ __device__ __forceinline__ void issue_subtile(unsigned char* st, uint64_t* bar, 
 // ordered after the grid barrier's acquire) instead of the read-only
 // non-coherent path.
 // CG: gathers of columns far from the sub-tile's rows bypass L1
-// (ld.global.cg) -- where x is spread too widely for L1 to hit, they would
-// only evict useful lines -- while columns within kNearRows of its first row
-// (a band around the diagonal, which neighbouring sub-tiles of the same CTA
-// read again) go through L1 (ld.global.ca).  The launch tuner decides per
-// matrix between this and plain read-only gathers.
+// (ld.global.cg: where x is spread too widely for L1 to hit), columns within
+// kNearRows of its first row use ld.global.ca.  On the irregular
+// lognormal-row matrix the split ran 6 % faster than bypassing L1 for all
+// gathers (fewer short-scoreboard stalls; the L1 hit rate stayed at 3 %).
+// The launch tuner decides per matrix between this and plain read-only
+// gathers.
 constexpr int kNearRows = 4096;
 
 template <typename VT, typename XT, typename AT, int IPT, bool XCOH = false, bool C16 = false, bool CG = false>
