@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(NT) k_merge_spmv(MergeArgs<VT, XT, AT> a) {
     warp_pass<MODE, VT, XT, AT, NT, IPT, false, C16, CG>(a, a.x, a.y, stages, bars[w], crow + 32 * w,
                                                          cval + 32 * w, hval + 32 * w, ticket, e,
                                                          policy_evict_first(), ss, mx);
-    if (MODE == MODE_SCALE && a.mx_out) warp_max_out(mx, a.mx_out);
+    if (MODE == MODE_SCALE && a.mx_out) block_max_out<NT>(mx, a.mx_out);
     if (MODE == MODE_POWER && a.npart) {
         // this CTA's share of ||y||^2 (k_fix_runs adds the fixed-up rows and
         // sums the shares in a fixed order)
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(256) k_fix_runs(const int4* __restrict__ runs,
         if (MODE == MODE_POWER) ss = fma((double)v, (double)v, ss);
         if (MODE == MODE_SCALE) mx = max(mx, mag_key(v));
     }
-    if (MODE == MODE_SCALE && nrm.mx_out) warp_max_out(mx, nrm.mx_out);
+    if (MODE == MODE_SCALE && nrm.mx_out) block_max_out<256>(mx, nrm.mx_out);
     if (MODE != MODE_POWER || !nrm.npart) return;
     __shared__ double red[8];
     __shared__ bool am_last;
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(NT, 6) k_power_persistent(PowerArgs<VT, XT, AT
             else
                 fixup_pass<MODE_SCALE, XT, AT, false>(a.row_start, p.subc, a.nor, a.nsub, out, a.carries, e, tid,
                                                       a.nsub, nthr, no_ss, &mx);
-            warp_max_out(mx, p.mxk + k + 1);
+            block_max_out<NT>(mx, p.mxk + k + 1);
             if (!grid_sync(p.barrier, a.status, p.wait.cycles, p.wait.extra)) return;
             prev_keys = true;
             continue;

@@ -180,6 +180,22 @@ __device__ __forceinline__ void warp_max_out(unsigned mx, unsigned int* out) {
     if ((threadIdx.x & 31) == 0 && mx != 0u) atomicMax(out, mx);
 }
 
+// The same for a whole CTA of NT threads (call with all of them): one
+// atomic per CTA (atomics on one address are serialised where it lives; a
+// 4096^2 pass makes 912 instead of 3648).
+template <int NT>
+__device__ __forceinline__ void block_max_out(unsigned mx, unsigned int* out) {
+    __shared__ unsigned wmax[NT / 32];
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned m = threadIdx.x < NT / 32 ? wmax[threadIdx.x] : 0u;
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (threadIdx.x == 0 && m != 0u) atomicMax(out, m);
+    }
+}
+
 // MODE_SPMV: y = A x.  MODE_POWER: y = 2^e A x with ||y||^2 summed (the power
 // method's steps whose norm is used).  MODE_SCALE: y = 2^e A x tracking only
 // the largest |y_i| (magnitude keys, integer max) -- the power method's
