@@ -17,6 +17,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -679,16 +680,21 @@ int pwmsvc_step(pwmsvc* s, int32_t* live, int32_t* queued, int32_t* finished) {
         for (size_t i = 0; i < batch.size(); ++i) built[i] = admit(s, batch[i]);
         defer_frees(nullptr);
     } else {
-        std::vector<std::vector<void*>> frees((size_t)nt);
+        std::vector<std::vector<void*>> frees((size_t)nt + 1);
         std::atomic<int> next{0};
+        auto work = [&](size_t slot) {
+            cudaSetDevice(s->device);
+            defer_frees(&frees[slot]);
+            for (int i; (i = next.fetch_add(1)) < (int)batch.size();) built[(size_t)i] = admit(s, batch[(size_t)i]);
+            defer_frees(nullptr);
+        };
         std::vector<std::thread> th;
-        for (int t = 0; t < nt; ++t)
-            th.emplace_back([&, t] {
-                cudaSetDevice(s->device);
-                defer_frees(&frees[(size_t)t]);
-                for (int i; (i = next.fetch_add(1)) < (int)batch.size();) built[(size_t)i] = admit(s, batch[(size_t)i]);
-                defer_frees(nullptr);
-            });
+        try {
+            for (int t = 0; t < nt; ++t) th.emplace_back(work, (size_t)t);
+        } catch (const std::system_error&) {
+            // no more threads: the ones started and this one share the rest
+        }
+        work((size_t)nt);
         for (auto& t : th) t.join();
         for (auto& f : frees) s->deferred.insert(s->deferred.end(), f.begin(), f.end());
     }
