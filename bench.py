@@ -684,6 +684,9 @@ def serving(pwm, args):
             lat = _stream_run(submit_fn, arr, step_fn, idle_fn)
             res = [svc.result(ids[i]) for i in range(R)]
             rec = lat_stats(lat, np.array([r.converged for r in res], bool), max(float(np.max(lat + arr)), 1e-9))
+            st = svc.stats()
+            rec["rounds"] = int(st.rounds)
+            rec["gpu_round_ms"] = round(st.gpu_round_ms, 1)
             rec["oracle_check"] = _oracle_checks([(specs[i][0], specs[i][1], res[i].lambda_, res[i].residual,
                                                    res[i].converged, svc.result(ids[i], want_vector=True)[1])
                                                   for i in sorted(check)])
