@@ -76,3 +76,7 @@ def test_null_arguments_are_rejected():
     assert L.pwmgpu_power(None, None, None, 3) == 1
     assert L.pwmgpu_destroy(None) == 0
     assert L.pwmgpu_create(7, 1, ctypes.byref(ctypes.c_void_p())) == 1  # unknown format
+    v = ctypes.c_int32()
+    assert L.pwmgpu_launch_variant(None, ctypes.byref(v)) == 1
+    assert L.pwmgpu_set_launch_variant(None, 0) == 1
+    assert L.pwmgpu_set_launch_variant(None, 12) == 1
