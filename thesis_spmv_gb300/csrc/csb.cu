@@ -561,8 +561,79 @@ bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<doubl
         th.emplace_back(work, a, b);
     }
     for (auto& t : th) t.join();
-    win_ptr.swap(new_ptr);
-    units.swap(new_units);
+
+    // A dense unit whose elements lie on at most kTileMaxDiag diagonals of
+    // the tile (a banded tile: a stencil's diagonal tiles) is split into one
+    // unit per diagonal, each with one element per row -- the kernel's
+    // element-per-lane path -- taken in diagonal order, which is column
+    // order within each row (the row sums keep CRS order).  The elements
+    // are reordered in place: diagonal by diagonal, rows ascending.
+    constexpr int kTileMaxDiag = 4;
+    std::vector<std::vector<int>> diag_len((size_t)nnew);  // elements per diagonal, or empty: keep the unit
+    auto band = [&](int v0, int v1) {
+        std::vector<std::tuple<int, uint32_t, uint32_t, double>> el;
+        for (int v = v0; v < v1; ++v) {
+            const int lo = new_units[4 * (size_t)v], hi = new_units[4 * (size_t)v + 1];
+            if (new_units[4 * (size_t)v + 2] < 0 || new_units[4 * (size_t)v + 3] == 2 || hi <= lo) continue;
+            int diags[kTileMaxDiag], nd = 0;
+            bool ok = true;
+            for (int k = lo; k < hi && ok; ++k) {
+                const uint32_t id = kind[(size_t)k];
+                const int d = (int)(id & (uint32_t)(S - 1)) - (int)((id >> 16) & (uint32_t)(S - 1));
+                int j = 0;
+                while (j < nd && diags[j] != d) ++j;
+                if (j == nd) {
+                    if (nd == kTileMaxDiag) ok = false;
+                    else diags[nd++] = d;
+                }
+            }
+            if (!ok || nd < 2) continue;
+            el.clear();
+            for (int k = lo; k < hi; ++k) {
+                const uint32_t id = kind[(size_t)k];
+                const int d = (int)(id & (uint32_t)(S - 1)) - (int)((id >> 16) & (uint32_t)(S - 1));
+                el.emplace_back(d, (id >> 16) & (uint32_t)(S - 1), id, kdata[(size_t)k]);
+            }
+            std::sort(el.begin(), el.end(), [](const auto& a, const auto& b) {
+                return std::get<0>(a) != std::get<0>(b) ? std::get<0>(a) < std::get<0>(b) : std::get<1>(a) < std::get<1>(b);
+            });
+            std::vector<int>& len = diag_len[(size_t)v];
+            for (size_t q = 0; q < el.size(); ++q) {
+                kind[(size_t)lo + q] = std::get<2>(el[q]);
+                kdata[(size_t)lo + q] = std::get<3>(el[q]);
+                if (q == 0 || std::get<0>(el[q]) != std::get<0>(el[q - 1])) len.push_back(0);
+                ++len.back();
+            }
+        }
+    };
+    th.clear();
+    for (int t = 0; t < nt; ++t) {
+        const int a = (int)((long long)nnew * t / nt), b = (int)((long long)nnew * (t + 1) / nt);
+        th.emplace_back(band, a, b);
+    }
+    for (auto& t : th) t.join();
+    std::vector<int> out_ptr(new_ptr.size(), 0), out_units;
+    out_units.reserve(new_units.size());
+    for (int w = 0; w < nwin; ++w) {
+        for (int part = 0; part < 2; ++part) {
+            out_ptr[2 * (size_t)w + part] = (int)(out_units.size() / 4);
+            for (int v = new_ptr[2 * (size_t)w + part]; v < new_ptr[2 * (size_t)w + part + 1]; ++v) {
+                const int* u = &new_units[4 * (size_t)v];
+                if (diag_len[(size_t)v].empty()) {
+                    out_units.insert(out_units.end(), {u[0], u[1], u[2], u[3]});
+                    continue;
+                }
+                int a = u[0];
+                for (int n : diag_len[(size_t)v]) {
+                    out_units.insert(out_units.end(), {a, a + n, u[2], 2});
+                    a += n;
+                }
+            }
+        }
+    }
+    out_ptr[2 * (size_t)nwin] = (int)(out_units.size() / 4);
+    win_ptr.swap(out_ptr);
+    units.swap(out_units);
     return true;
 }
 
