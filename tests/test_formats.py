@@ -34,6 +34,23 @@ def _random_coo(n, mean_len, seed, noc=None, empty_frac=0.0):
     return n, noc, rows, cols, vals
 
 
+def _banded_coo(n, offsets, seed, keep=0.9):
+    """Entries on the given diagonals (col - row = offset), each kept with
+    probability `keep`: banded tiles whose diagonals are partly empty."""
+    rng = np.random.default_rng(seed)
+    rows, cols = [], []
+    for d in offsets:
+        r = np.arange(max(0, -d), min(n, n - d))
+        r = r[rng.random(r.size) < keep]
+        rows.append(r)
+        cols.append(r + d)
+    rows = np.concatenate(rows).astype(np.int32)
+    cols = np.concatenate(cols).astype(np.int32)
+    order = np.lexsort((cols, rows))
+    rows, cols = rows[order], cols[order]
+    return n, n, rows, cols, rng.uniform(-1, 1, rows.size)
+
+
 def _crs_of(nor, noc, rows, cols, vals):
     return O.triplet_to_crs(nor, noc, rows.copy(), cols.copy(), vals.copy())
 
@@ -45,6 +62,9 @@ MATS = {
     "random_5000": lambda: _random_coo(5000, 7, 1),
     "random_empty_rows": lambda: _random_coo(3000, 3, 2, empty_frac=0.3),
     "random_rect": lambda: _random_coo(700, 5, 3, noc=1300),
+    # banded tiles: split per diagonal (4 diagonals) or kept whole (5)
+    "banded_4diag": lambda: _banded_coo(40000, (-2, 0, 1, 3), 5),
+    "banded_5diag": lambda: _banded_coo(30000, (-3, -1, 0, 2, 5), 6),
 }
 
 
