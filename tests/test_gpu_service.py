@@ -254,3 +254,45 @@ def test_service_batch_classes_confirmed_by_oracle(svc_mod, precision):
             assert r.iterations >= 2000 and abs(r.residual - res_o) <= 1e-12, (kind, kw, r.residual, res_o)
     assert svc.result(ids[2]).converged and svc.result(ids[4]).converged  # the random classes converge
     svc.close()
+
+
+def test_service_burst_built_beside_a_round(svc_mod):
+    """Requests that arrive while solves are live are built beside the
+    running round, several matrices at a time on host threads, and then join
+    the next round: each result equals the same request served alone, bit
+    for bit, in every source and precision."""
+    t, S = svc_mod
+    A = _positive_random(3000, 6, 11)
+    reqs = [
+        lambda s: s.submit_poisson(60, 40, max_it=96, tol=0.0, precision=t.PREC_F64, x0_seed=1, keep_vector=True),
+        lambda s: s.submit_random(40000, 3, max_it=96, tol=0.0, precision=t.PREC_MIXED, x0_seed=2,
+                                  keep_vector=True),
+        lambda s: s.submit_csr(A, max_it=96, tol=0.0, precision=t.PREC_F32, x0_seed=3, keep_vector=True),
+        lambda s: s.submit_poisson(90, 90, max_it=96, tol=0.0, precision=t.PREC_MIXED, x0_seed=4,
+                                   keep_vector=True),
+        lambda s: s.submit_random(20000, 8, mean_len=6.0, max_it=96, tol=0.0, precision=t.PREC_F64, x0_seed=5,
+                                  keep_vector=True),
+    ]
+
+    def alone(i):
+        svc = S.Service(round_iterations=8)
+        rid = reqs[i](svc)
+        svc.run_until_idle()
+        out = svc.result(rid, want_vector=True)
+        svc.close()
+        return out
+
+    svc = S.Service(round_iterations=8)
+    first = svc.submit_poisson(200, 200, max_it=400, tol=0.0, precision=t.PREC_F64, x0_seed=9)
+    svc.step()  # admits the first request with nothing live
+    svc.step()  # its round runs
+    ids = [f(svc) for f in reqs]  # a burst while it is live
+    svc.run_until_idle()
+    assert svc.result(first).state == S.DONE
+    for i, rid in enumerate(ids):
+        r, u = svc.result(rid, want_vector=True)
+        ra, ua = alone(i)
+        assert r.state == S.DONE and r.iterations == ra.iterations == 96
+        assert r.lambda_ == ra.lambda_ and r.residual == ra.residual
+        assert np.array_equal(u.view(np.uint64), ua.view(np.uint64))
+    svc.close()
