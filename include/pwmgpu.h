@@ -360,6 +360,22 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
                           int64_t* blocks, int64_t* block_row_jumps, int32_t* part_info, uint16_t* row_jump,
                           uint16_t* col_jump, double* data, int32_t* block_nnz, int16_t* row_jump_block,
                           int16_t* col_jump_block);
+/* Layout inspection (no device work; no reference counterpart): the device
+ * copy the CSB (format PWMGPU_FMT_CSB) or CO-H (PWMGPU_FMT_COH, with
+ * `partitions`) kernel reads, for windows of `window` rows (a power of two in
+ * [64, min(beta, 1024)]).  sizes[3] = entries of win_ptr, of units and of
+ * ind / data / col; the arrays are filled when all five pointers are
+ * non-null.  win_ptr[2w], win_ptr[2w+1], win_ptr[2w+2]: window w's first
+ * unit, its first dense unit, the next window's first unit.  units: 4 ints
+ * per unit {lo, hi, c0, kind}: c0 = -1 for the window's flat unit (col holds
+ * each element's global column), else the first column of the unit's x
+ * window; kind 0 = row-major elements, 2 = one element per row (rows
+ * ascending).  ind = row << 16 | column within the block (CSB.hpp:89-91)
+ * or the tile (CO-H); the kernel reads both modulo the window. */
+int pwmgpu_tile_layout_host(int32_t format, int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start,
+                            const int32_t* col_ind, const double* vals, int32_t partitions, int32_t window,
+                            int64_t* sizes, int32_t* win_ptr, int32_t* units, uint32_t* ind, double* data,
+                            int32_t* col);
 
 /* The merge kernels' launch variant the load-time tuner picked for this
  * matrix (prefer_l1: 0 = most resident CTAs, 1 = a smaller shared-memory

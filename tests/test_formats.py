@@ -34,14 +34,16 @@ def _random_coo(n, mean_len, seed, noc=None, empty_frac=0.0):
     return n, noc, rows, cols, vals
 
 
-def _banded_coo(n, offsets, seed, keep=0.9):
+def _banded_coo(n, offsets, seed, keep=0.9, dup=0.0):
     """Entries on the given diagonals (col - row = offset), each kept with
-    probability `keep`: banded tiles whose diagonals are partly empty."""
+    probability `keep`: banded tiles whose diagonals are partly empty.  A
+    fraction `dup` of the entries appears twice (CRS keeps both)."""
     rng = np.random.default_rng(seed)
     rows, cols = [], []
     for d in offsets:
         r = np.arange(max(0, -d), min(n, n - d))
         r = r[rng.random(r.size) < keep]
+        r = np.concatenate([r, r[rng.random(r.size) < dup]])
         rows.append(r)
         cols.append(r + d)
     rows = np.concatenate(rows).astype(np.int32)
@@ -65,6 +67,8 @@ MATS = {
     # banded tiles: split per diagonal (4 diagonals) or kept whole (5)
     "banded_4diag": lambda: _banded_coo(40000, (-2, 0, 1, 3), 5),
     "banded_5diag": lambda: _banded_coo(30000, (-3, -1, 0, 2, 5), 6),
+    # a tridiagonal band with repeated coordinates: its tiles are not split
+    "banded_dups": lambda: _banded_coo(30000, (-1, 0, 1), 7, dup=0.02),
 }
 
 

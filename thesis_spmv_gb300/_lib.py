@@ -108,6 +108,8 @@ SIGNATURES = {
     "pwmgpu_coh_build_host": (C.c_int, [i32, i32, i64, vp, vp, vp, i32, C.POINTER(i32), C.POINTER(i64),
                                         C.POINTER(i64), C.POINTER(i64), vp, vp, vp, vp, vp, vp, vp]),
     "pwmgpu_mv_csr_device_noalloc": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp]),
+    "pwmgpu_tile_layout_host": (C.c_int, [i32, i32, i32, i64, vp, vp, vp, i32, i32, C.POINTER(i64), vp, vp, vp, vp,
+                                          vp]),
 }
 
 

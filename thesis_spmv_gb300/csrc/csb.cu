@@ -597,6 +597,12 @@ bool csb_kernel_layout(const std::vector<uint32_t>& ind, const std::vector<doubl
             std::sort(el.begin(), el.end(), [](const auto& a, const auto& b) {
                 return std::get<0>(a) != std::get<0>(b) ? std::get<0>(a) < std::get<0>(b) : std::get<1>(a) < std::get<1>(b);
             });
+            // a repeated coordinate puts two elements of one row on one
+            // diagonal: such a unit is not one element per row, keep it whole
+            bool dup = false;
+            for (size_t q = 1; q < el.size() && !dup; ++q)
+                dup = std::get<0>(el[q]) == std::get<0>(el[q - 1]) && std::get<1>(el[q]) == std::get<1>(el[q - 1]);
+            if (dup) continue;
             std::vector<int>& len = diag_len[(size_t)v];
             for (size_t q = 0; q < el.size(); ++q) {
                 kind[(size_t)lo + q] = std::get<2>(el[q]);

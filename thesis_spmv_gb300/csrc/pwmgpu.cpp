@@ -1771,6 +1771,49 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
     return PWMGPU_OK;
 }
 
+int pwmgpu_tile_layout_host(int32_t format, int32_t nor, int32_t noc, int64_t nnz, const int32_t* row_start,
+                            const int32_t* col_ind, const double* vals, int32_t partitions, int32_t window,
+                            int64_t* sizes, int32_t* win_ptr, int32_t* units, uint32_t* ind, double* data,
+                            int32_t* col) {
+    TRY(check_sizes(nor, noc, nnz));
+    if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
+    if (format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH) return fail(PWMGPU_ERR_INVALID, "format: CSB or CO-H");
+    if (!row_start || !sizes || (nnz > 0 && (!col_ind || !vals))) return fail(PWMGPU_ERR_INVALID, "null array");
+    int beta = 1024, bits = 0;
+    if (format == PWMGPU_FMT_CSB) csb_params(nor, noc, &beta, &bits);
+    if (window < 64 || window > std::min(beta, 1024) || (window & (window - 1)) != 0)
+        return fail(PWMGPU_ERR_INVALID, "window: a power of two in [64, min(beta, 1024)]");
+    std::vector<uint32_t> eind, kind;
+    std::vector<double> edata, kdata;
+    std::vector<int32_t> blk, kcol;
+    std::vector<int> wp, un;
+    if (format == PWMGPU_FMT_CSB) {
+        csb_build_host(nor, noc, nnz, row_start, col_ind, vals, beta, bits, eind, edata, blk, window, wp, un);
+    } else {
+        std::vector<int32_t> pi, bn;
+        std::vector<uint16_t> rj, cj;
+        std::vector<double> d;
+        std::vector<int16_t> rjb, cjb;
+        std::vector<int> parts, blks;
+        coh_build_host(nor, noc, nnz, row_start, col_ind, vals, std::max(partitions, 1), pi, rj, cj, d, bn, rjb, cjb,
+                       parts, blks);
+        coh_tile_units(nor, noc, nnz, row_start, col_ind, vals, parts, window, eind, edata, wp, un);
+    }
+    if (!csb_kernel_layout(eind, edata, window, wp, un, kind, kdata, kcol))
+        return fail(PWMGPU_ERR_INVALID, "the padded device copy exceeds 32-bit element offsets");
+    sizes[0] = (int64_t)wp.size();
+    sizes[1] = (int64_t)un.size();
+    sizes[2] = (int64_t)kind.size();
+    if (win_ptr && units && ind && data && col) {
+        std::memcpy(win_ptr, wp.data(), sizeof(int32_t) * wp.size());
+        if (!un.empty()) std::memcpy(units, un.data(), sizeof(int32_t) * un.size());
+        std::memcpy(ind, kind.data(), sizeof(uint32_t) * kind.size());
+        std::memcpy(data, kdata.data(), sizeof(double) * kdata.size());
+        std::memcpy(col, kcol.data(), sizeof(int32_t) * kcol.size());
+    }
+    return PWMGPU_OK;
+}
+
 int pwmgpu_launch_config(const pwmgpu_matrix* m, int32_t* prefer_l1, int32_t* grid, int32_t* power_grid,
                          float* tuned_ms) {
     if (!m) return fail(PWMGPU_ERR_INVALID, "null handle");
