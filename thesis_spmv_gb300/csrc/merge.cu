@@ -241,12 +241,34 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         AT xv[IPT];
         gather_subtile<VT, XT, AT, IPT, XCOH, C16, CG>(st, x, xv);
         constexpr bool NORM = MODE == MODE_POWER;
-        if (reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral)
+        const bool general = reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral;
+        if constexpr (MODE == MODE_SCALE && !CG) {
+            // a key-tracking step without a rescale (e == 0, nearly every
+            // step) runs the instance without the rescale in its unrolled
+            // loop: 4096^2 stencil power step 0.2209 -> 0.2171 ms.  (The
+            // L1-bypass instances keep one instance: the split made the
+            // irregular matrix's step 2 % slower.)
+            if (e != 0) {
+                if (general)
+                    finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM, true>(s, st, xv, a.row_start, y, a.carries,
+                                                                                 a.nor, e, crow, cval, hval, ss, &mx);
+                else
+                    finish_subtile<MODE, false, VT, XT, AT, IPT, C16, NORM, true>(s, st, xv, a.row_start, y, a.carries,
+                                                                                  a.nor, e, crow, cval, hval, ss, &mx);
+            } else if (general) {
+                finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM, false>(s, st, xv, a.row_start, y, a.carries,
+                                                                              a.nor, e, crow, cval, hval, ss, &mx);
+            } else {
+                finish_subtile<MODE, false, VT, XT, AT, IPT, C16, NORM, false>(s, st, xv, a.row_start, y, a.carries,
+                                                                               a.nor, e, crow, cval, hval, ss, &mx);
+            }
+        } else if (general) {
             finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
                                                                    crow, cval, hval, ss, &mx);
-        else
+        } else {
             finish_subtile<MODE, false, VT, XT, AT, IPT, C16, NORM>(s, st, xv, a.row_start, y, a.carries, a.nor, e,
                                                                     crow, cval, hval, ss, &mx);
+        }
         // every lane is done with this stage (finish_subtile ends with a warp
         // barrier): refill it with the warp's sub-tile i + NS
         if (lane == 0 && i + NS < n) {

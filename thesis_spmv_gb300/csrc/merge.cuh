@@ -307,8 +307,9 @@ __device__ __forceinline__ void gather_subtile(const unsigned char* st, const XT
 // one predicated FMA per slot.  Without NORM the rows are stored directly
 // (the buffer's extra shared-memory round trip made the plain SpMV ~4 %
 // slower on the 4096^2 Poisson matrix).
+// SC = false: the caller knows e == 0 (no rescale code in the unrolled loop).
 template <int MODE, bool GENERAL, typename VT, typename XT, typename AT, int IPT, bool C16 = false,
-          bool NORM = false>
+          bool NORM = false, bool SC = true>
 __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const AT (&xv)[IPT],
                                                const int32_t* __restrict__ row_start, XT* __restrict__ y,
                                                AT* __restrict__ carries, int nor, int e, int* crow, AT* cval,
@@ -367,7 +368,7 @@ __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const A
             acc = fma((AT)vr[j], xv[j], acc);
             if ((mask >> j) & 1u) {
                 AT v = acc;
-                if (MODE != MODE_SPMV && e != 0) v = scale_pow2(v, e);
+                if (MODE != MODE_SPMV && SC && e != 0) v = scale_pow2(v, e);
                 if (to_head) {
                     hval[lane] = v;
                 } else if (!BUF) {
@@ -409,7 +410,7 @@ __device__ __forceinline__ void finish_subtile(int s, unsigned char* st, const A
             // Lane u completes row a.  If the row began before lane u, lane u
             // left its part in hval[u] and the total is written here.
             if (cu < 0) {
-                const XT t = (XT)(hval[u] + (MODE != MODE_SPMV && e != 0 ? scale_pow2(sum, e) : sum));
+                const XT t = (XT)(hval[u] + (MODE != MODE_SPMV && SC && e != 0 ? scale_pow2(sum, e) : sum));
                 if (!BUF) {
                     y[a] = t;
                     if (NORM && a != open_row) ss = fma((double)t, (double)t, ss);
