@@ -242,12 +242,13 @@ __device__ __forceinline__ bool warp_pass(const MergeArgs<VT, XT, AT>& a, const 
         gather_subtile<VT, XT, AT, IPT, XCOH, C16, CG>(st, x, xv);
         constexpr bool NORM = MODE == MODE_POWER;
         const bool general = reinterpret_cast<const int4*>(st)[1].y & kFlagGeneral;
-        if constexpr (MODE == MODE_SCALE && !CG) {
+        if constexpr (MODE == MODE_SCALE && !CG && !XCOH) {
             // a key-tracking step without a rescale (e == 0, nearly every
             // step) runs the instance without the rescale in its unrolled
             // loop: 4096^2 stencil power step 0.2209 -> 0.2171 ms.  (The
-            // L1-bypass instances keep one instance: the split made the
-            // irregular matrix's step 2 % slower.)
+            // L1-bypass instances and the persistent kernel keep one
+            // instance: the split made the irregular matrix's step 2 % and
+            // the persistent kernel's iteration 6 % slower.)
             if (e != 0) {
                 if (general)
                     finish_subtile<MODE, true, VT, XT, AT, IPT, C16, NORM, true>(s, st, xv, a.row_start, y, a.carries,
