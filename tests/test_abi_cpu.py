@@ -80,3 +80,47 @@ def test_null_arguments_are_rejected():
     assert L.pwmgpu_launch_variant(None, ctypes.byref(v)) == 1
     assert L.pwmgpu_set_launch_variant(None, 0) == 1
     assert L.pwmgpu_set_launch_variant(None, 12) == 1
+
+
+def test_host_builders_reject_malformed_crs():
+    """The host-side builders (CSB, CO-H, the tile layout) index the caller's
+    CRS arrays: row_start not running from 0 to nnz, a decreasing row_start
+    or a column outside [0, noc) give PWMGPU_ERR_INVALID, not a crash."""
+    import numpy as np
+    import thesis_spmv_gb300 as t
+    L = t.lib()
+    nor, noc = 4, 5
+    good_rs = np.array([0, 2, 3, 3, 5], np.int32)
+    good_ci = np.array([0, 4, 1, 2, 3], np.int32)
+    bad = [
+        (np.array([1, 2, 3, 3, 5], np.int32), good_ci),    # does not start at 0
+        (np.array([0, 2, 3, 3, 4], np.int32), good_ci),    # does not end at nnz
+        (np.array([0, 3, 2, 3, 5], np.int32), good_ci),    # decreases
+        (good_rs, np.array([0, 5, 1, 2, 3], np.int32)),    # column == noc
+        (good_rs, np.array([0, -1, 1, 2, 3], np.int32)),   # negative column
+    ]
+    vals = np.ones(5)
+    ind = np.zeros(5, np.uint32)
+    data = np.zeros(5)
+    blk = np.zeros(64, np.int32)
+    part = np.zeros(9 * 2, np.int32)
+    T, nrj, nblk, nrjb = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    sizes = (ctypes.c_int64 * 3)()
+    for rs, ci in [(good_rs, good_ci)] + bad:
+        want = 0 if rs is good_rs and ci is good_ci else 1
+        args = (nor, noc, 5, rs.ctypes.data, ci.ctypes.data, vals.ctypes.data)
+        assert L.pwmgpu_csb_build_host(*args, ind.ctypes.data, data.ctypes.data, blk.ctypes.data) == want
+        assert L.pwmgpu_coh_build_host(*args, 2, ctypes.byref(T), ctypes.byref(nrj), ctypes.byref(nblk),
+                                       ctypes.byref(nrjb), part.ctypes.data, None, None, None, None, None,
+                                       None) == want
+        if want:
+            assert t._lib.last_error()
+    # the tile layout needs at least a 64-row window: same checks on a taller matrix
+    n = 128
+    rs = np.arange(n + 1, dtype=np.int32)
+    ci = np.arange(n, dtype=np.int32)
+    ci_bad = ci.copy()
+    ci_bad[7] = n
+    for c, want in ((ci, 0), (ci_bad, 1)):
+        assert L.pwmgpu_tile_layout_host(1, n, n, n, rs.ctypes.data, c.ctypes.data, np.ones(n).ctypes.data, 1, 64,
+                                         sizes, None, None, None, None, None) == want

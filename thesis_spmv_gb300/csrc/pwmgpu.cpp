@@ -382,6 +382,21 @@ int check_sizes(long long nor, long long noc, long long nnz) {
     if (noc >= (1LL << 31)) return fail(PWMGPU_ERR_INVALID, "noc too large");
     return PWMGPU_OK;
 }
+
+// Host CRS arrays a host-side builder may index: row_start runs from 0 to
+// nnz without decreasing, every column lies in [0, noc).
+static int check_host_crs(int nor, int noc, long long nnz, const int32_t* row_start, const int32_t* col_ind) {
+    if (row_start[0] != 0 || row_start[nor] != nnz)
+        return fail(PWMGPU_ERR_INVALID, "row_start must run from 0 to nnz (got %d..%d, nnz %lld)", row_start[0],
+                    row_start[nor], nnz);
+    for (int i = 0; i < nor; ++i)
+        if (row_start[i + 1] < row_start[i]) return fail(PWMGPU_ERR_INVALID, "row_start decreases at row %d", i);
+    for (long long k = 0; k < nnz; ++k)
+        if (col_ind[k] < 0 || col_ind[k] >= noc)
+            return fail(PWMGPU_ERR_INVALID, "column index %d at nonzero %lld out of range [0,%d)", col_ind[k], k,
+                        noc);
+    return PWMGPU_OK;
+}
 }  // namespace pwmgpu
 namespace {
 
@@ -1723,6 +1738,7 @@ int pwmgpu_csb_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
     if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
     if (!row_start || !blk_ptr || (nnz > 0 && (!col_ind || !vals || !ind || !data)))
         return fail(PWMGPU_ERR_INVALID, "null array");
+    TRY(check_host_crs(nor, noc, nnz, row_start, col_ind));
     int beta = 0, bits = 0;
     csb_params(nor, noc, &beta, &bits);
     std::vector<uint32_t> vi;
@@ -1747,6 +1763,7 @@ int pwmgpu_coh_build_host(int32_t nor, int32_t noc, int64_t nnz, const int32_t* 
     if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
     if (!row_start || !part_info || (nnz > 0 && (!col_ind || !vals)))
         return fail(PWMGPU_ERR_INVALID, "null array");
+    TRY(check_host_crs(nor, noc, nnz, row_start, col_ind));
     std::vector<int32_t> pi, bn;
     std::vector<uint16_t> rj, cj;
     std::vector<double> d;
@@ -1779,6 +1796,7 @@ int pwmgpu_tile_layout_host(int32_t format, int32_t nor, int32_t noc, int64_t nn
     if (nor < 1 || noc < 1) return fail(PWMGPU_ERR_INVALID, "empty matrix");
     if (format != PWMGPU_FMT_CSB && format != PWMGPU_FMT_COH) return fail(PWMGPU_ERR_INVALID, "format: CSB or CO-H");
     if (!row_start || !sizes || (nnz > 0 && (!col_ind || !vals))) return fail(PWMGPU_ERR_INVALID, "null array");
+    TRY(check_host_crs(nor, noc, nnz, row_start, col_ind));
     int beta = 1024, bits = 0;
     if (format == PWMGPU_FMT_CSB) csb_params(nor, noc, &beta, &bits);
     if (window < 64 || window > std::min(beta, 1024) || (window & (window - 1)) != 0)
